@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""Benchmark of the tiled-Cholesky hot path on GB300.
+
+Workload (one step): FP64 tiled Cholesky of an N x N SPD matrix, tile NB, followed by the solve
+of nrhs right-hand sides — N=32768, NB=512, nrhs=1 by default; A = (M+M^T)/2 + N*I with
+M ~ U[-0.5, 0.5) from seed 42 (counter-based generator), b ~ N(0,1) from seed 42.
+
+Metric: effective TFLOP/s = (N^3/3) / (factor + solve time), higher is better.
+  value  — inputs resident in HBM; per-step CUDA events around factor + solve; the 4.4 GB
+           restore of A between steps is outside the events and flushes the 129 MB L2.
+  e2e    — the same step through the C ABI with host buffers: pinned H2D of A and b, factor,
+           solve, D2H of the factor and x, all inside the events.
+  roofline — the persistent flowgraph executor (potrf_dag_f64_kernel) timed alone with events,
+           against the measured cuBLAS FP64 GEMM rate of this GPU.
+  cpu_baseline — the CPU restatement of the flowgraph with OpenBLAS tile kernels on all host
+           cores, on a bounded sample (N=16384).
+
+--impl reference times that CPU restatement (the reference's own PaRSEC build is not available)
+on the same metric. Under torchrun every rank runs an independent replica ("replicas only":
+the tiled factorisation of one matrix on one GPU has no data-parallel split in this build).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--N", type=int, default=32768)
+    p.add_argument("--NB", type=int, default=512)
+    p.add_argument("--nrhs", type=int, default=1)
+    p.add_argument("--cpu-N", type=int, default=16384, help="bounded CPU sample size")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def flops_factor(N):
+    return N ** 3 / 3.0
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling in the background during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------
+def cpu_run(N, NB, reps, nthreads=0):
+    """CPU restatement of the flowgraph (oracle) with OpenBLAS tile kernels; returns seconds per rep."""
+    import numpy as np
+    import oracle
+    ok = oracle.load_openblas()
+    base = oracle.uniform_sym_tiles(N, NB, 42)
+    times = []
+    for _ in range(reps):
+        t = base.copy()
+        t0 = time.perf_counter()
+        st, _, _ = oracle.potrf_tiled(t, N, NB, nthreads=nthreads, use_blas=ok)
+        b = np.random.default_rng(42).standard_normal(N)
+        oracle.potrs_tiled(t, N, NB, b)
+        times.append(time.perf_counter() - t0)
+        assert st == 0
+    return times, ok
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    N = args.cpu_N
+    NB = args.NB
+    times, blas = cpu_run(N, NB, args.warmup + args.steps)
+    t = times[args.warmup:]
+    sec = sum(t) / len(t)
+    val = flops_factor(N) / sec / 1e12
+    cores = cpu_cores()
+    line = {
+        "impl": "reference", "metric": "cholesky_solve_tflops", "value": val, "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "potrf+potrs FP64 N=%d NB=%d nrhs=1 (bounded CPU sample of the N=%d workload)"
+                   % (N, NB, args.N), "N": N, "NB": NB, "nrhs": 1},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": "N=%d NB=%d factor+solve, %s tile kernels, %d threads" %
+                                   (N, NB, "OpenBLAS" if blas else "plain-loop", cores)},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def measure_fp64_gemm_peak(dev):
+    """cuBLAS FP64 GEMM rate on this GPU (the FP64 counterpart of the driver's bf16 peak)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def run_ours(args, ws, rank, local):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import ttg_gb300 as gbx
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    N, NB, nrhs = args.N, args.NB, args.nrhs
+    NTb = (N + min(NB, 128) - 1) // min(NB, 128) if NB > 128 else (N + NB - 1) // NB
+    numel = gbx.tiled_numel(N, NB)
+    A0 = torch.empty(numel, dtype=torch.float64, device=dev)
+    T = torch.empty_like(A0)
+    gbx.gen_uniform_sym(A0, N, NB, seed=42)
+    b_host = torch.from_numpy(np.random.default_rng(42).standard_normal((nrhs, N)))
+    b0 = b_host.to(dev)
+    X = torch.empty_like(b0)
+    work = torch.empty(gbx.potrf_workspace_bytes(N, NB), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    launches_per_step = 1 + 2 * (2 * NTb - 1)
+
+    def step(events):
+        e0, e1, e2 = events
+        e0.record()
+        gbx.call("gbx_dpotrf_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(work.data_ptr()),
+                 work.numel(), sp)
+        e1.record()
+        gbx.call("gbx_dpotrs_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), nrhs, ctypes.c_void_p(X.data_ptr()), N, sp)
+        e2.record()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.warmup + args.steps)]
+    for i in range(args.warmup):
+        T.copy_(A0)
+        X.copy_(b0)
+        step(ev[i])
+    torch.cuda.synchronize()
+    st = gbx.potrf_status(work)
+    assert st == 0, st
+    clocks = ClockSampler(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms, dag_ms = [], []
+    for i in range(args.warmup, args.warmup + args.steps):
+        T.copy_(A0)  # restore A (4.4 GB): also flushes L2 between timed steps
+        X.copy_(b0)
+        step(ev[i])
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    for i in range(args.warmup, args.warmup + args.steps):
+        e0, e1, e2 = ev[i]
+        step_ms.append(e0.elapsed_time(e2))
+        dag_ms.append(e0.elapsed_time(e1))
+    assert gbx.potrf_status(work) == 0
+    ms = max_over_ranks(ws, sum(step_ms) / len(step_ms))
+    value = flops_factor(N) / (ms * 1e-3) / 1e12 * ws
+
+    # solution quality of the last step (backward error through a matvec with the lower tiles)
+    berr = backward_error(gbx, A0, T, X, b0, N, NB, dev)
+
+    line = {
+        "metric": "cholesky_solve_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "potrf+potrs FP64 N=%d NB=%d nrhs=%d" % (N, NB, nrhs), "N": N, "NB": NB,
+                   "nrhs": nrhs, "generator": "(M+M^T)/2 + N*I, M~U[-0.5,0.5) seed 42",
+                   "l2": "inputs 4.4 GB > L2; A restored (4.4 GB copy) between timed steps",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "backward_error": berr,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk,
+    }
+
+    peak = measure_fp64_gemm_peak(dev)
+    dag_s = statistics.mean(dag_ms) * 1e-3
+    achieved = flops_factor(N) / dag_s / 1e12
+    line["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "kernel": "potrf_dag_f64_kernel",
+                        "peak_source": "cuBLAS FP64 GEMM 4096^3 measured in this run (no FP64 entry in the "
+                                       "measured-peaks file)"}
+
+    if not args.no_e2e:
+        line["e2e"] = run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps=max(1, min(args.steps, 2)))
+
+    if rank == 0 and not args.no_cpu:
+        times, blas = cpu_run(args.cpu_N, NB, 2)
+        sec = min(times)
+        line["cpu_baseline"] = {"value": flops_factor(args.cpu_N) / sec / 1e12, "unit": "TFLOP/s",
+                                "cores": cpu_cores(), "kind": "port",
+                                "sample": "N=%d NB=%d factor+solve, best of 2, %s tile kernels" %
+                                          (args.cpu_N, NB, "OpenBLAS" if blas else "plain-loop")}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def backward_error(gbx, A0, T, X, b0, N, NB, dev):
+    """||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) for the first rhs, with A from its lower tiles."""
+    import torch
+    import oracle  # noqa: F401  (tile slot arithmetic only)
+    nt = gbx.ntiles(N, NB)
+    tv = A0.view(-1, NB, NB)
+    x = X[0]
+    r = b0[0].clone()
+    rowsum = torch.zeros(N, dtype=torch.float64, device=dev)
+    for n in range(nt):
+        for m in range(n, nt):
+            s = n * nt - n * (n - 1) // 2 + (m - n)
+            blk = tv[s].T  # (rows of tile m) x (cols of tile n)
+            rm, rn = min(NB, N - m * NB), min(NB, N - n * NB)
+            blk = blk[:rm, :rn]
+            if m == n:
+                full = torch.tril(blk) + torch.tril(blk, -1).T
+                r[m * NB:m * NB + rm] -= full @ x[n * NB:n * NB + rn]
+                rowsum[m * NB:m * NB + rm] += full.abs().sum(1)
+            else:
+                r[m * NB:m * NB + rm] -= blk @ x[n * NB:n * NB + rn]
+                r[n * NB:n * NB + rn] -= blk.T @ x[m * NB:m * NB + rm]
+                rowsum[m * NB:m * NB + rm] += blk.abs().sum(1)
+                rowsum[n * NB:n * NB + rn] += blk.abs().sum(0)
+    return (r.abs().max() / (rowsum.max() * x.abs().max() + b0[0].abs().max())).item()
+
+
+def run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps):
+    import ctypes
+
+    import torch
+    A_host = torch.empty(A0.numel(), dtype=torch.float64, pin_memory=True)
+    A_host.copy_(A0)
+    b_host = torch.empty(b0.shape, dtype=torch.float64, pin_memory=True)
+    b_host.copy_(b0)
+    L_host = torch.empty_like(A_host, pin_memory=True)
+    x_host = torch.empty_like(b_host, pin_memory=True)
+    T = torch.empty_like(A0)
+    X = torch.empty_like(b0)
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    times = []
+    for i in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        T.copy_(A_host, non_blocking=True)
+        X.copy_(b_host, non_blocking=True)
+        gbx.call("gbx_dpotrf_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(work.data_ptr()),
+                 work.numel(), sp)
+        gbx.call("gbx_dpotrs_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), nrhs, ctypes.c_void_p(X.data_ptr()), N, sp)
+        L_host.copy_(T, non_blocking=True)
+        x_host.copy_(X, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        if i > 0:
+            times.append(e0.elapsed_time(e1))
+    assert gbx.potrf_status(work) == 0
+    ms = sum(times) / len(times)
+    del T, X
+    return {"value": flops_factor(N) / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": ms,
+            "h2d_bytes_per_step": A_host.numel() * 8 + b_host.numel() * 8,
+            "d2h_bytes_per_step": L_host.numel() * 8 + x_host.numel() * 8, "steps": reps,
+            "api": "gbx_dpotrf_tiled + gbx_dpotrs_tiled (C ABI) with pinned host buffers"}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,130 @@
+/*
+ * gbx_potrf.h — C ABI of the GB300 (sm_103a) tiled-Cholesky library.
+ *
+ * Plain pointers, sizes and a cudaStream_t passed as void*; no C++ or torch types. Every
+ * function returns an int status:
+ *    0                 success
+ *   >0                 (factorisations) LAPACK-style info: 1-based global index of the first
+ *                      non-positive pivot; the factor is left partially computed
+ *   GBX_ERR_ARG        invalid argument (nothing launched)
+ *   GBX_ERR_CUDA       a CUDA runtime call failed
+ *   GBX_ERR_TIMEOUT    a device-side dependency wait ran out of time (the kernel returned
+ *                      without hanging; the context stays usable)
+ *   GBX_ERR_WORKSPACE  the caller's workspace is too small
+ *
+ * Matrix layouts.
+ *   Tile-major lower storage (the layout of the reference's sym_block_cyclic matrix,
+ *   examples/potrf/pmw.h:52-59 and testing_dpotrf.cc:99-102): NT = ceil(N/NB) tile rows and
+ *   columns; tile (m,n), m >= n, is an NB x NB column-major slot with lda = NB at slot index
+ *   n*NT - n*(n-1)/2 + (m-n). The last tile row/column holds N-(NT-1)*NB valid rows/columns.
+ *   Tile-level calls take ordinary column-major tiles with their leading dimension.
+ *
+ * Streams. Every call is asynchronous on `stream` (NULL = legacy default stream) unless its
+ * comment says otherwise. Statuses written by kernels live in device memory and are read
+ * back by the *_status calls, which synchronise the stream.
+ *
+ * Thread safety. Calls on different streams with disjoint workspaces may run concurrently.
+ * The library keeps no mutable global state besides a per-device cache of launch attributes
+ * guarded by a mutex.
+ */
+#ifndef GBX_POTRF_H
+#define GBX_POTRF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBX_OK 0
+#define GBX_ERR_ARG (-1)
+#define GBX_ERR_CUDA (-2)
+#define GBX_ERR_TIMEOUT (-3)
+#define GBX_ERR_WORKSPACE (-4)
+
+/* Library version and the device architecture it was built for (e.g. 1030). */
+int gbx_version(void);
+int gbx_built_arch(void);
+
+/* Default time limit of one device-side dependency wait, in nanoseconds (default 20 s). A wait
+ * that runs out sets GBX_ERR_TIMEOUT and makes every CTA of the launch return. */
+void gbx_set_wait_timeout_ns(uint64_t ns);
+uint64_t gbx_get_wait_timeout_ns(void);
+
+/* ============================================================================================
+ * Tile kernels: drop-in replacements for the four vendor-library calls of the device bodies
+ * of the potrf flowgraph. FP64, column-major tiles.
+ * ========================================================================================== */
+
+/* Replaces cusolverDnDpotrf_bufferSize (examples/potrf/potrf.h:39-42): bytes of device
+ * workspace gbx_dpotrf_tile needs for an n x n tile. */
+int gbx_dpotrf_tile_bufferSize(int n, int lda, size_t* bytes);
+
+/* Replaces cusolverDnDpotrf(handle, CUBLAS_FILL_MODE_LOWER, n, A, lda, work, lwork, devInfo)
+ * (examples/potrf/potrf.h:62-66): A = L L^T in place, lower triangle only (the strict upper
+ * triangle is not touched). devInfo (device int) receives 0 or the 1-based index of the first
+ * non-positive pivot, exactly as cuSOLVER reports it. */
+int gbx_dpotrf_tile(int n, double* A, int lda, void* work, size_t work_bytes, int* devInfo, void* stream);
+
+/* Replaces cublasDtrsm(handle, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+ * CUBLAS_DIAG_NON_UNIT, m, n, &one, L, ldl, B, ldb) (examples/potrf/potrf.h:292-297):
+ * B := B * L^{-T}, B m x n, L n x n lower. */
+int gbx_dtrsm_rlt_tile(int m, int n, const double* L, int ldl, double* B, int ldb, void* stream);
+
+/* Replaces cublasDsyrk(handle, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, &minus_one, A, lda,
+ * &one, C, ldc) (examples/potrf/potrf.h:422-427): C := C - A A^T on the lower triangle. */
+int gbx_dsyrk_ln_tile(int n, int k, const double* A, int lda, double* C, int ldc, void* stream);
+
+/* Replaces cublasDgemm(handle, CUBLAS_OP_N, CUBLAS_OP_T, m, n, k, &minus_one, A, lda, B, ldb,
+ * &one, C, ldc) (examples/potrf/potrf.h:547-553): C := C - A B^T. */
+int gbx_dgemm_nt_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                      double* C, int ldc, void* stream);
+
+/* ============================================================================================
+ * Whole-flowgraph device executor. One persistent launch runs every POTRF/TRSM/SYRK/GEMM task
+ * of the potrf flowgraph (examples/potrf/potrf.h:670-764) over a tile-major lower matrix: CTAs
+ * take tasks from a device-side ready queue (the flowgraph's keys in a lookahead order) and
+ * wait, with a time limit, on per-block completion counters that encode the flowgraph's
+ * successor rules (potrf.h:112-116, 259-268, 449-457, 578-586). Tiles larger than 128 are
+ * processed as 128 x 128 blocks inside the tile.
+ * Supported NB: any NB <= 128, or a multiple of 32 above that.
+ * ========================================================================================== */
+
+/* Bytes of device workspace gbx_dpotrf_tiled needs. */
+int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes);
+
+/* Factorises the tile-major lower matrix in place (asynchronous). The status is kept in the
+ * workspace; read it with gbx_dpotrf_tiled_status. */
+int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream);
+
+/* Synchronises `stream` and returns the status of the last gbx_dpotrf_tiled on `work`:
+ * 0, >0 (first bad pivot, 1-based global index) or GBX_ERR_TIMEOUT. */
+int gbx_dpotrf_tiled_status(const void* work, void* stream);
+
+/* Solves (L L^T) X = B in place for nrhs right-hand sides (B column-major, N x nrhs, ldb),
+ * using the tile-major factor written by gbx_dpotrf_tiled (asynchronous). */
+int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, int ldb, void* stream);
+
+/* Fills a tile-major lower matrix on the device (asynchronous).
+ * gbx_dplgsy_tiled: the PLASMA generator of the reference (examples/potrf/core_plgsy.h:64-150
+ *   with the LCG of examples/potrf/random.h), bump added to the diagonal, bit-identical to it.
+ * gbx_dgen_uniform_sym_tiled: A = (M + M^T)/2 + shift*I with M_ij uniform in [-0.5, 0.5) from a
+ *   counter-based generator keyed by (seed, i, j). */
+int gbx_dplgsy_tiled(int N, int NB, double bump, unsigned long long seed, double* tiles, void* stream);
+int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double shift, double* tiles,
+                               void* stream);
+
+/* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
+ * task is skipped, so the dependency wait of the second task can never be satisfied and must
+ * run out after `timeout_ns`. Returns the status the kernel reported (GBX_ERR_TIMEOUT when the
+ * time limit works). `work` must hold gbx_dpotrf_tiled_bufferSize(2*NB, NB) bytes, `tiles`
+ * 3 tiles of NB*NB doubles. Synchronises the stream. */
+int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_bytes, uint64_t timeout_ns,
+                             void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBX_POTRF_H */

@@ -1,0 +1,64 @@
+"""CPU tests of the C-ABI boundary: the library loads, exports every symbol its header declares,
+and validates arguments without touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(gbx_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for n in ["gbx_dpotrf_tile", "gbx_dtrsm_rlt_tile", "gbx_dsyrk_ln_tile", "gbx_dgemm_nt_tile",
+              "gbx_dpotrf_tiled", "gbx_dpotrs_tiled"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(gbx):
+    L = gbx.lib()
+    missing = [n for n in declared_symbols() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header(gbx):
+    assert declared_symbols() <= set(gbx.SIGNATURES)
+
+
+def test_built_for_sm103a(gbx):
+    assert gbx.lib().gbx_built_arch() == 1030
+
+
+def test_argument_validation_without_gpu(gbx):
+    L = gbx.lib()
+    sz = ctypes.c_size_t(0)
+    assert L.gbx_dpotrf_tiled_bufferSize(-1, 32, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
+    assert L.gbx_dpotrf_tiled_bufferSize(1000, 200, ctypes.byref(sz)) == gbx.GBX_ERR_ARG  # 200: no block edge
+    assert L.gbx_dpotrf_tiled_bufferSize(32768, 512, ctypes.byref(sz)) == 0
+    ntb = 32768 // 128
+    assert sz.value >= 64 + ntb * (ntb + 1) // 2 * 4
+    assert L.gbx_dpotrf_tiled(100, 0, None, None, 0, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dgemm_nt_tile(10, 10, 10, None, 5, None, 10, None, 10, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dtrsm_rlt_tile(10, 10, None, 10, None, 5, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dpotrs_tiled(100, 32, None, 1, None, 50, None) == gbx.GBX_ERR_ARG
+
+
+def test_wait_timeout_setting(gbx):
+    L = gbx.lib()
+    old = L.gbx_get_wait_timeout_ns()
+    L.gbx_set_wait_timeout_ns(12345)
+    assert L.gbx_get_wait_timeout_ns() == 12345
+    L.gbx_set_wait_timeout_ns(old)

@@ -1,0 +1,290 @@
+"""GPU parity tests of the FP64 path, through the C ABI, against the CPU oracle.
+
+Tolerances (FP64):
+  * generators: bit-exact;
+  * tile kernels: elementwise |C - C_ref| <= 4 k eps (|C0| + |A||B|^T) (the standard GEMM bound);
+  * factorisations: max |L - L_ref| <= 1e-12 max |L_ref| and, elementwise, |L_ij - L_ref_ij| <=
+    1e-12 |L_ref_ij| wherever |L_ref_ij| >= 1e-6 max|L_ref|; residual ||A - L L^T||_F / (N ||A||_F)
+    <= 1e-15 and the reference driver's ||LL^T - A||_inf / (||A||_inf N eps) < 60.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+EPS = np.finfo(np.float64).eps
+
+
+def _vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _s():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def to_dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def colmajor_dev(a, ld, cuda):
+    """numpy (rows x cols) -> CUDA tensor holding it column-major with leading dimension ld."""
+    import torch
+    rows, cols = a.shape
+    buf = np.full((cols, ld), np.nan)
+    buf[:, :rows] = a.T
+    return torch.from_numpy(buf).to(cuda)
+
+
+def from_colmajor(t, rows):
+    return t.cpu().numpy()[:, :rows].T.copy()
+
+
+def assert_factor_close(L, Lref, tol=1e-12):
+    mx = np.max(np.abs(Lref))
+    d = np.abs(L - Lref)
+    assert np.max(d) <= tol * mx, np.max(d) / mx
+    big = np.abs(Lref) >= 1e-6 * mx
+    rel = d[big] / np.abs(Lref[big])
+    assert np.max(rel) <= tol, np.max(rel)
+
+
+# ---- generators --------------------------------------------------------------------------------
+@pytest.mark.parametrize("N,NB", [(160, 32), (1000, 128), (2048, 512)])
+def test_device_plgsy_bit_exact(gbx, cuda, N, NB):
+    import torch
+    t = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.plgsy(t, N, NB, N, 3872)
+    assert np.array_equal(t.cpu().numpy(), oracle.plgsy_tiles(N, NB, N, 3872))
+
+
+@pytest.mark.parametrize("N,NB", [(777, 128), (1024, 512)])
+def test_device_uniform_sym_bit_exact(gbx, cuda, N, NB):
+    import torch
+    t = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(t, N, NB, seed=42)
+    assert np.array_equal(t.cpu().numpy(), oracle.uniform_sym_tiles(N, NB, 42))
+
+
+# ---- tile kernels (drop-ins for the four library calls) ----------------------------------------
+GEMM_SHAPES = [(512, 512, 512), (128, 128, 128), (100, 77, 33), (300, 200, 600), (1, 1, 1), (129, 257, 17)]
+
+
+@pytest.mark.parametrize("m,n,k", GEMM_SHAPES)
+def test_tile_dgemm_nt(gbx, cuda, m, n, k):
+    rng = np.random.default_rng(m * 7 + n * 3 + k)
+    A, B, C = rng.uniform(-1, 1, (m, k)), rng.uniform(-1, 1, (n, k)), rng.uniform(-1, 1, (m, n))
+    lda, ldb, ldc = m + 3, n + 1, m + 5
+    dA, dB, dC = colmajor_dev(A, lda, cuda), colmajor_dev(B, ldb, cuda), colmajor_dev(C, ldc, cuda)
+    gbx.call("gbx_dgemm_nt_tile", m, n, k, _vp(dA), lda, _vp(dB), ldb, _vp(dC), ldc, _s())
+    got = from_colmajor(dC, m)
+    Cref = np.asfortranarray(C.copy())
+    oracle.lib().orc_gemm_nt_tile(m, n, k, oracle._p(np.asfortranarray(A)), m, oracle._p(np.asfortranarray(B)), n,
+                                  oracle._p(Cref), m)
+    bound = 4 * k * EPS * (np.abs(C) + np.abs(A) @ np.abs(B).T)
+    assert np.all(np.abs(got - Cref) <= bound)
+    # padding rows between m and ldc untouched
+    assert np.all(np.isnan(dC.cpu().numpy()[:, m:ldc]))
+
+
+@pytest.mark.parametrize("n,k", [(512, 512), (128, 128), (100, 33), (257, 129)])
+def test_tile_dsyrk_ln(gbx, cuda, n, k):
+    rng = np.random.default_rng(n + k)
+    A, C = rng.uniform(-1, 1, (n, k)), rng.uniform(-1, 1, (n, n))
+    dA, dC = colmajor_dev(A, n, cuda), colmajor_dev(C, n + 2, cuda)
+    gbx.call("gbx_dsyrk_ln_tile", n, k, _vp(dA), n, _vp(dC), n + 2, _s())
+    got = from_colmajor(dC, n)
+    ref = C - A @ A.T
+    bound = 4 * k * EPS * (np.abs(C) + np.abs(A) @ np.abs(A).T)
+    low = np.tril(np.ones((n, n), dtype=bool))
+    assert np.all(np.abs(got - ref)[low] <= bound[low])
+    assert np.array_equal(got[~low], C[~low])  # strict upper untouched
+
+
+def spd(n, seed):
+    return oracle.uniform_sym_full(n, seed)
+
+
+@pytest.mark.parametrize("m,n", [(512, 512), (128, 128), (100, 77), (300, 33), (5, 200)])
+def test_tile_dtrsm_rlt(gbx, cuda, m, n):
+    L = np.linalg.cholesky(spd(n, 5))
+    rng = np.random.default_rng(m + n)
+    B = rng.uniform(-1, 1, (m, n))
+    dL, dB = colmajor_dev(L, n + 1, cuda), colmajor_dev(B, m + 2, cuda)
+    gbx.call("gbx_dtrsm_rlt_tile", m, n, _vp(dL), n + 1, _vp(dB), m + 2, _s())
+    got = from_colmajor(dB, m)
+    ref = np.asfortranarray(B.copy())
+    oracle.lib().orc_trsm_rlt_tile(m, n, oracle._p(np.asfortranarray(L)), n, oracle._p(ref), m)
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("n", [1, 31, 128, 129, 512, 1000])
+def test_tile_dpotrf(gbx, cuda, n):
+    import torch
+    A = spd(n, n)
+    lda = n + 4
+    dA = colmajor_dev(A, lda, cuda)
+    ws = ctypes.c_size_t(0)
+    gbx.call("gbx_dpotrf_tile_bufferSize", n, lda, ctypes.byref(ws))
+    work = torch.empty(ws.value, dtype=torch.uint8, device=cuda)
+    info = torch.full((1,), -7, dtype=torch.int32, device=cuda)
+    gbx.call("gbx_dpotrf_tile", n, _vp(dA), lda, _vp(work), ws.value, _vp(info), _s())
+    assert int(info.item()) == 0
+    got = from_colmajor(dA, n)
+    ref = np.asfortranarray(A.copy())
+    assert oracle.lib().orc_potrf_tile(n, oracle._p(ref), n) == 0
+    assert_factor_close(np.tril(got), np.tril(ref))
+    assert np.array_equal(np.triu(got, 1), np.triu(A, 1))  # upper untouched, like cuSOLVER
+
+
+@pytest.mark.parametrize("n,bad", [(64, 40), (300, 170)])
+def test_tile_dpotrf_reports_pivot(gbx, cuda, n, bad):
+    import torch
+    A = spd(n, 1)
+    A[bad, bad] = -5.0  # makes the leading (bad+1) minor indefinite
+    dA = colmajor_dev(A, n, cuda)
+    ws = ctypes.c_size_t(0)
+    gbx.call("gbx_dpotrf_tile_bufferSize", n, n, ctypes.byref(ws))
+    work = torch.empty(ws.value, dtype=torch.uint8, device=cuda)
+    info = torch.zeros(1, dtype=torch.int32, device=cuda)
+    gbx.call("gbx_dpotrf_tile", n, _vp(dA), n, _vp(work), ws.value, _vp(info), _s())
+    ref = np.asfortranarray(A.copy())
+    assert int(info.item()) == oracle.lib().orc_potrf_tile(n, oracle._p(ref), n) == bad + 1
+
+
+# ---- the whole flowgraph on the device ---------------------------------------------------------
+def run_dag(gbx, cuda, N, NB, tiles_np):
+    import torch
+    t = to_dev(tiles_np, cuda)
+    gbx.potrf_tiled(t, N, NB)
+    return t.cpu().numpy()
+
+
+CASES = [("plgsy", 160, 32), ("plgsy", 1000, 128), ("uniform", 2048, 128), ("uniform", 2048, 512),
+         ("uniform", 1536, 384), ("uniform", 700, 96), ("uniform", 2500, 512), ("uniform", 64, 64)]
+
+
+@pytest.mark.parametrize("gen,N,NB", CASES)
+def test_dag_potrf_matches_oracle(gbx, cuda, gen, N, NB):
+    t0 = oracle.plgsy_tiles(N, NB, N, 3872) if gen == "plgsy" else oracle.uniform_sym_tiles(N, NB, 42)
+    got = run_dag(gbx, cuda, N, NB, t0)
+    ref = t0.copy()
+    if oracle.load_openblas():
+        st, _, _ = oracle.potrf_tiled(ref, N, NB, nthreads=0, use_blas=True)
+    else:
+        st, _, _ = oracle.potrf_tiled(ref, N, NB, nthreads=0)
+    assert st == 0
+    L, Lref = oracle.tiles_to_lower(got, N, NB), oracle.tiles_to_lower(ref, N, NB)
+    assert_factor_close(L, Lref)
+    if N <= 2048:
+        A0 = oracle.tiles_to_lower(t0, N, NB)
+        A0 = A0 + np.tril(A0, -1).T
+        assert oracle.check_dpotrf(L, A0) < 60.0
+        assert oracle.frob_residual(L, A0) <= 1e-15
+
+
+def test_dag_potrf_8192_vs_cpu_oracle(gbx, cuda):
+    # the checked size of the N=32768 configuration
+    N, NB = 8192, 512
+    if not oracle.load_openblas():
+        pytest.skip("OpenBLAS not found for the N=8192 oracle run")
+    t0 = oracle.uniform_sym_tiles(N, NB, 42)
+    got = run_dag(gbx, cuda, N, NB, t0)
+    ref = t0.copy()
+    assert oracle.potrf_tiled(ref, N, NB, nthreads=0, use_blas=True)[0] == 0
+    assert_factor_close(oracle.tiles_to_lower(got, N, NB), oracle.tiles_to_lower(ref, N, NB))
+
+
+def test_dag_reports_first_bad_pivot(gbx, cuda):
+    N, NB = 1000, 128
+    A = oracle.uniform_sym_full(N, 9)
+    A[700, 700] = -1.0
+    t0 = oracle.tiles_from_full(A, NB)
+    ref = t0.copy()
+    st, info, _ = oracle.potrf_tiled(ref, N, NB, nthreads=1)
+    expect = (st - 1) * NB + info
+    assert expect == 701
+    import torch
+    t = to_dev(t0, cuda)
+    with pytest.raises(gbx.NotPositiveDefinite) as e:
+        gbx.potrf_tiled(t, N, NB)
+    assert e.value.info == expect
+
+
+def test_dag_wait_times_out_and_context_survives(gbx, cuda):
+    import torch
+    NB = 32
+    tiles = torch.zeros(3 * NB * NB, dtype=torch.float64, device=cuda)
+    need = gbx.potrf_workspace_bytes(2 * NB, NB)
+    work = torch.empty(need, dtype=torch.uint8, device=cuda)
+    st = gbx.lib().gbx_dag_timeout_selftest(NB, _vp(tiles), _vp(work), need, 200_000_000, _s())
+    assert st == gbx.GBX_ERR_TIMEOUT
+    # the context is still usable
+    t0 = oracle.uniform_sym_tiles(256, 64, 1)
+    got = run_dag(gbx, cuda, 256, 64, t0)
+    ref = t0.copy()
+    oracle.potrf_tiled(ref, 256, 64, nthreads=1)
+    assert_factor_close(got, ref)
+
+
+def test_dag_workspace_too_small(gbx, cuda):
+    import torch
+    t = torch.zeros(gbx.tiled_numel(512, 128), dtype=torch.float64, device=cuda)
+    w = torch.empty(16, dtype=torch.uint8, device=cuda)
+    st = gbx.lib().gbx_dpotrf_tiled(512, 128, _vp(t), _vp(w), 16, _s())
+    assert st == gbx.GBX_ERR_WORKSPACE
+
+
+# ---- solve ---------------------------------------------------------------------------------------
+@pytest.mark.parametrize("N,NB,nrhs", [(1000, 128, 1), (2048, 512, 8), (160, 32, 3)])
+def test_potrs_matches_oracle(gbx, cuda, N, NB, nrhs):
+    import torch
+    A = oracle.uniform_sym_full(N, 42)
+    t0 = oracle.tiles_from_full(A, NB)
+    t = to_dev(t0, cuda)
+    gbx.potrf_tiled(t, N, NB)
+    rng = np.random.default_rng(42)
+    B = rng.standard_normal((nrhs, N))
+    dB = to_dev(B, cuda)
+    gbx.potrs_tiled(t, N, NB, dB)
+    X = dB.cpu().numpy()
+    for r in range(nrhs):
+        x = X[r]
+        berr = np.linalg.norm(A @ x - B[r], np.inf) / (np.linalg.norm(A, np.inf) * np.linalg.norm(x, np.inf)
+                                                      + np.linalg.norm(B[r], np.inf))
+        assert berr <= 1e-15
+    ref_f = t.cpu().numpy()
+    Xref = oracle.potrs_tiled(ref_f, N, NB, B.T.copy())
+    assert np.max(np.abs(X.T - Xref)) <= 1e-12 * np.max(np.abs(Xref))
+
+
+def test_full_size_solve_backward_error(gbx, cuda):
+    """N=16384: size-independent property — the solve's normwise backward error stays at FP64 level."""
+    import torch
+    N, NB = 16384, 512
+    t = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(t, N, NB, seed=42)
+    # dense copy of A for the residual (symmetric from the lower tiles)
+    nt = gbx.ntiles(N, NB)
+    A = torch.empty((N, N), dtype=torch.float64, device=cuda)
+    tv = t.view(-1, NB, NB)
+    for n in range(nt):
+        for m in range(n, nt):
+            s = oracle.tile_slot(m, n, nt)
+            blk = tv[s].T  # tile is column-major: row index fastest
+            A[m * NB:(m + 1) * NB, n * NB:(n + 1) * NB] = blk
+            if m != n:
+                A[n * NB:(n + 1) * NB, m * NB:(m + 1) * NB] = blk.T
+    gbx.potrf_tiled(t, N, NB)
+    g = torch.Generator(device=cuda).manual_seed(42)
+    b = torch.randn(N, dtype=torch.float64, device=cuda, generator=g)
+    x = b.clone()
+    gbx.potrs_tiled(t, N, NB, x)
+    r = A @ x - b
+    berr = (r.abs().max() / (A.abs().sum(1).max() * x.abs().max() + b.abs().max())).item()
+    assert berr <= 1e-15

@@ -1,0 +1,123 @@
+"""CPU tests of the oracle: pinned against the reference's own generator and the golden fixtures,
+cross-checked against numpy, and the restated flowgraph's scheduling rules."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "potrf_golden.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+def test_plgsy_matches_reference_generator_ragged(gold):
+    # bit-exact against examples/potrf/core_plgsy.h compiled from the reference
+    t = oracle.plgsy_tiles(100, 32, 100, 3872)
+    assert np.array_equal(t, gold["plgsy_N100_NB32"])
+
+
+@pytest.mark.parametrize("N,NB", [(160, 32), (1000, 128)])
+def test_plgsy_matches_reference_generator_hash(gold, N, NB):
+    t = oracle.plgsy_tiles(N, NB, N, 3872)
+    h = np.frombuffer(hashlib.sha256(t.tobytes()).digest(), dtype=np.uint8)
+    assert np.array_equal(h, gold["sha256_plgsy_N%d_NB%d" % (N, NB)])
+
+
+def test_uniform_generator_golden(gold):
+    vals = [oracle.lib().orc_uniform_elem(42, int(i), int(j)) for i, j in gold["uniform_seed42_idx"]]
+    assert np.array_equal(np.array(vals), gold["uniform_seed42_val"])
+
+
+def test_uniform_sym_properties():
+    N = 300
+    A = oracle.uniform_sym_full(N, 42)
+    assert np.array_equal(A, A.T)
+    off = A - np.diag(np.diag(A))
+    assert np.abs(off).max() <= 0.5
+    assert np.all(np.abs(np.diag(A) - N) <= 0.5)
+    t = oracle.uniform_sym_tiles(N, 64, 42)
+    assert np.array_equal(oracle.tiles_to_lower(t, N, 64), np.tril(A))
+
+
+def test_factor_golden(gold):
+    t = gold["plgsy_N100_NB32"].copy()
+    st, info, _ = oracle.potrf_tiled(t, 100, 32, nthreads=3)
+    assert st == 0
+    # the flowgraph fixes the update order of every tile, so the factor is bit-reproducible
+    assert np.array_equal(t, gold["factor_N100_NB32"])
+
+
+@pytest.mark.parametrize("N,NB", [(160, 32), (100, 32), (257, 64), (64, 64), (1, 8)])
+def test_oracle_vs_numpy_and_reference_check(N, NB):
+    t = oracle.plgsy_tiles(N, NB, N, 3872)
+    A0 = oracle.tiles_to_lower(t, N, NB)
+    A0 = A0 + np.tril(A0, -1).T
+    st, info, _ = oracle.potrf_tiled(t, N, NB, nthreads=4)
+    assert st == 0
+    L = oracle.tiles_to_lower(t, N, NB)
+    Lr = np.linalg.cholesky(A0)
+    assert np.max(np.abs(L - Lr)) <= 1e-12 * np.max(np.abs(Lr))
+    # the reference driver's acceptance criterion (testing_dpotrf.cc:277-335)
+    assert oracle.check_dpotrf(L, A0) < 60.0
+    assert oracle.frob_residual(L, A0) <= 1e-15
+
+
+def test_oracle_openblas_agrees():
+    if not oracle.load_openblas():
+        pytest.skip("no OpenBLAS shared library next to scipy")
+    N, NB = 520, 128
+    t = oracle.uniform_sym_tiles(N, NB, 42)
+    t2 = t.copy()
+    oracle.potrf_tiled(t, N, NB, nthreads=4, use_blas=False)
+    oracle.potrf_tiled(t2, N, NB, nthreads=4, use_blas=True)
+    assert np.max(np.abs(t - t2)) <= 1e-12 * np.max(np.abs(t))
+
+
+def test_flowgraph_trace_is_a_valid_schedule():
+    N, NB = 8 * 16, 16
+    NT = 8
+    t = oracle.uniform_sym_tiles(N, NB, 7)
+    st, info, tr = oracle.potrf_tiled(t, N, NB, nthreads=3, trace=True)
+    assert st == 0
+    keys = [(int(x) >> 60, (int(x) >> 40) & 0xFFFFF, (int(x) >> 20) & 0xFFFFF, int(x) & 0xFFFFF) for x in tr]
+    assert len(keys) == len(set(keys)) == NT + NT * (NT - 1) + NT * (NT - 1) * (NT - 2) // 6
+    pos = {k: i for i, k in enumerate(keys)}
+    for (ty, a, b, c), i in pos.items():
+        if ty == 1:  # TRSM(M,K) after POTRF(K) and GEMM(M,K,K-1)
+            assert pos[(0, b, 0, 0)] < i
+            if b > 0:
+                assert pos[(3, a, b, b - 1)] < i
+        if ty == 3:  # GEMM(M,N,K) after TRSM(M,K), TRSM(N,K)
+            assert pos[(1, a, c, 0)] < i and pos[(1, b, c, 0)] < i
+
+
+def test_priorities_match_reference_formulas():
+    nt = 10
+    assert oracle.lib().orc_priority(0, nt, 3, 0, 0) == (nt - 3) ** 3
+    assert oracle.lib().orc_priority(1, nt, 5, 2, 0) == (nt - 5) ** 3 + 3 * ((2 * nt) - 2 - 5 - 1) * (5 - 2)
+    assert oracle.lib().orc_priority(2, nt, 2, 5, 0) == (nt - 2) ** 3 + 3 * (2 - 5)
+    assert oracle.lib().orc_priority(3, nt, 7, 4, 1) == (nt - 7) ** 3 + 3 * ((2 * nt) - 7 - 4 - 3) * (7 - 4) + 6 * (7 - 1)
+
+
+def test_non_spd_reports_failing_tile():
+    N, NB = 96, 32
+    A = oracle.uniform_sym_full(N, 3, shift=0.0)  # indefinite
+    t = oracle.tiles_from_full(A, NB)
+    st, info, _ = oracle.potrf_tiled(t, N, NB, nthreads=2)
+    assert st >= 1 and info >= 1
+
+
+def test_potrs_oracle():
+    N, NB = 200, 64
+    A = oracle.uniform_sym_full(N, 42)
+    t = oracle.tiles_from_full(A, NB)
+    oracle.potrf_tiled(t, N, NB, nthreads=2)
+    b = np.random.default_rng(1).standard_normal(N)
+    x = oracle.potrs_tiled(t, N, NB, b)[:, 0]
+    assert np.linalg.norm(A @ x - b) / (np.linalg.norm(A) * np.linalg.norm(x)) < 1e-15

@@ -1,0 +1,814 @@
+// FP64 tiled Cholesky for GB300 (sm_103a): block kernels, the persistent flowgraph executor,
+// the tile-level drop-in entry points, the tiled solve and the device-side generators.
+//
+// FP64 on GB300 runs at ~2 DFMA/clk/SM, so every kernel here is organised to keep the FP64
+// pipe busy (enough independent FMAs per warp, operands staged in shared memory, L2-only loads)
+// and the executor is organised to keep every SM busy (device-side ready queue, lookahead order,
+// fine-grained 128 x 128 blocks, no host round trip per task).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <vector>
+
+#include "gbx_common.cuh"
+#include "gbx_potrf.h"
+
+namespace gbx {
+
+constexpr int kThreads = 256;  // threads per CTA of every FP64 block kernel
+constexpr int kBlk = 128;      // largest block edge handled by one CTA
+constexpr int kKC = 16;        // k-chunk of the GEMM staging
+constexpr int kPW = 32;        // panel width of the TRSM
+
+// ------------------------------------------------------------------------------------------------
+// block GEMM:  C(m x n) := C - A(m x k) * B(n x k)^T   (lower: only i >= j of C is written)
+// 256 threads, each owning an 8 x 8 micro-tile (rows tx+16i, cols ty+16j); k staged through
+// shared memory in double-buffered chunks of 16 with a register prefetch of the next chunk.
+// smem: 2 * 2 * 16 * 128 doubles = 64 KB
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ void op_gemm_nt(const double* __restrict__ A, int lda, const double* __restrict__ B,
+                                           int ldb, double* C, int ldc, int m, int n, int k, bool lower,
+                                           double* sm) {
+  double* As = sm;                       // [2][kKC][kBlk]
+  double* Bs = sm + 2 * kKC * kBlk;      // [2][kKC][kBlk]
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int lrow = tid & 127, lk0 = tid >> 7;
+  double acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0;
+
+  const int nchunks = (k + kKC - 1) / kKC;
+  double ra[8], rb[8];
+  auto gload = [&](int k0) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int kk = k0 + lk0 + 2 * s;
+      ra[s] = (lrow < m && kk < k) ? __ldcg(A + lrow + (long long)kk * lda) : 0.0;
+      rb[s] = (lrow < n && kk < k) ? __ldcg(B + lrow + (long long)kk * ldb) : 0.0;
+    }
+  };
+  auto sstore = [&](int buf) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      As[(buf * kKC + lk0 + 2 * s) * kBlk + lrow] = ra[s];
+      Bs[(buf * kKC + lk0 + 2 * s) * kBlk + lrow] = rb[s];
+    }
+  };
+  if (nchunks > 0) {
+    gload(0);
+    sstore(0);
+    __syncthreads();
+    for (int c = 0; c < nchunks; ++c) {
+      const int buf = c & 1;
+      if (c + 1 < nchunks) gload((c + 1) * kKC);
+      const double* as = As + buf * kKC * kBlk;
+      const double* bs = Bs + buf * kKC * kBlk;
+#pragma unroll
+      for (int kk = 0; kk < kKC; ++kk) {
+        double a[8], b[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = as[kk * kBlk + tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) b[j] = bs[kk * kBlk + ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      if (c + 1 < nchunks) sstore(buf ^ 1);
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int col = ty + 16 * j;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = tx + 16 * i;
+      if (row < m && col < n && (!lower || row >= col)) {
+        double* p = C + row + (long long)col * ldc;
+        __stcg(p, __ldcg(p) - acc[i][j]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------------------
+// block POTRF (lower, n <= 128) in shared memory; right-looking, one column per step.
+// Returns 0 or the 1-based local index of the first non-positive pivot (LAPACK info); the
+// strict upper triangle of A is not touched. smem: 128 * 128 doubles + 1 int.
+// ------------------------------------------------------------------------------------------------
+__device__ int op_potrf(double* A, int lda, int n, double* sm) {
+  double* S = sm;                              // col-major, ld 128
+  int* flag = (int*)(sm + kBlk * kBlk);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) *flag = 0;
+  for (int idx = tid; idx < kBlk * n; idx += kThreads) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    if (i < n && i >= j) S[i + kBlk * j] = __ldcg(A + i + (long long)j * lda);
+  }
+  __syncthreads();
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    if (tid == 0) {
+      const double d = S[j + kBlk * j];
+      if (!(d > 0.0)) *flag = j + 1;
+      else S[j + kBlk * j] = sqrt(d);
+    }
+    __syncthreads();
+    info = *flag;
+    if (info) break;
+    const double djj = S[j + kBlk * j];
+    for (int i = j + 1 + tid; i < n; i += kThreads) S[i + kBlk * j] = S[i + kBlk * j] / djj;
+    __syncthreads();
+    for (int c = j + 1 + warp; c < n; c += kThreads / 32) {
+      const double lcj = S[c + kBlk * j];
+      for (int i = c + lane; i < n; i += 32) S[i + kBlk * c] = fma(-S[i + kBlk * j], lcj, S[i + kBlk * c]);
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < kBlk * n; idx += kThreads) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    if (i < n && i >= j) __stcg(A + i + (long long)j * lda, S[i + kBlk * j]);
+  }
+  __syncthreads();
+  return info;
+}
+
+// ------------------------------------------------------------------------------------------------
+// block TRSM (Right, Lower, Trans, NonUnit): B(m x n) := B * L^{-T}, m <= 128, any n.
+// Column panels of 32: left-looking update of the panel from the already-solved columns (a
+// 128 x 32 x p0 GEMM, 4 x 4 micro-tiles), then each thread solves its own row across the panel.
+// smem: panel 32*128 + X chunk 16*128 + L chunk 16*32 + diagonal 32*32 doubles = 60 KB
+// ------------------------------------------------------------------------------------------------
+__device__ void op_trsm(const double* __restrict__ L, int ldl, double* B, int ldb, int m, int n, double* sm) {
+  double* P = sm;                    // [kPW][128]  panel, P[c*128 + r]
+  double* Xc = P + kPW * kBlk;       // [kKC][128]
+  double* Lc = Xc + kKC * kBlk;      // [kKC][kPW]
+  double* Ld = Lc + kKC * kPW;       // [kPW][kPW]  Ld[c2*32 + c] = L(p0+c, p0+c2)
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  for (int p0 = 0; p0 < n; p0 += kPW) {
+    const int pw = min(kPW, n - p0);
+    for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
+      const int r = idx & (kBlk - 1), c = idx >> 7;
+      P[idx] = (r < m && c < pw) ? __ldcg(B + r + (long long)(p0 + c) * ldb) : 0.0;
+    }
+    for (int idx = tid; idx < kPW * kPW; idx += kThreads) {
+      const int c = idx & 31, c2 = idx >> 5;
+      Ld[idx] = (c < pw && c2 <= c) ? __ldcg(L + (p0 + c) + (long long)(p0 + c2) * ldl) : 0.0;
+    }
+    __syncthreads();
+    if (p0 > 0) {
+      double acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+      for (int k0 = 0; k0 < p0; k0 += kKC) {
+        for (int idx = tid; idx < kKC * kBlk; idx += kThreads) {
+          const int r = idx & (kBlk - 1), kk = idx >> 7;
+          Xc[idx] = (r < m) ? __ldcg(B + r + (long long)(k0 + kk) * ldb) : 0.0;
+        }
+        for (int idx = tid; idx < kKC * kPW; idx += kThreads) {
+          const int c = idx & 31, kk = idx >> 5;
+          Lc[idx] = (c < pw) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kKC; ++kk) {
+          double a[4], b[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) a[i] = Xc[kk * kBlk + tx + 32 * i];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) b[j] = Lc[kk * kPW + ty + 8 * j];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) P[(ty + 8 * j) * kBlk + tx + 32 * i] -= acc[i][j];
+      __syncthreads();
+    }
+    if (tid < m && tid < kBlk) {
+      const int r = tid;
+      for (int c = 0; c < pw; ++c) {
+        double s0 = P[c * kBlk + r], s1 = 0.0;
+        int c2 = 0;
+        for (; c2 + 1 < c; c2 += 2) {
+          s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
+          s1 = fma(-P[(c2 + 1) * kBlk + r], Ld[(c2 + 1) * kPW + c], s1);
+        }
+        if (c2 < c) s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
+        P[c * kBlk + r] = (s0 + s1) / Ld[c * kPW + c];
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
+      const int r = idx & (kBlk - 1), c = idx >> 7;
+      if (r < m && c < pw) __stcg(B + r + (long long)(p0 + c) * ldb, P[idx]);
+    }
+    __syncthreads();
+  }
+}
+
+constexpr size_t kDagSmemBytes = (size_t)kBlk * kBlk * sizeof(double) + 64;  // POTRF dominates
+
+// ------------------------------------------------------------------------------------------------
+// the device-side ready queue: task index -> flowgraph key, in lookahead order
+//   prologue: POTRF(0), TRSM(m,0) m=1..
+//   for k = 0 .. NTb-2:
+//     panel part (column k+1): SYRK(k,k+1), GEMM(m,k+1,k) m>k+1, POTRF(k+1), TRSM(m,k+1) m>k+1
+//     trailing part: for n = k+2..: SYRK(k,n), GEMM(m,n,k) m>n
+// Every task's predecessors come earlier in this order, so CTAs that take tasks in order and
+// wait for their predecessors always make progress.
+// ------------------------------------------------------------------------------------------------
+enum : int { T_POTRF = 0, T_TRSM = 1, T_SYRK = 2, T_GEMM = 3 };
+
+struct TaskKey {
+  int type, a, b, c;
+};
+
+__host__ __device__ __forceinline__ long long seg_prefix(long long k, long long R) {
+  // sum over j < k of seg(j) = 2 r + r (r-1) / 2 with r = R - j
+  const long long s1 = k * R - k * (k - 1) / 2;
+  const long long s2 = k * R * R - R * k * (k - 1) + (k - 1) * k * (2 * k - 1) / 6;
+  return (3 * s1 + s2) / 2;
+}
+
+__host__ __device__ __forceinline__ long long dag_num_tasks(int NTb) {
+  return NTb + seg_prefix(NTb - 1, NTb - 1);
+}
+
+__host__ __device__ inline TaskKey dag_decode(long long t, int NTb) {
+  if (t < NTb) return t == 0 ? TaskKey{T_POTRF, 0, 0, 0} : TaskKey{T_TRSM, (int)t, 0, 0};
+  const long long u = t - NTb, R = NTb - 1;
+  int lo = 0, hi = NTb - 2;  // largest k with seg_prefix(k) <= u
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg_prefix(mid, R) <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  const int k = lo;
+  const long long p = u - seg_prefix(k, R);
+  const int r = NTb - k - 1;
+  if (p == 0) return TaskKey{T_SYRK, k, k + 1, 0};
+  if (p < r) return TaskKey{T_GEMM, k + 1 + (int)p, k + 1, k};
+  if (p == r) return TaskKey{T_POTRF, k + 1, 0, 0};
+  if (p < 2 * (long long)r) return TaskKey{T_TRSM, k + 1 + (int)(p - r), k + 1, 0};
+  const long long pp = p - 2 * (long long)r, q = r - 1;  // trailing columns n = k+2 .. NTb-1
+  int clo = 0, chi = (int)q - 1;                           // largest c with S(c) <= pp
+  while (clo < chi) {
+    const int mid = (clo + chi + 1) >> 1;
+    const long long S = (long long)mid * q - (long long)mid * (mid - 1) / 2;
+    if (S <= pp) clo = mid;
+    else chi = mid - 1;
+  }
+  const long long o = pp - ((long long)clo * q - (long long)clo * (clo - 1) / 2);
+  const int n = k + 2 + clo;
+  if (o == 0) return TaskKey{T_SYRK, k, n, 0};
+  return TaskKey{T_GEMM, n + (int)o, n, k};
+}
+
+struct DagParams {
+  BlockView V;
+  int NTb;
+  long long ntasks;
+  DagState* st;
+  int* cnt;            // packed lower per-block completion counters
+  uint64_t timeout_ns;
+};
+
+// Persistent executor: one CTA per SM takes tasks from the ready queue in order.
+// Counter protocol (writers of block (M,N) in order: GEMM(M,N,0..N-1), then TRSM(M,N); of (M,M):
+// SYRK(0..M-1,M), then POTRF(M)):
+//   POTRF(K):      cnt(K,K) >= K
+//   TRSM(M,K):     cnt(K,K) >= K+1, cnt(M,K) >= K
+//   SYRK(K,M):     cnt(M,K) >= K+1, cnt(M,M) >= K
+//   GEMM(M,N,K):   cnt(M,K) >= K+1, cnt(N,K) >= K+1, cnt(M,N) >= K
+__global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P) {
+  extern __shared__ __align__(16) double smem[];
+  __shared__ long long s_task;
+  __shared__ int s_go;
+  const BlockView& V = P.V;
+  const int NTb = P.NTb;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long t = -1;
+      if (!ld_volatile(&P.st->abort)) t = (long long)atomicAdd(&P.st->head, 1ULL);
+      s_task = (t >= 0 && t < P.ntasks) ? t : -1;
+    }
+    __syncthreads();
+    const long long t = s_task;
+    if (t < 0) break;
+    const TaskKey tk = dag_decode(t, NTb);
+    int* target;
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      switch (tk.type) {
+        case T_POTRF:
+          ok = wait_geq(P.cnt + tri_index(tk.a, tk.a, NTb), tk.a, P.st, P.timeout_ns);
+          break;
+        case T_TRSM:
+          ok = wait_geq(P.cnt + tri_index(tk.b, tk.b, NTb), tk.b + 1, P.st, P.timeout_ns) &&
+               wait_geq(P.cnt + tri_index(tk.a, tk.b, NTb), tk.b, P.st, P.timeout_ns);
+          break;
+        case T_SYRK:
+          ok = wait_geq(P.cnt + tri_index(tk.b, tk.a, NTb), tk.a + 1, P.st, P.timeout_ns) &&
+               wait_geq(P.cnt + tri_index(tk.b, tk.b, NTb), tk.a, P.st, P.timeout_ns);
+          break;
+        default:
+          ok = wait_geq(P.cnt + tri_index(tk.a, tk.c, NTb), tk.c + 1, P.st, P.timeout_ns) &&
+               wait_geq(P.cnt + tri_index(tk.b, tk.c, NTb), tk.c + 1, P.st, P.timeout_ns) &&
+               wait_geq(P.cnt + tri_index(tk.a, tk.b, NTb), tk.c, P.st, P.timeout_ns);
+          break;
+      }
+      s_go = ok;
+    }
+    __syncthreads();
+    if (!s_go) break;
+    switch (tk.type) {
+      case T_POTRF: {
+        const int K = tk.a;
+        const int info = op_potrf(V.ptr(K, K), V.ld, V.dim(K), smem);
+        if (info != 0) {
+          if (threadIdx.x == 0) {
+            atomicCAS(&P.st->status, 0, K * V.b + info);
+            atomicExch(&P.st->abort, 1);
+          }
+          __syncthreads();
+          return;
+        }
+        target = P.cnt + tri_index(K, K, NTb);
+        break;
+      }
+      case T_TRSM: {
+        const int M = tk.a, K = tk.b;
+        op_trsm(V.ptr(K, K), V.ld, V.ptr(M, K), V.ld, V.dim(M), V.dim(K), smem);
+        target = P.cnt + tri_index(M, K, NTb);
+        break;
+      }
+      case T_SYRK: {
+        const int K = tk.a, M = tk.b;
+        const double* a = V.ptr(M, K);
+        op_gemm_nt(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
+        target = P.cnt + tri_index(M, M, NTb);
+        break;
+      }
+      default: {
+        const int M = tk.a, Nn = tk.b, K = tk.c;
+        op_gemm_nt(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn), V.dim(K), false,
+                   smem);
+        target = P.cnt + tri_index(M, Nn, NTb);
+        break;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) signal_done(target);
+  }
+}
+
+// ---- single-purpose grids for the tile-level entry points ------------------------------------
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_nt_grid_kernel(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+                        int lower) {
+  extern __shared__ __align__(16) double smem[];
+  int bi = blockIdx.x, bj = blockIdx.y;
+  if (lower) {  // blockIdx.x enumerates the lower block pairs (bi >= bj)
+    const int t = blockIdx.x;
+    bj = 0;
+    int rem = t;
+    const int nb = (n + kBlk - 1) / kBlk;
+    while (rem >= nb - bj) {
+      rem -= nb - bj;
+      ++bj;
+    }
+    bi = bj + rem;
+  }
+  const int r0 = bi * kBlk, c0 = bj * kBlk;
+  op_gemm_nt(A + r0, lda, B + c0, ldb, C + r0 + (long long)c0 * ldc, ldc, min(kBlk, m - r0), min(kBlk, n - c0), k,
+             lower && bi == bj, smem);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    trsm_rlt_grid_kernel(int m, int n, const double* L, int ldl, double* B, int ldb) {
+  extern __shared__ __align__(16) double smem[];
+  const int r0 = blockIdx.x * kBlk;
+  op_trsm(L, ldl, B + r0, ldb, min(kBlk, m - r0), n, smem);
+}
+
+__global__ void copy_info_kernel(const DagState* st, int* devInfo) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *devInfo = st->status;
+}
+
+__global__ void set_head_kernel(DagState* st, unsigned long long head) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) st->head = head;
+}
+
+// ---- tiled solve: forward (L y = b) and backward (L^T x = y) sweeps over b x b blocks ---------
+// diag solve of one block for all nrhs columns: column-oriented substitution, the columns of L
+// read straight from L2.
+__global__ void __launch_bounds__(kThreads) trsv_diag_kernel(BlockView V, int K, double* X, int ldx, int nrhs,
+                                                             int trans) {
+  __shared__ double xs[kBlk];
+  const int kb = V.dim(K);
+  const double* L = V.ptr(K, K);
+  const long long ld = V.ld;
+  for (int r = 0; r < nrhs; ++r) {
+    double* x = X + (long long)r * ldx + (long long)K * V.b;
+    for (int i = threadIdx.x; i < kb; i += blockDim.x) xs[i] = x[i];
+    __syncthreads();
+    if (!trans) {
+      for (int j = 0; j < kb; ++j) {
+        const double xj = xs[j] / L[j + j * ld];
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = xj;
+        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) xs[i] = fma(-L[i + j * ld], xj, xs[i]);
+        __syncthreads();
+      }
+    } else {
+      for (int j = kb - 1; j >= 0; --j) {
+        const double xj = xs[j] / L[j + j * ld];
+        __syncthreads();
+        if (threadIdx.x == 0) xs[j] = xj;
+        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] = fma(-L[j + i * ld], xj, xs[i]);
+        __syncthreads();
+      }
+    }
+    for (int i = threadIdx.x; i < kb; i += blockDim.x) x[i] = xs[i];
+    __syncthreads();
+  }
+}
+
+// forward update: x_M -= L_MK x_K for every M > K (one CTA per block row M)
+// backward update: x_J -= L_KJ^T x_K for every J < K (one CTA per block column J)
+__global__ void __launch_bounds__(kThreads) trsv_update_kernel(BlockView V, int K, double* X, int ldx, int nrhs,
+                                                               int trans) {
+  __shared__ double xk[kBlk];
+  __shared__ double part[kThreads];
+  const int kb = V.dim(K);
+  if (!trans) {
+    const int M = K + 1 + blockIdx.x;
+    const int mb = V.dim(M);
+    const double* L = V.ptr(M, K);
+    for (int r = 0; r < nrhs; ++r) {
+      const double* xsrc = X + (long long)r * ldx + (long long)K * V.b;
+      for (int i = threadIdx.x; i < kb; i += blockDim.x) xk[i] = xsrc[i];
+      __syncthreads();
+      // rows split over 2 halves of the CTA along k
+      const int row = threadIdx.x & (kBlk - 1), half = threadIdx.x >> 7;
+      double s = 0.0;
+      if (row < mb)
+        for (int c = half; c < kb; c += 2) s = fma(L[row + (long long)c * V.ld], xk[c], s);
+      part[threadIdx.x] = s;
+      __syncthreads();
+      if (half == 0 && row < mb) X[(long long)r * ldx + (long long)M * V.b + row] -= part[row] + part[row + kBlk];
+      __syncthreads();
+    }
+  } else {
+    const int J = blockIdx.x;  // J < K
+    const int jb = V.dim(J);
+    const double* L = V.ptr(K, J);  // kb x jb block, we need L^T
+    for (int r = 0; r < nrhs; ++r) {
+      const double* xsrc = X + (long long)r * ldx + (long long)K * V.b;
+      for (int i = threadIdx.x; i < kb; i += blockDim.x) xk[i] = xsrc[i];
+      __syncthreads();
+      // output index j (column of L_KJ): dot of column j with xk; 2 threads per column? use warps
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int j = warp; j < jb; j += kThreads / 32) {
+        double s = 0.0;
+        for (int i = lane; i < kb; i += 32) s = fma(L[i + (long long)j * V.ld], xk[i], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) X[(long long)r * ldx + (long long)J * V.b + j] -= s;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ---- device generators ----------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long lcg_jump_dev(unsigned long long n, unsigned long long seed) {
+  unsigned long long a = 6364136223846793005ULL, c = 1ULL, x = seed;
+  while (n) {
+    if (n & 1ULL) x = a * x + c;
+    c *= (a + 1);
+    a *= a;
+    n >>= 1;
+  }
+  return x;
+}
+
+__device__ __forceinline__ double plgsy_entry(unsigned long long ran) {
+  // `0.5f - ran * RndF_Mul` evaluated in float, as the reference generator does
+  const float r = __ull2float_rn(ran);
+  const float p = __fmul_rn(r, 5.4210108624275222e-20f);
+  return (double)__fsub_rn(0.5f, p);
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double uniform_elem(uint64_t seed, long long i, long long j) {
+  const uint64_t r = mix64(mix64(seed) ^ (((uint64_t)i << 32) | (uint64_t)(uint32_t)j));
+  return __dsub_rn(__dmul_rn((double)(r >> 11), 1.0 / 9007199254740992.0), 0.5);
+}
+
+// grid: x over the NB*NB elements of a tile, y = tile row m, z = tile column n (m >= n)
+__global__ void gen_tiles_kernel(int N, int NB, int NT, int kind, double bump_or_shift, unsigned long long seed,
+                                 double* tiles) {
+  const int m = blockIdx.y, n = blockIdx.z;
+  if (m < n) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)NB * NB) return;
+  const int i = (int)(e % NB), j = (int)(e / NB);
+  const long long slot = (long long)n * NT - (long long)n * (n - 1) / 2 + (m - n);
+  double* out = tiles + slot * (long long)NB * NB + e;
+  const long long gi = (long long)m * NB + i, gj = (long long)n * NB + j;
+  if (gi >= N || gj >= N) {
+    *out = 0.0;
+    return;
+  }
+  double v;
+  if (kind == 0) {  // PLASMA: lower entries at stream position gi + gj*N, mirrored above
+    const long long hi = gi >= gj ? gi : gj, lo = gi >= gj ? gj : gi;
+    v = plgsy_entry(lcg_jump_dev((unsigned long long)hi + (unsigned long long)lo * (unsigned long long)N, seed));
+    if (gi == gj) v = __dadd_rn(v, bump_or_shift);
+  } else {
+    if (gi == gj) v = __dadd_rn(uniform_elem(seed, gi, gi), bump_or_shift);
+    else v = __dmul_rn(0.5, __dadd_rn(uniform_elem(seed, gi, gj), uniform_elem(seed, gj, gi)));
+  }
+  *out = v;
+}
+
+// ---- host side --------------------------------------------------------------------------------
+struct DevInfo {
+  int sms = 0;
+  int dag_blocks_per_sm = 0;
+  bool attrs_set = false;
+};
+std::mutex g_mtx;
+std::vector<DevInfo> g_dev;
+uint64_t g_timeout_ns = 20ull * 1000 * 1000 * 1000;
+
+int device_info(DevInfo& out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GBX_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if ((int)g_dev.size() <= dev) g_dev.resize(dev + 1);
+  DevInfo& d = g_dev[dev];
+  if (!d.attrs_set) {
+    if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
+    if (cudaFuncSetAttribute(potrf_dag_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kDagSmemBytes) != cudaSuccess)
+      return GBX_ERR_CUDA;
+    if (cudaFuncSetAttribute(gemm_nt_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(4 * kKC * kBlk * sizeof(double))) != cudaSuccess)
+      return GBX_ERR_CUDA;
+    if (cudaFuncSetAttribute(trsm_rlt_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)((kPW * kBlk + kKC * kBlk + kKC * kPW + kPW * kPW) * sizeof(double))) != cudaSuccess)
+      return GBX_ERR_CUDA;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, potrf_dag_f64_kernel, kThreads, kDagSmemBytes) !=
+        cudaSuccess)
+      return GBX_ERR_CUDA;
+    d.dag_blocks_per_sm = std::max(1, occ);
+    d.attrs_set = true;
+  }
+  out = d;
+  return GBX_OK;
+}
+
+// block edge used inside NB x NB tiles: NB itself up to 128, else the largest of 128/64/32 dividing NB
+int block_edge(int NB) {
+  if (NB <= kBlk) return NB;
+  for (int b : {128, 64, 32})
+    if (NB % b == 0) return b;
+  return 0;
+}
+
+size_t dag_workspace_bytes(int NTb) {
+  const size_t counters = (size_t)NTb * (NTb + 1) / 2 * sizeof(int);
+  return sizeof(DagState) + ((counters + 255) / 256) * 256;
+}
+
+int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaStream_t s, long long first_task,
+               uint64_t timeout_ns) {
+  const size_t need = dag_workspace_bytes(NTb);
+  if (work == nullptr || work_bytes < need) return GBX_ERR_WORKSPACE;
+  DevInfo di;
+  if (int e = device_info(di)) return e;
+  if (cudaMemsetAsync(work, 0, need, s) != cudaSuccess) return GBX_ERR_CUDA;
+  DagState* st = (DagState*)work;
+  if (first_task) set_head_kernel<<<1, 32, 0, s>>>(st, (unsigned long long)first_task);
+  DagParams P;
+  P.V = V;
+  P.NTb = NTb;
+  P.ntasks = dag_num_tasks(NTb);
+  P.st = st;
+  P.cnt = (int*)((char*)work + sizeof(DagState));
+  P.timeout_ns = timeout_ns;
+  long long grid = (long long)di.sms * di.dag_blocks_per_sm;
+  grid = std::max(1LL, std::min(grid, P.ntasks));
+  potrf_dag_f64_kernel<<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(P);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+BlockView tiled_view(int N, int NB, double* tiles) {
+  BlockView V;
+  V.base = tiles;
+  V.N = N;
+  V.b = block_edge(NB);
+  V.ld = NB;
+  V.r = NB / V.b;
+  V.NT = (N + NB - 1) / NB;
+  V.tile_elems = (long long)NB * NB;
+  return V;
+}
+
+BlockView plain_view(int n, double* A, int lda) {
+  BlockView V;
+  V.base = A;
+  V.N = n;
+  V.b = n <= kBlk ? std::max(n, 1) : kBlk;
+  V.ld = lda;
+  V.r = 1 << 30;
+  V.NT = 1;
+  V.tile_elems = 0;
+  return V;
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" {
+
+int gbx_version(void) { return 100; }
+int gbx_built_arch(void) {
+#if defined(GBX_ARCH)
+  return GBX_ARCH;
+#else
+  return 0;
+#endif
+}
+
+void gbx_set_wait_timeout_ns(uint64_t ns) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_timeout_ns = ns;
+}
+uint64_t gbx_get_wait_timeout_ns(void) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  return g_timeout_ns;
+}
+
+int gbx_dpotrf_tile_bufferSize(int n, int lda, size_t* bytes) {
+  if (n < 0 || lda < std::max(1, n) || bytes == nullptr) return GBX_ERR_ARG;
+  const int b = n <= kBlk ? std::max(n, 1) : kBlk;
+  const int NTb = (n + b - 1) / b;
+  *bytes = dag_workspace_bytes(std::max(NTb, 1));
+  return GBX_OK;
+}
+
+int gbx_dpotrf_tile(int n, double* A, int lda, void* work, size_t work_bytes, int* devInfo, void* stream) {
+  if (n < 0 || lda < std::max(1, n) || (n > 0 && A == nullptr) || devInfo == nullptr) return GBX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+  const BlockView V = plain_view(n, A, lda);
+  const int NTb = (n + V.b - 1) / V.b;
+  if (int e = launch_dag(V, NTb, work, work_bytes, s, 0, gbx_get_wait_timeout_ns())) return e;
+  copy_info_kernel<<<1, 32, 0, s>>>((const DagState*)work, devInfo);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int gbx_dtrsm_rlt_tile(int m, int n, const double* L, int ldl, double* B, int ldb, void* stream) {
+  if (m < 0 || n < 0 || ldl < std::max(1, n) || ldb < std::max(1, m)) return GBX_ERR_ARG;
+  if (m == 0 || n == 0) return GBX_OK;
+  if (!L || !B) return GBX_ERR_ARG;
+  DevInfo di;
+  if (int e = device_info(di)) return e;
+  const size_t smem = (kPW * kBlk + kKC * kBlk + kKC * kPW + kPW * kPW) * sizeof(double);
+  trsm_rlt_grid_kernel<<<(m + kBlk - 1) / kBlk, kThreads, smem, (cudaStream_t)stream>>>(m, n, L, ldl, B, ldb);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int gbx_dsyrk_ln_tile(int n, int k, const double* A, int lda, double* C, int ldc, void* stream) {
+  if (n < 0 || k < 0 || lda < std::max(1, n) || ldc < std::max(1, n)) return GBX_ERR_ARG;
+  if (n == 0 || k == 0) return GBX_OK;
+  if (!A || !C) return GBX_ERR_ARG;
+  DevInfo di;
+  if (int e = device_info(di)) return e;
+  const int nb = (n + kBlk - 1) / kBlk;
+  const size_t smem = 4 * kKC * kBlk * sizeof(double);
+  gemm_nt_grid_kernel<<<nb * (nb + 1) / 2, kThreads, smem, (cudaStream_t)stream>>>(n, n, k, A, lda, A, lda, C, ldc,
+                                                                                  1);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int gbx_dgemm_nt_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+                      void* stream) {
+  if (m < 0 || n < 0 || k < 0 || lda < std::max(1, m) || ldb < std::max(1, n) || ldc < std::max(1, m))
+    return GBX_ERR_ARG;
+  if (m == 0 || n == 0 || k == 0) return GBX_OK;
+  if (!A || !B || !C) return GBX_ERR_ARG;
+  DevInfo di;
+  if (int e = device_info(di)) return e;
+  const size_t smem = 4 * kKC * kBlk * sizeof(double);
+  dim3 grid((m + kBlk - 1) / kBlk, (n + kBlk - 1) / kBlk);
+  gemm_nt_grid_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(m, n, k, A, lda, B, ldb, C, ldc, 0);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes) {
+  if (N < 0 || NB <= 0 || bytes == nullptr) return GBX_ERR_ARG;
+  const int b = block_edge(NB);
+  if (b == 0) return GBX_ERR_ARG;
+  const int NTb = std::max(1, (N + b - 1) / b);
+  *bytes = dag_workspace_bytes(NTb);
+  return GBX_OK;
+}
+
+int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream) {
+  if (N < 0 || NB <= 0 || block_edge(NB) == 0) return GBX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (N == 0) {
+    if (!work || work_bytes < sizeof(DagState)) return GBX_ERR_WORKSPACE;
+    return cudaMemsetAsync(work, 0, sizeof(DagState), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+  }
+  if (!tiles) return GBX_ERR_ARG;
+  const BlockView V = tiled_view(N, NB, tiles);
+  const int NTb = (N + V.b - 1) / V.b;
+  return launch_dag(V, NTb, work, work_bytes, s, 0, gbx_get_wait_timeout_ns());
+}
+
+int gbx_dpotrf_tiled_status(const void* work, void* stream) {
+  if (!work) return GBX_ERR_ARG;
+  int st = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(&st, work, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
+  return st;
+}
+
+int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, int ldb, void* stream) {
+  if (N < 0 || NB <= 0 || block_edge(NB) == 0 || nrhs < 0 || ldb < std::max(1, N)) return GBX_ERR_ARG;
+  if (N == 0 || nrhs == 0) return GBX_OK;
+  if (!tiles || !B) return GBX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const BlockView V = tiled_view(N, NB, const_cast<double*>(tiles));
+  const int NTb = (N + V.b - 1) / V.b;
+  for (int K = 0; K < NTb; ++K) {
+    trsv_diag_kernel<<<1, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 0);
+    if (K + 1 < NTb) trsv_update_kernel<<<NTb - K - 1, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 0);
+  }
+  for (int K = NTb - 1; K >= 0; --K) {
+    trsv_diag_kernel<<<1, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 1);
+    if (K > 0) trsv_update_kernel<<<K, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 1);
+  }
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+static int gen_tiles(int N, int NB, int kind, double v, unsigned long long seed, double* tiles, void* stream) {
+  if (N < 0 || NB <= 0) return GBX_ERR_ARG;
+  if (N == 0) return GBX_OK;
+  if (!tiles) return GBX_ERR_ARG;
+  const int NT = (N + NB - 1) / NB;
+  if (NT > 65535) return GBX_ERR_ARG;
+  const long long per_tile = (long long)NB * NB;
+  dim3 grid((unsigned)((per_tile + 255) / 256), NT, NT);
+  gen_tiles_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(N, NB, NT, kind, v, seed, tiles);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int gbx_dplgsy_tiled(int N, int NB, double bump, unsigned long long seed, double* tiles, void* stream) {
+  return gen_tiles(N, NB, 0, bump, seed, tiles, stream);
+}
+
+int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double shift, double* tiles, void* stream) {
+  return gen_tiles(N, NB, 1, shift, seed, tiles, stream);
+}
+
+int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_bytes, uint64_t timeout_ns,
+                             void* stream) {
+  if (NB <= 0 || NB > kBlk || !tiles) return GBX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const BlockView V = tiled_view(2 * NB, NB, tiles);
+  // skip task 0 (POTRF(0)): TRSM(1,0) then waits for a counter nothing will ever move
+  if (int e = launch_dag(V, 2, work, work_bytes, s, 1, timeout_ns)) return e;
+  return gbx_dpotrf_tiled_status(work, stream);
+}
+
+}  // extern "C"
