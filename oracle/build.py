@@ -46,6 +46,42 @@ def build_ref(force=False):
     return out
 
 
+def _cuda_inc():
+    for d in ("/usr/local/cuda/include",):
+        if os.path.isdir(d):
+            return d
+    return "/usr/local/cuda/include"
+
+
+def build_ref_flowgraph(force=False):
+    """Compiles the reference's own potrf flowgraph (examples/potrf/potrf.h, plgsy.h, result.h,
+    pmw.h, ../matrixtile.h) and its unmodified driver testing_dpotrf.cc against this project's
+    ttg.h, with the PaRSEC/LAPACK stand-ins of oracle/ref_shim and the oracle's tile kernels.
+    Returns (ref_potrf, testing_dpotrf) paths, or None without a reference checkout."""
+    potrf_dir = os.path.join(REF_ROOT, "examples", "potrf")
+    if not os.path.exists(os.path.join(potrf_dir, "potrf.h")):
+        return None
+    root = os.path.dirname(HERE)
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    common = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-pthread",
+              "-I", os.path.join(HERE, "ref_shim"), "-I", HERE, "-I", os.path.join(root, "include"),
+              "-I", potrf_dir, "-I", os.path.dirname(potrf_dir), "-I", _cuda_inc()]
+    libs = ["-L/usr/local/cuda/lib64", "-lcudart", "-ldl"]
+    deps = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle.h", "ref_potrf_main.cpp", "ref_shim/parsec.h",
+                                            "ref_shim/lapack.hh")]
+    deps += [os.path.join(root, "include", "ttg", f) for f in ("tt.h", "runtime.h", "buffer.h", "device/task.h")]
+    outs = []
+    for name, src in (("ref_potrf", os.path.join(HERE, "ref_potrf_main.cpp")),
+                      ("testing_dpotrf", os.path.join(potrf_dir, "testing_dpotrf.cc"))):
+        out = os.path.join(outdir, name)
+        if force or not _newer(out, deps + [src]):
+            subprocess.check_call(common + [src, os.path.join(HERE, "oracle.cpp"), "-o", out] + libs)
+        outs.append(out)
+    return tuple(outs)
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_flowgraph(force=True))
