@@ -115,6 +115,12 @@ int gbx_dplgsy_tiled(int N, int NB, double bump, unsigned long long seed, double
 int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double shift, double* tiles,
                                void* stream);
 
+/* Replaces CORE_dplgsy (examples/potrf/core_plgsy.h:64-150) for one tile: fills the m x n
+ * column-major tile A (lda) holding rows m0.. and columns n0.. of the gM x gM PLASMA test matrix,
+ * bit-identical to the reference generator (diagonal tiles mirrored and bumped). */
+int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m0, int n0, unsigned long long seed,
+                    void* stream);
+
 /* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
  * task is skipped, so the dependency wait of the second task can never be satisfied and must
  * run out after `timeout_ns`. Returns the status the kernel reported (GBX_ERR_TIMEOUT when the

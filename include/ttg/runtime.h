@@ -196,6 +196,11 @@ class Runtime {
     cv_.notify_all();
     for (auto& t : workers_) t.join();
     workers_.clear();
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      executing_ = false;  // a re-initialised runtime waits for execute() again
+      stop_ = false;
+    }
     if (dev_ready_) {
       for (auto s : streams_) cudaStreamDestroy(s);
       streams_.clear();

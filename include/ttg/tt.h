@@ -90,8 +90,12 @@ using HolderPtr = std::shared_ptr<Holder<V>>;
 
 template <typename V>
 V deep_copy(V& v) {
-  sync_value_to_host(v);  // copy constructors read host data
-  return V(static_cast<const V&>(v));
+  if constexpr (std::is_copy_constructible_v<V>) {
+    sync_value_to_host(v);  // copy constructors read host data
+    return V(static_cast<const V&>(v));
+  } else {
+    throw std::runtime_error("ttg: a move-only value cannot be given to more than one writer");
+  }
 }
 
 // the running task's inputs: a value it sends on is forwarded (same holder), not copied — the
@@ -189,6 +193,8 @@ class TerminalBase {
     name_ = name;
   }
   const std::vector<TerminalBase*>& get_connections() const { return successors_; }
+  const std::vector<TerminalBase*>& get_predecessors() const { return predecessors_; }
+  void add_predecessor(TerminalBase* p) { predecessors_.push_back(p); }
   virtual bool is_input() const = 0;
   bool is_connected() const { return connected_; }
 
@@ -196,7 +202,7 @@ class TerminalBase {
   TTBase* tt_ = nullptr;
   size_t index_ = 0;
   std::string name_;
-  std::vector<TerminalBase*> successors_;
+  std::vector<TerminalBase*> successors_, predecessors_;
   bool connected_ = false;
   friend class TTBase;
 };
@@ -229,6 +235,7 @@ class Out : public TerminalBase {
     successors_.push_back(in);
     connected_ = true;
     in->mark_connected();
+    in->add_predecessor(this);
   }
   size_t nsuccessors() const { return ins_.size(); }
 
@@ -440,25 +447,29 @@ constexpr std::array<int, sizeof...(Values) + 1> input_arg_positions() {
   return pos;
 }
 
+template <typename Args, int Pos>
+constexpr bool arg_mutable_at() {
+  if constexpr (Pos < 0) return true;
+  else if constexpr ((size_t)Pos < std::tuple_size_v<Args>) return arg_is_mutable<std::tuple_element_t<(size_t)Pos, Args>>;
+  else return true;
+}
+
+template <typename Func, bool VoidKey, typename... Values, size_t... I>
+constexpr std::array<bool, sizeof...(Values) + 1> input_mutability_impl(std::index_sequence<I...>) {
+  using args = typename memfn_args<decltype(&std::decay_t<Func>::operator())>::type;
+  constexpr auto pos = input_arg_positions<VoidKey, Values...>();
+  return std::array<bool, sizeof...(Values) + 1>{arg_mutable_at<args, pos[I]>()..., true};
+}
+
 template <typename Func, bool VoidKey, typename... Values>
 constexpr std::array<bool, sizeof...(Values) + 1> input_mutability() {
-  std::array<bool, sizeof...(Values) + 1> mut{};
   if constexpr (!is_generic<Func>::value) {
-    using args = typename memfn_args<decltype(&std::decay_t<Func>::operator())>::type;
-    constexpr auto pos = input_arg_positions<VoidKey, Values...>();
-    [&]<size_t... I>(std::index_sequence<I...>) {
-      ((mut[I] = [&] {
-         if constexpr (pos[I] < 0) return true;
-         else if constexpr ((size_t)pos[I] < std::tuple_size_v<args>)
-           return arg_is_mutable<std::tuple_element_t<(size_t)pos[I], args>>;
-         else return true;
-       }()),
-       ...);
-    }(std::make_index_sequence<sizeof...(Values)>{});
+    return input_mutability_impl<Func, VoidKey, Values...>(std::make_index_sequence<sizeof...(Values)>{});
   } else {
-    for (size_t i = 0; i < sizeof...(Values); ++i) mut[i] = true;  // generic: bind inputs as rvalues
+    std::array<bool, sizeof...(Values) + 1> mut{};
+    for (size_t i = 0; i < sizeof...(Values) + 1; ++i) mut[i] = true;  // generic: bind inputs as rvalues
+    return mut;
   }
-  return mut;
 }
 }  // namespace detail
 
@@ -886,17 +897,20 @@ auto make_ttg(std::vector<std::unique_ptr<TTBase>>&& ops, const InsTuple& ins, c
 }
 
 namespace detail {
+// every TT reachable through predecessors and successors (ttg/ttg/traverse.h:29-100)
 inline void collect(TTBase* tt, std::set<TTBase*>& seen) {
   if (!tt || !seen.insert(tt).second) return;
   for (auto* o : tt->get_ops()) collect(o, seen);
+  for (auto* in : tt->get_inputs_base())
+    for (auto* pred : in->get_predecessors()) collect(pred->get_tt(), seen);
   for (auto* out : tt->get_outputs_base())
     for (auto* succ : out->get_connections()) collect(succ->get_tt(), seen);
-  for (auto* in : tt->get_inputs_base()) (void)in;
 }
 }  // namespace detail
 
-/// Makes every TT reachable from the given ones executable (ttg/ttg/func.h:78-87). Returns true
-/// when every reachable input terminal is connected.
+/// Makes every TT reachable from the given ones executable (ttg/ttg/func.h:78-87). Like the
+/// reference's traversal it returns false, and names the terminal, when a reachable input or
+/// output terminal is not connected.
 template <typename... TTs>
 bool make_graph_executable(TTs*... tts) {
   std::set<TTBase*> seen;
@@ -904,7 +918,25 @@ bool make_graph_executable(TTs*... tts) {
   bool connected = true;
   for (auto* t : seen) {
     t->make_executable();
-    for (auto* in : t->get_inputs_base()) connected = connected && in->is_connected();
+    if (t->is_composite()) continue;
+    int i = 0;
+    for (auto* in : t->get_inputs_base()) {
+      if (!in->is_connected()) {
+        std::cout << "ttg::Traverse: " << t->get_name() << " input terminal #" << i << " " << in->get_name()
+                  << " is not connected\n";
+        connected = false;
+      }
+      ++i;
+    }
+    i = 0;
+    for (auto* out : t->get_outputs_base()) {
+      if (!out->is_connected()) {
+        std::cout << "ttg::Traverse: " << t->get_name() << " output terminal #" << i << " " << out->get_name()
+                  << " is not connected\n";
+        connected = false;
+      }
+      ++i;
+    }
   }
   return connected;
 }

@@ -62,5 +62,26 @@ def build(force=False, verbose=False):
     return LIB
 
 
+DRIVER_SRC = os.path.join(HERE, "potrf", "testing_dpotrf.cc")
+DRIVER = os.path.join(HERE, "potrf", "testing_dpotrf")
+
+
+def build_driver(force=False):
+    """The potrf flowgraph driver on the TTG API (C++ host code linked to libgbx_potrf.so)."""
+    lib = build()
+    deps = [DRIVER_SRC, lib, os.path.join(HERE, "potrf", "potrf.h"), os.path.join(HERE, "potrf", "matrix.h")]
+    deps += glob.glob(os.path.join(INCLUDE, "ttg", "*.h")) + glob.glob(os.path.join(INCLUDE, "ttg", "*", "*.h"))
+    if force or _stale(DRIVER, deps):
+        cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))) if os.path.isabs(nvcc()) else "/usr/local/cuda"
+        cmd = ["g++", "-std=c++20", "-O2", "-pthread", "-I", INCLUDE, "-I", os.path.join(HERE, "potrf"),
+               "-I", os.path.join(cuda, "include"), DRIVER_SRC, "-o", DRIVER, "-L", HERE, "-lgbx_potrf",
+               "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + HERE]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return DRIVER
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose=True))
+    print(build_driver(force=True))

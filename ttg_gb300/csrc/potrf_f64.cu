@@ -554,6 +554,19 @@ __global__ void gen_tiles_kernel(int N, int NB, int NT, int kind, double bump_or
   *out = v;
 }
 
+// one tile of the PLASMA generator: x over the m*n elements
+__global__ void plgsy_tile_kernel(double bump, int m, int n, double* A, int lda, int gM, int m0, int n0,
+                                  unsigned long long seed) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)m * n) return;
+  const int i = (int)(e % m), j = (int)(e / m);
+  const long long gi = (long long)m0 + i, gj = (long long)n0 + j;
+  const long long hi = gi >= gj ? gi : gj, lo = gi >= gj ? gj : gi;
+  double v = plgsy_entry(lcg_jump_dev((unsigned long long)hi + (unsigned long long)lo * (unsigned long long)gM, seed));
+  if (gi == gj) v = __dadd_rn(v, bump);
+  A[i + (long long)j * lda] = v;
+}
+
 // ---- host side --------------------------------------------------------------------------------
 struct DevInfo {
   int sms = 0;
@@ -799,6 +812,17 @@ int gbx_dplgsy_tiled(int N, int NB, double bump, unsigned long long seed, double
 
 int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double shift, double* tiles, void* stream) {
   return gen_tiles(N, NB, 1, shift, seed, tiles, stream);
+}
+
+int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m0, int n0, unsigned long long seed,
+                    void* stream) {
+  if (m < 0 || n < 0 || lda < std::max(1, m) || m0 < 0 || n0 < 0 || gM < 0) return GBX_ERR_ARG;
+  if (m == 0 || n == 0) return GBX_OK;
+  if (!A) return GBX_ERR_ARG;
+  const long long total = (long long)m * n;
+  plgsy_tile_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(bump, m, n, A, lda, gM, m0, n0,
+                                                                                       seed);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
 int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_bytes, uint64_t timeout_ns,
