@@ -121,6 +121,18 @@ int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double sh
 int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m0, int n0, unsigned long long seed,
                     void* stream);
 
+/* ============================================================================================
+ * Tensor-core building block (tcgen05, sm_103a)
+ * ========================================================================================== */
+
+/* D := A * B^T in fp32 on the 5th-generation tensor cores: A is M x K and B is N x K, both bf16
+ * and K-major (row-major, leading dimensions lda/ldb multiples of 8, 16-byte aligned), D is
+ * column-major M x N (ldd). No reference counterpart: this is the low-precision contraction the
+ * mixed-precision factorisation is built on, exposed for testing and reuse. `status` (device int,
+ * may be NULL) receives GBX_ERR_TIMEOUT if a pipeline wait ran out of time. */
+int gbx_gemm_bf16_nt_f32(int M, int N, int K, const void* A, int lda, const void* B, int ldb, float* D, int ldd,
+                         int* status, void* stream);
+
 /* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
  * task is skipped, so the dependency wait of the second task can never be satisfied and must
  * run out after `timeout_ns`. Returns the status the kernel reported (GBX_ERR_TIMEOUT when the

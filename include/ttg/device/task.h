@@ -224,6 +224,7 @@ template <typename TTT>
 struct DeviceDriver {
   using Handle = std::coroutine_handle<device::detail::promise_type>;
   TTT* tt;
+  typename TTT::key_store key{};  // the body holds `const Key&` across suspensions: keep it alive here
   std::function<void()> release;  // releases the task's inputs and its runtime count
   device::Task task;
   cudaStream_t stream = nullptr;
@@ -344,9 +345,10 @@ void TT<Space, Key, Func, OutTerms, Values...>::run_task(const key_store& k, std
       release_inputs(*sp);
       rt::Runtime::get().done();
     };
+    drv->key = k;
     try {
       detail::tl_outputs() = &out_ptrs_;
-      drv->task = call_body(k, *sp);  // runs until the first suspension (select / wait / send)
+      drv->task = call_body(drv->key, *sp);  // runs until the first suspension (select / wait / send)
       detail::tl_outputs() = nullptr;
     } catch (...) {
       detail::tl_outputs() = nullptr;

@@ -443,7 +443,7 @@ constexpr std::array<int, sizeof...(Values) + 1> input_arg_positions() {
   std::array<int, sizeof...(Values) + 1> pos{};
   constexpr bool isvoid[] = {std::is_void_v<Values>..., false};
   int a = VoidKey ? 0 : 1;
-  for (size_t i = 0; i < sizeof...(Values); ++i) pos[i] = isvoid[i] ? -1 : a++;
+  for (size_t i = 0; i + 1 < sizeof...(Values) + 1; ++i) pos[i] = isvoid[i] ? -1 : a++;
   return pos;
 }
 
@@ -478,7 +478,11 @@ template <ExecutionSpace Space, typename Key, typename Func, typename OutTerms, 
 class TT : public TTBase {
   static constexpr size_t numins = sizeof...(Values);
   static constexpr bool void_key = std::is_void_v<Key>;
+
+ public:
   using key_store = std::conditional_t<void_key, int, Key>;
+
+ private:
   template <size_t I>
   using value_t = std::tuple_element_t<I, std::tuple<Values...>>;
   static constexpr auto kMut = detail::input_mutability<Func, void_key, Values...>();

@@ -51,6 +51,7 @@ SIGNATURES = {
     "gbx_dgen_uniform_sym_tiled": (_i, [_i, _i, _ull, _d, _vp, _vp]),
     "gbx_dplgsy_tile": (_i, [_d, _i, _i, _vp, _i, _i, _i, _i, _ull, _vp]),
     "gbx_dag_timeout_selftest": (_i, [_i, _vp, _vp, _sz, _u64, _vp]),
+    "gbx_gemm_bf16_nt_f32": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp]),
 }
 
 
