@@ -42,6 +42,7 @@ extern "C" {
 #define GBX_ERR_CUDA (-2)
 #define GBX_ERR_TIMEOUT (-3)
 #define GBX_ERR_WORKSPACE (-4)
+#define GBX_ERR_NOCONV (-5)
 
 /* Library version and the device architecture it was built for (e.g. 1030). */
 int gbx_version(void);
@@ -115,6 +116,12 @@ int gbx_dplgsy_tiled(int N, int NB, double bump, unsigned long long seed, double
 int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double shift, double* tiles,
                                void* stream);
 
+/* A = Q diag(lam) Q^T on the device, Q = I - U V^T the compact-WY form of a product of r <= 8
+ * Householder reflectors (U, V column-major N x r, G = V^T diag(lam) V column-major r x r; all
+ * device pointers). The generator of the ill-conditioned (kappa = max lam / min lam) workloads. */
+int gbx_dgen_lowrank_sym_tiled(int N, int NB, const double* lam, const double* U, const double* V, const double* G,
+                               int r, double* tiles, void* stream);
+
 /* Replaces CORE_dplgsy (examples/potrf/core_plgsy.h:64-150) for one tile: fills the m x n
  * column-major tile A (lda) holding rows m0.. and columns n0.. of the gM x gM PLASMA test matrix,
  * bit-identical to the reference generator (diagonal tiles mirrored and bumped). */
@@ -132,6 +139,61 @@ int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m
  * may be NULL) receives GBX_ERR_TIMEOUT if a pipeline wait ran out of time. */
 int gbx_gemm_bf16_nt_f32(int M, int N, int K, const void* A, int lda, const void* B, int ldb, float* D, int ldd,
                          int* status, void* stream);
+
+/* ============================================================================================
+ * Mixed precision: low-precision tensor-core factorisation + FP64 refinement. No counterpart in
+ * the reference (which has no solve and no mixed precision); built on the same flowgraph.
+ * ========================================================================================== */
+
+/* Precision of the off-diagonal tensor-core operands. */
+#define GBX_PREC_BF16 0
+#define GBX_PREC_FP16 1
+
+/* Bytes of workspace gbx_potrf_mixed needs (NB a multiple of 256, at most 1024). */
+int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes);
+
+/* Low-precision Cholesky of the FP64 tile-major lower matrix A into the FP32 tile-major factor W
+ * (same layout): diagonal POTRF and TRSM in FP32, SYRK/GEMM updates on the tensor cores with
+ * bf16/fp16 operands scaled per row by powers of two and FP32 accumulation. The diagonal of A is
+ * multiplied by (1 + shift) first (0 for none). Asynchronous; the status (0, first bad pivot, or
+ * GBX_ERR_TIMEOUT) and the largest diagonal-tile condition estimate come from
+ * gbx_potrf_mixed_info, which synchronises the stream. */
+int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work, size_t work_bytes,
+                    void* stream);
+int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, void* stream);
+
+/* Inverses of the FP32 diagonal factor tiles: Inv holds NT tiles of NB*NB floats, tile K =
+ * L_KK^{-T} column-major. */
+int gbx_spotri_diag(int N, int NB, const float* W, float* Inv, void* stream);
+
+/* Z := (W W^T)^{-1} R for nrhs <= 16 column-major FP64 right-hand sides (FP32 arithmetic inside);
+ * tmp holds 2*N*nrhs floats. */
+int gbx_sprecond(int N, int NB, const float* W, const float* Inv, int nrhs, const double* R, double* Z, float* tmp,
+                 void* stream);
+
+/* Y := alpha A X + beta Y in FP64 with A symmetric, stored as FP64 tile-major lower tiles;
+ * X and Y column-major N x nrhs (nrhs <= 16). */
+int gbx_dsymm_tiled(int N, int NB, const double* A, int nrhs, double alpha, const double* X, double beta, double* Y,
+                    void* stream);
+
+typedef struct gbx_refine_info {
+  int iterations;        /* preconditioned CG iterations */
+  int factor_retries;    /* low-precision factorisations repeated with a larger diagonal shift */
+  double shift;          /* diagonal shift of the factorisation that succeeded */
+  double backward_error; /* max over right-hand sides of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) */
+  double anorm;          /* ||A||_inf */
+  float cond_estimate;   /* largest diagonal-tile condition estimate seen by the factorisation */
+} gbx_refine_info;
+
+/* Bytes of workspace gbx_dposv_mixed needs. */
+int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes);
+
+/* Solves A X = B (A FP64 tile-major lower, B and X column-major N x nrhs, nrhs <= 16) to the FP64
+ * backward error `tol`: low-precision factorisation into W, then CG in FP64 preconditioned by W.
+ * Synchronises the stream. Returns 0, a positive pivot index if every shifted factorisation broke
+ * down, GBX_ERR_NOCONV if `maxiter` iterations did not reach `tol`, or another error. */
+int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec, double tol,
+                    int maxiter, float* W, void* work, size_t work_bytes, gbx_refine_info* info, void* stream);
 
 /* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
  * task is skipped, so the dependency wait of the second task can never be satisfied and must

@@ -269,7 +269,15 @@ struct DeviceDriver {
           continue;
         }
         case device::detail::State::WaitKernel: {
-          for (auto& r : pr.wait_refs) r.st->to_host_async(stream);
+          for (auto& r : pr.wait_refs) {
+            // a buffer this task holds mutably may have been changed by any kernel since select
+            for (auto& t : touched)
+              if (t.st == r.st && !t.is_const) {
+                r.st->mark_device_written();
+                break;
+              }
+            r.st->to_host_async(stream);
+          }
           pr.wait_refs.clear();
           rt::Runtime::get().when_stream_done(stream, prio, [self]() {
             self->set_current();

@@ -1,0 +1,97 @@
+"""GPU tests of the mixed-precision path (tensor-core low-precision factorisation + FP64
+refinement), through the C ABI.
+
+Tolerances:
+  * factor: max |W - L64| / max |L64| <= 3e-2 (bf16 operands, unit roundoff 2^-8 x growth) and
+    <= 4e-3 (fp16, 2^-11), L64 from the CPU oracle;
+  * solve: the spec bar, normwise backward error max_j ||b_j - A x_j||_inf /
+    (||A||_inf ||x_j||_inf + ||b_j||_inf) <= 1e-14, and the forward error against an FP64 solve of
+    the same system bounded by kappa(A) * 1e-14.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from ttg_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def dense_from_tiles(t, N, NB):
+    L = oracle.tiles_to_lower(t, N, NB)
+    return L + np.tril(L, -1).T
+
+
+@pytest.mark.parametrize("N,NB,prec,tol", [(2048, 512, "bf16", 3e-2), (2048, 512, "fp16", 4e-3),
+                                           (1800, 256, "bf16", 3e-2), (1024, 256, "fp16", 4e-3)])
+def test_mixed_factor_close_to_fp64(gbx, cuda, N, NB, prec, tol):
+    import torch
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=42)
+    W, work, st, cond = gbx.potrf_mixed(A, N, NB, prec=prec)
+    assert st == 0
+    ref = A.cpu().numpy().copy()
+    oracle.load_openblas()
+    assert oracle.potrf_tiled(ref, N, NB, nthreads=0, use_blas=oracle.lib().orc_blas_loaded())[0] == 0
+    Lw = oracle.tiles_to_lower(W.double().cpu().numpy(), N, NB)
+    L64 = oracle.tiles_to_lower(ref, N, NB)
+    err = np.abs(Lw - L64).max() / np.abs(L64).max()
+    assert err <= tol, err
+    assert 1.0 <= cond < 10.0  # diagonally dominant tiles
+
+
+def solve_and_check(gbx, cuda, A, N, NB, nrhs, prec, kappa):
+    import torch
+    Bn = workloads.rhs(N, nrhs, seed=42)
+    B = torch.from_numpy(Bn).to(cuda)
+    X, info, st = gbx.dposv_mixed(A, N, NB, B, prec=prec, tol=1e-14, maxiter=300)
+    assert st == 0, info
+    assert info["backward_error"] <= 1e-14, info
+    Ad = dense_from_tiles(A.cpu().numpy(), N, NB)
+    Xn = X.cpu().numpy()
+    # independent backward error on the host
+    for j in range(nrhs):
+        r = Bn[j] - Ad @ Xn[j]
+        be = np.abs(r).max() / (np.abs(Ad).sum(1).max() * np.abs(Xn[j]).max() + np.abs(Bn[j]).max())
+        assert be <= 1.5e-14, be
+    Xref = np.linalg.solve(Ad, Bn.T).T
+    fe = np.abs(Xn - Xref).max() / np.abs(Xref).max()
+    assert fe <= kappa * 1e-14, fe
+    return info
+
+
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_dposv_mixed_well_conditioned(gbx, cuda, prec):
+    import torch
+    N, NB = 3000, 512
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=42)
+    info = solve_and_check(gbx, cuda, A, N, NB, 8, prec, kappa=10.0)
+    assert info["iterations"] <= 10, info
+
+
+@pytest.mark.parametrize("kappa,prec", [(1e4, "bf16"), (1e6, "bf16"), (1e6, "fp16")])
+def test_dposv_mixed_householder(gbx, cuda, kappa, prec):
+    N, NB = 2048, 512
+    A = workloads.householder_tiles(N, NB, 4, kappa, 42, cuda)
+    Ad = dense_from_tiles(A.cpu().numpy(), N, NB)
+    Aref = workloads.householder_dense(N, 4, kappa, seed=42)
+    assert np.abs(Ad - Aref).max() <= 1e-14  # device generator against the reflector products
+    solve_and_check(gbx, cuda, A, N, NB, 8, prec, kappa=kappa)
+
+
+def test_dsymm_tiled_matches_dense(gbx, cuda):
+    import ctypes
+    import torch
+    N, NB, nrhs = 1100, 256, 3
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=5)
+    X = torch.randn(nrhs, N, dtype=torch.float64, device=cuda)
+    Y = torch.randn(nrhs, N, dtype=torch.float64, device=cuda)
+    Y0 = Y.clone()
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    gbx.call("gbx_dsymm_tiled", N, NB, ctypes.c_void_p(A.data_ptr()), nrhs, -1.0, ctypes.c_void_p(X.data_ptr()), 2.0,
+             ctypes.c_void_p(Y.data_ptr()), s)
+    Ad = torch.from_numpy(dense_from_tiles(A.cpu().numpy(), N, NB)).to(cuda)
+    ref = 2.0 * Y0 - (Ad @ X.T).T
+    assert (Y - ref).abs().max().item() <= 1e-12 * ref.abs().max().item()

@@ -18,9 +18,12 @@ GBX_ERR_ARG = -1
 GBX_ERR_CUDA = -2
 GBX_ERR_TIMEOUT = -3
 GBX_ERR_WORKSPACE = -4
+GBX_ERR_NOCONV = -5
+PREC = {"bf16": 0, "fp16": 1}
 
 _ERRNAMES = {GBX_ERR_ARG: "invalid argument", GBX_ERR_CUDA: "CUDA runtime error",
-             GBX_ERR_TIMEOUT: "device-side wait timed out", GBX_ERR_WORKSPACE: "workspace too small"}
+             GBX_ERR_TIMEOUT: "device-side wait timed out", GBX_ERR_WORKSPACE: "workspace too small",
+             GBX_ERR_NOCONV: "refinement did not reach the tolerance"}
 
 _lib = None
 
@@ -52,6 +55,15 @@ SIGNATURES = {
     "gbx_dplgsy_tile": (_i, [_d, _i, _i, _vp, _i, _i, _i, _i, _ull, _vp]),
     "gbx_dag_timeout_selftest": (_i, [_i, _vp, _vp, _sz, _u64, _vp]),
     "gbx_gemm_bf16_nt_f32": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp]),
+    "gbx_dgen_lowrank_sym_tiled": (_i, [_i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
+    "gbx_potrf_mixed_bufferSize": (_i, [_i, _i, _szp]),
+    "gbx_potrf_mixed": (_i, [_i, _i, _vp, _vp, _i, _d, _vp, _sz, _vp]),
+    "gbx_potrf_mixed_info": (_i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_float), _vp]),
+    "gbx_spotri_diag": (_i, [_i, _i, _vp, _vp, _vp]),
+    "gbx_sprecond": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
+    "gbx_dsymm_tiled": (_i, [_i, _i, _vp, _i, _d, _vp, _d, _vp, _vp]),
+    "gbx_dposv_mixed_bufferSize": (_i, [_i, _i, _i, _szp]),
+    "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
 }
 
 
@@ -159,4 +171,62 @@ def gen_uniform_sym(tiles, N, NB, seed=42, shift=None, stream=None):
 
 def plgsy(tiles, N, NB, bump, seed, stream=None):
     call("gbx_dplgsy_tiled", N, NB, float(bump), seed, _ptr(tiles), _stream(stream))
+    return tiles
+
+
+class RefineInfo(ctypes.Structure):
+    """gbx_refine_info of include/gbx_potrf.h."""
+    _fields_ = [("iterations", ctypes.c_int), ("factor_retries", ctypes.c_int), ("shift", ctypes.c_double),
+                ("backward_error", ctypes.c_double), ("anorm", ctypes.c_double),
+                ("cond_estimate", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def potrf_mixed(A_tiles, N, NB, prec="bf16", shift=0.0, W=None, work=None, stream=None):
+    """Low-precision factorisation of an FP64 tile-major lower matrix into FP32 tiles W.
+    Returns (W, work, status, cond_estimate)."""
+    import torch
+    need = _sz(0)
+    call("gbx_potrf_mixed_bufferSize", N, NB, ctypes.byref(need))
+    if W is None:
+        W = torch.empty(A_tiles.numel(), dtype=torch.float32, device=A_tiles.device)
+    if work is None or work.numel() < need.value:
+        work = torch.empty(need.value, dtype=torch.uint8, device=A_tiles.device)
+    s = _stream(stream)
+    call("gbx_potrf_mixed", N, NB, _ptr(A_tiles), _ptr(W), PREC[prec], float(shift), _ptr(work), need.value, s)
+    cond = ctypes.c_float(0)
+    st = call("gbx_potrf_mixed_info", _ptr(work), N, NB, ctypes.byref(cond), s)
+    return W, work, st, cond.value
+
+
+def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=None, work=None, W=None):
+    """Solves A X = B to FP64 backward error `tol` (B: (nrhs, N) CUDA float64, rows = right-hand
+    sides). Returns (X, info dict, status)."""
+    import torch
+    nrhs = B.shape[0]
+    need = _sz(0)
+    call("gbx_dposv_mixed_bufferSize", N, NB, nrhs, ctypes.byref(need))
+    if work is None or work.numel() < need.value:
+        work = torch.empty(need.value, dtype=torch.uint8, device=A_tiles.device)
+    if W is None:
+        W = torch.empty(A_tiles.numel(), dtype=torch.float32, device=A_tiles.device)
+    X = torch.empty_like(B)
+    info = RefineInfo()
+    st = lib().gbx_dposv_mixed(N, NB, _ptr(A_tiles), nrhs, _ptr(B), _ptr(X), PREC[prec], float(tol), int(maxiter),
+                               _ptr(W), _ptr(work), need.value, ctypes.byref(info), _stream(stream))
+    if st < 0 and st != GBX_ERR_NOCONV:
+        raise GbxError("gbx_dposv_mixed", st)
+    return X, info.as_dict(), st
+
+
+def gen_lowrank(tiles, N, NB, lam, U, V, G, stream=None):
+    """Device generator of Q diag(lam) Q^T (see workloads.householder_factors)."""
+    r = U.shape[1] if U is not None else 0
+    Uc = U.T.contiguous() if r else None  # column-major N x r
+    Vc = V.T.contiguous() if r else None
+    Gc = G.T.contiguous() if r else None
+    call("gbx_dgen_lowrank_sym_tiled", N, NB, _ptr(lam), _ptr(Uc) if r else None, _ptr(Vc) if r else None,
+         _ptr(Gc) if r else None, r, _ptr(tiles), _stream(stream))
     return tiles

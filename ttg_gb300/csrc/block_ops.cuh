@@ -1,0 +1,215 @@
+// Block operations of the tiled Cholesky, templated on the element type (double for the FP64
+// path, float for the working precision of the mixed path). One CTA of 256 threads per call.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace gbx {
+
+constexpr int kThreads = 256;  // threads per CTA of every FP64 block kernel
+constexpr int kBlk = 128;      // largest block edge handled by one CTA
+constexpr int kKC = 16;        // k-chunk of the GEMM staging
+constexpr int kPW = 32;        // panel width of the TRSM
+
+// ------------------------------------------------------------------------------------------------
+// block GEMM:  C(m x n) := C - A(m x k) * B(n x k)^T   (lower: only i >= j of C is written)
+// 256 threads, each owning an 8 x 8 micro-tile (rows tx+16i, cols ty+16j); k staged through
+// shared memory in double-buffered chunks of 16 with a register prefetch of the next chunk.
+// smem: 2 * 2 * 16 * 128 doubles = 64 KB
+// ------------------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb, T* C,
+                                           int ldc, int m, int n, int k, bool lower, T* sm) {
+  T* As = sm;                       // [2][kKC][kBlk]
+  T* Bs = sm + 2 * kKC * kBlk;           // [2][kKC][kBlk]
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int lrow = tid & 127, lk0 = tid >> 7;
+  T acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+
+  const int nchunks = (k + kKC - 1) / kKC;
+  T ra[8], rb[8];
+  auto gload = [&](int k0) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int kk = k0 + lk0 + 2 * s;
+      ra[s] = (lrow < m && kk < k) ? __ldcg(A + lrow + (long long)kk * lda) : T(0);
+      rb[s] = (lrow < n && kk < k) ? __ldcg(B + lrow + (long long)kk * ldb) : T(0);
+    }
+  };
+  auto sstore = [&](int buf) {
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      As[(buf * kKC + lk0 + 2 * s) * kBlk + lrow] = ra[s];
+      Bs[(buf * kKC + lk0 + 2 * s) * kBlk + lrow] = rb[s];
+    }
+  };
+  if (nchunks > 0) {
+    gload(0);
+    sstore(0);
+    __syncthreads();
+    for (int c = 0; c < nchunks; ++c) {
+      const int buf = c & 1;
+      if (c + 1 < nchunks) gload((c + 1) * kKC);
+      const T* as = As + buf * kKC * kBlk;
+      const T* bs = Bs + buf * kKC * kBlk;
+#pragma unroll
+      for (int kk = 0; kk < kKC; ++kk) {
+        T a[8], b[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = as[kk * kBlk + tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) b[j] = bs[kk * kBlk + ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      if (c + 1 < nchunks) sstore(buf ^ 1);
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int col = ty + 16 * j;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = tx + 16 * i;
+      if (row < m && col < n && (!lower || row >= col)) {
+        T* p = C + row + (long long)col * ldc;
+        __stcg(p, __ldcg(p) - acc[i][j]);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------------------------------------
+// block POTRF (lower, n <= 128) in shared memory; right-looking, one column per step.
+// Returns 0 or the 1-based local index of the first non-positive pivot (LAPACK info); the
+// strict upper triangle of A is not touched. smem: 128 * 128 doubles + 1 int.
+// ------------------------------------------------------------------------------------------------
+template <typename T>
+__device__ int op_potrf(T* A, int lda, int n, T* sm) {
+  T* S = sm;                              // col-major, ld 128
+  int* flag = (int*)(sm + kBlk * kBlk);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) *flag = 0;
+  for (int idx = tid; idx < kBlk * n; idx += kThreads) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    if (i < n && i >= j) S[i + kBlk * j] = __ldcg(A + i + (long long)j * lda);
+  }
+  __syncthreads();
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    if (tid == 0) {
+      const T d = S[j + kBlk * j];
+      if (!(d > T(0))) *flag = j + 1;
+      else S[j + kBlk * j] = sqrt(d);
+    }
+    __syncthreads();
+    info = *flag;
+    if (info) break;
+    const T djj = S[j + kBlk * j];
+    for (int i = j + 1 + tid; i < n; i += kThreads) S[i + kBlk * j] = S[i + kBlk * j] / djj;
+    __syncthreads();
+    for (int c = j + 1 + warp; c < n; c += kThreads / 32) {
+      const T lcj = S[c + kBlk * j];
+      for (int i = c + lane; i < n; i += 32) S[i + kBlk * c] = fma(-S[i + kBlk * j], lcj, S[i + kBlk * c]);
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < kBlk * n; idx += kThreads) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    if (i < n && i >= j) __stcg(A + i + (long long)j * lda, S[i + kBlk * j]);
+  }
+  __syncthreads();
+  return info;
+}
+
+// ------------------------------------------------------------------------------------------------
+// block TRSM (Right, Lower, Trans, NonUnit): B(m x n) := B * L^{-T}, m <= 128, any n.
+// Column panels of 32: left-looking update of the panel from the already-solved columns (a
+// 128 x 32 x p0 GEMM, 4 x 4 micro-tiles), then each thread solves its own row across the panel.
+// smem: panel 32*128 + X chunk 16*128 + L chunk 16*32 + diagonal 32*32 doubles = 60 KB
+// ------------------------------------------------------------------------------------------------
+template <typename T>
+__device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, int n, T* sm) {
+  T* P = sm;                    // [kPW][128]  panel, P[c*128 + r]
+  T* Xc = P + kPW * kBlk;       // [kKC][128]
+  T* Lc = Xc + kKC * kBlk;      // [kKC][kPW]
+  T* Ld = Lc + kKC * kPW;       // [kPW][kPW]  Ld[c2*32 + c] = L(p0+c, p0+c2)
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  for (int p0 = 0; p0 < n; p0 += kPW) {
+    const int pw = min(kPW, n - p0);
+    for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
+      const int r = idx & (kBlk - 1), c = idx >> 7;
+      P[idx] = (r < m && c < pw) ? __ldcg(B + r + (long long)(p0 + c) * ldb) : T(0);
+    }
+    for (int idx = tid; idx < kPW * kPW; idx += kThreads) {
+      const int c = idx & 31, c2 = idx >> 5;
+      Ld[idx] = (c < pw && c2 <= c) ? __ldcg(L + (p0 + c) + (long long)(p0 + c2) * ldl) : T(0);
+    }
+    __syncthreads();
+    if (p0 > 0) {
+      T acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+      for (int k0 = 0; k0 < p0; k0 += kKC) {
+        for (int idx = tid; idx < kKC * kBlk; idx += kThreads) {
+          const int r = idx & (kBlk - 1), kk = idx >> 7;
+          Xc[idx] = (r < m) ? __ldcg(B + r + (long long)(k0 + kk) * ldb) : T(0);
+        }
+        for (int idx = tid; idx < kKC * kPW; idx += kThreads) {
+          const int c = idx & 31, kk = idx >> 5;
+          Lc[idx] = (c < pw) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kKC; ++kk) {
+          T a[4], b[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) a[i] = Xc[kk * kBlk + tx + 32 * i];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) b[j] = Lc[kk * kPW + ty + 8 * j];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) P[(ty + 8 * j) * kBlk + tx + 32 * i] -= acc[i][j];
+      __syncthreads();
+    }
+    if (tid < m && tid < kBlk) {
+      const int r = tid;
+      for (int c = 0; c < pw; ++c) {
+        T s0 = P[c * kBlk + r], s1 = T(0);
+        int c2 = 0;
+        for (; c2 + 1 < c; c2 += 2) {
+          s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
+          s1 = fma(-P[(c2 + 1) * kBlk + r], Ld[(c2 + 1) * kPW + c], s1);
+        }
+        if (c2 < c) s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
+        P[c * kBlk + r] = (s0 + s1) / Ld[c * kPW + c];
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
+      const int r = idx & (kBlk - 1), c = idx >> 7;
+      if (r < m && c < pw) __stcg(B + r + (long long)(p0 + c) * ldb, P[idx]);
+    }
+    __syncthreads();
+  }
+}
+
+
+}  // namespace gbx

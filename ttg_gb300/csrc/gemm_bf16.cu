@@ -142,6 +142,22 @@ int make_tmap_kmajor_bf16(CUtensorMap* map, const void* base, uint64_t rows, uin
   return r == CUDA_SUCCESS ? GBX_OK : GBX_ERR_ARG;
 }
 
+// same for fp16 (bf16 = false)
+int make_tmap_kmajor_16b(CUtensorMap* map, const void* base, uint64_t rows, uint64_t k, uint64_t ld, uint32_t box_rows,
+                         bool bf16) {
+  auto enc = encode_fn();
+  if (!enc) return GBX_ERR_CUDA;
+  if (((uintptr_t)base & 15) || ((ld * 2) & 15) || rows == 0 || k == 0) return GBX_ERR_ARG;
+  cuuint64_t dims[2] = {k, rows};
+  cuuint64_t strides[1] = {ld * 2};
+  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                   const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? GBX_OK : GBX_ERR_ARG;
+}
+
 }  // namespace tc
 }  // namespace gbx
 

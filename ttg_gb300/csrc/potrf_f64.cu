@@ -12,214 +12,11 @@
 #include <mutex>
 #include <vector>
 
+#include "block_ops.cuh"
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
 
 namespace gbx {
-
-constexpr int kThreads = 256;  // threads per CTA of every FP64 block kernel
-constexpr int kBlk = 128;      // largest block edge handled by one CTA
-constexpr int kKC = 16;        // k-chunk of the GEMM staging
-constexpr int kPW = 32;        // panel width of the TRSM
-
-// ------------------------------------------------------------------------------------------------
-// block GEMM:  C(m x n) := C - A(m x k) * B(n x k)^T   (lower: only i >= j of C is written)
-// 256 threads, each owning an 8 x 8 micro-tile (rows tx+16i, cols ty+16j); k staged through
-// shared memory in double-buffered chunks of 16 with a register prefetch of the next chunk.
-// smem: 2 * 2 * 16 * 128 doubles = 64 KB
-// ------------------------------------------------------------------------------------------------
-__device__ __forceinline__ void op_gemm_nt(const double* __restrict__ A, int lda, const double* __restrict__ B,
-                                           int ldb, double* C, int ldc, int m, int n, int k, bool lower,
-                                           double* sm) {
-  double* As = sm;                       // [2][kKC][kBlk]
-  double* Bs = sm + 2 * kKC * kBlk;      // [2][kKC][kBlk]
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const int lrow = tid & 127, lk0 = tid >> 7;
-  double acc[8][8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0;
-
-  const int nchunks = (k + kKC - 1) / kKC;
-  double ra[8], rb[8];
-  auto gload = [&](int k0) {
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-      const int kk = k0 + lk0 + 2 * s;
-      ra[s] = (lrow < m && kk < k) ? __ldcg(A + lrow + (long long)kk * lda) : 0.0;
-      rb[s] = (lrow < n && kk < k) ? __ldcg(B + lrow + (long long)kk * ldb) : 0.0;
-    }
-  };
-  auto sstore = [&](int buf) {
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-      As[(buf * kKC + lk0 + 2 * s) * kBlk + lrow] = ra[s];
-      Bs[(buf * kKC + lk0 + 2 * s) * kBlk + lrow] = rb[s];
-    }
-  };
-  if (nchunks > 0) {
-    gload(0);
-    sstore(0);
-    __syncthreads();
-    for (int c = 0; c < nchunks; ++c) {
-      const int buf = c & 1;
-      if (c + 1 < nchunks) gload((c + 1) * kKC);
-      const double* as = As + buf * kKC * kBlk;
-      const double* bs = Bs + buf * kKC * kBlk;
-#pragma unroll
-      for (int kk = 0; kk < kKC; ++kk) {
-        double a[8], b[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) a[i] = as[kk * kBlk + tx + 16 * i];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) b[j] = bs[kk * kBlk + ty + 16 * j];
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-          for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-      }
-      if (c + 1 < nchunks) sstore(buf ^ 1);
-      __syncthreads();
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const int col = ty + 16 * j;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int row = tx + 16 * i;
-      if (row < m && col < n && (!lower || row >= col)) {
-        double* p = C + row + (long long)col * ldc;
-        __stcg(p, __ldcg(p) - acc[i][j]);
-      }
-    }
-  }
-  __syncthreads();
-}
-
-// ------------------------------------------------------------------------------------------------
-// block POTRF (lower, n <= 128) in shared memory; right-looking, one column per step.
-// Returns 0 or the 1-based local index of the first non-positive pivot (LAPACK info); the
-// strict upper triangle of A is not touched. smem: 128 * 128 doubles + 1 int.
-// ------------------------------------------------------------------------------------------------
-__device__ int op_potrf(double* A, int lda, int n, double* sm) {
-  double* S = sm;                              // col-major, ld 128
-  int* flag = (int*)(sm + kBlk * kBlk);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) *flag = 0;
-  for (int idx = tid; idx < kBlk * n; idx += kThreads) {
-    const int i = idx & (kBlk - 1), j = idx >> 7;
-    if (i < n && i >= j) S[i + kBlk * j] = __ldcg(A + i + (long long)j * lda);
-  }
-  __syncthreads();
-  int info = 0;
-  for (int j = 0; j < n; ++j) {
-    if (tid == 0) {
-      const double d = S[j + kBlk * j];
-      if (!(d > 0.0)) *flag = j + 1;
-      else S[j + kBlk * j] = sqrt(d);
-    }
-    __syncthreads();
-    info = *flag;
-    if (info) break;
-    const double djj = S[j + kBlk * j];
-    for (int i = j + 1 + tid; i < n; i += kThreads) S[i + kBlk * j] = S[i + kBlk * j] / djj;
-    __syncthreads();
-    for (int c = j + 1 + warp; c < n; c += kThreads / 32) {
-      const double lcj = S[c + kBlk * j];
-      for (int i = c + lane; i < n; i += 32) S[i + kBlk * c] = fma(-S[i + kBlk * j], lcj, S[i + kBlk * c]);
-    }
-    __syncthreads();
-  }
-  for (int idx = tid; idx < kBlk * n; idx += kThreads) {
-    const int i = idx & (kBlk - 1), j = idx >> 7;
-    if (i < n && i >= j) __stcg(A + i + (long long)j * lda, S[i + kBlk * j]);
-  }
-  __syncthreads();
-  return info;
-}
-
-// ------------------------------------------------------------------------------------------------
-// block TRSM (Right, Lower, Trans, NonUnit): B(m x n) := B * L^{-T}, m <= 128, any n.
-// Column panels of 32: left-looking update of the panel from the already-solved columns (a
-// 128 x 32 x p0 GEMM, 4 x 4 micro-tiles), then each thread solves its own row across the panel.
-// smem: panel 32*128 + X chunk 16*128 + L chunk 16*32 + diagonal 32*32 doubles = 60 KB
-// ------------------------------------------------------------------------------------------------
-__device__ void op_trsm(const double* __restrict__ L, int ldl, double* B, int ldb, int m, int n, double* sm) {
-  double* P = sm;                    // [kPW][128]  panel, P[c*128 + r]
-  double* Xc = P + kPW * kBlk;       // [kKC][128]
-  double* Lc = Xc + kKC * kBlk;      // [kKC][kPW]
-  double* Ld = Lc + kKC * kPW;       // [kPW][kPW]  Ld[c2*32 + c] = L(p0+c, p0+c2)
-  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-  for (int p0 = 0; p0 < n; p0 += kPW) {
-    const int pw = min(kPW, n - p0);
-    for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
-      const int r = idx & (kBlk - 1), c = idx >> 7;
-      P[idx] = (r < m && c < pw) ? __ldcg(B + r + (long long)(p0 + c) * ldb) : 0.0;
-    }
-    for (int idx = tid; idx < kPW * kPW; idx += kThreads) {
-      const int c = idx & 31, c2 = idx >> 5;
-      Ld[idx] = (c < pw && c2 <= c) ? __ldcg(L + (p0 + c) + (long long)(p0 + c2) * ldl) : 0.0;
-    }
-    __syncthreads();
-    if (p0 > 0) {
-      double acc[4][4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-      for (int k0 = 0; k0 < p0; k0 += kKC) {
-        for (int idx = tid; idx < kKC * kBlk; idx += kThreads) {
-          const int r = idx & (kBlk - 1), kk = idx >> 7;
-          Xc[idx] = (r < m) ? __ldcg(B + r + (long long)(k0 + kk) * ldb) : 0.0;
-        }
-        for (int idx = tid; idx < kKC * kPW; idx += kThreads) {
-          const int c = idx & 31, kk = idx >> 5;
-          Lc[idx] = (c < pw) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : 0.0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kKC; ++kk) {
-          double a[4], b[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) a[i] = Xc[kk * kBlk + tx + 32 * i];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) b[j] = Lc[kk * kPW + ty + 8 * j];
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-        }
-        __syncthreads();
-      }
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) P[(ty + 8 * j) * kBlk + tx + 32 * i] -= acc[i][j];
-      __syncthreads();
-    }
-    if (tid < m && tid < kBlk) {
-      const int r = tid;
-      for (int c = 0; c < pw; ++c) {
-        double s0 = P[c * kBlk + r], s1 = 0.0;
-        int c2 = 0;
-        for (; c2 + 1 < c; c2 += 2) {
-          s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
-          s1 = fma(-P[(c2 + 1) * kBlk + r], Ld[(c2 + 1) * kPW + c], s1);
-        }
-        if (c2 < c) s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
-        P[c * kBlk + r] = (s0 + s1) / Ld[c * kPW + c];
-      }
-    }
-    __syncthreads();
-    for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
-      const int r = idx & (kBlk - 1), c = idx >> 7;
-      if (r < m && c < pw) __stcg(B + r + (long long)(p0 + c) * ldb, P[idx]);
-    }
-    __syncthreads();
-  }
-}
 
 constexpr size_t kDagSmemBytes = (size_t)kBlk * kBlk * sizeof(double) + 64;  // POTRF dominates
 
@@ -339,7 +136,7 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     switch (tk.type) {
       case T_POTRF: {
         const int K = tk.a;
-        const int info = op_potrf(V.ptr(K, K), V.ld, V.dim(K), smem);
+        const int info = op_potrf<double>(V.ptr(K, K), V.ld, V.dim(K), smem);
         if (info != 0) {
           if (threadIdx.x == 0) {
             atomicCAS(&P.st->status, 0, K * V.b + info);
@@ -353,20 +150,20 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
       }
       case T_TRSM: {
         const int M = tk.a, K = tk.b;
-        op_trsm(V.ptr(K, K), V.ld, V.ptr(M, K), V.ld, V.dim(M), V.dim(K), smem);
+        op_trsm<double>(V.ptr(K, K), V.ld, V.ptr(M, K), V.ld, V.dim(M), V.dim(K), smem);
         target = P.cnt + tri_index(M, K, NTb);
         break;
       }
       case T_SYRK: {
         const int K = tk.a, M = tk.b;
         const double* a = V.ptr(M, K);
-        op_gemm_nt(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
+        op_gemm_nt<double>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
         target = P.cnt + tri_index(M, M, NTb);
         break;
       }
       default: {
         const int M = tk.a, Nn = tk.b, K = tk.c;
-        op_gemm_nt(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn), V.dim(K), false,
+        op_gemm_nt<double>(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn), V.dim(K), false,
                    smem);
         target = P.cnt + tri_index(M, Nn, NTb);
         break;
@@ -395,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     bi = bj + rem;
   }
   const int r0 = bi * kBlk, c0 = bj * kBlk;
-  op_gemm_nt(A + r0, lda, B + c0, ldb, C + r0 + (long long)c0 * ldc, ldc, min(kBlk, m - r0), min(kBlk, n - c0), k,
+  op_gemm_nt<double>(A + r0, lda, B + c0, ldb, C + r0 + (long long)c0 * ldc, ldc, min(kBlk, m - r0), min(kBlk, n - c0), k,
              lower && bi == bj, smem);
 }
 
@@ -403,7 +200,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     trsm_rlt_grid_kernel(int m, int n, const double* L, int ldl, double* B, int ldb) {
   extern __shared__ __align__(16) double smem[];
   const int r0 = blockIdx.x * kBlk;
-  op_trsm(L, ldl, B + r0, ldb, min(kBlk, m - r0), n, smem);
+  op_trsm<double>(L, ldl, B + r0, ldb, min(kBlk, m - r0), n, smem);
 }
 
 __global__ void copy_info_kernel(const DagState* st, int* devInfo) {
@@ -552,6 +349,43 @@ __global__ void gen_tiles_kernel(int N, int NB, int NT, int kind, double bump_or
     else v = __dmul_rn(0.5, __dadd_rn(uniform_elem(seed, gi, gj), uniform_elem(seed, gj, gi)));
   }
   *out = v;
+}
+
+// A = diag(lam) + low-rank symmetric part, the closed form of Q diag(lam) Q^T for
+// Q = I - U V^T (compact WY form of a product of r Householder reflectors):
+//   A_ij = lam_i d_ij - lam_j (U V^T)_ij - lam_i (V U^T)_ij + (U G U^T)_ij,  G = V^T diag(lam) V
+// U, V: column-major N x r (r <= 8), G: r x r column-major; one element per thread.
+__global__ void gen_lowrank_kernel(int N, int NB, int NT, const double* __restrict__ lam,
+                                   const double* __restrict__ U, const double* __restrict__ V,
+                                   const double* __restrict__ G, int r, double* tiles) {
+  const int m = blockIdx.y, n = blockIdx.z;
+  if (m < n) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)NB * NB) return;
+  const int i = (int)(e % NB), j = (int)(e / NB);
+  const long long slot = (long long)n * NT - (long long)n * (n - 1) / 2 + (m - n);
+  double* out = tiles + slot * (long long)NB * NB + e;
+  const long long gi = (long long)m * NB + i, gj = (long long)n * NB + j;
+  if (gi >= N || gj >= N) {
+    *out = 0.0;
+    return;
+  }
+  double ui[8], uj[8];
+  double uv = 0.0, vu = 0.0;
+  for (int a = 0; a < r; ++a) {
+    ui[a] = U[gi + (long long)a * N];
+    uj[a] = U[gj + (long long)a * N];
+    uv = fma(ui[a], V[gj + (long long)a * N], uv);
+    vu = fma(V[gi + (long long)a * N], uj[a], vu);
+  }
+  double ugu = 0.0;
+  for (int b = 0; b < r; ++b) {
+    double t = 0.0;
+    for (int a = 0; a < r; ++a) t = fma(ui[a], G[a + b * r], t);
+    ugu = fma(t, uj[b], ugu);
+  }
+  const double li = lam[gi], lj = lam[gj];
+  *out = (gi == gj ? li : 0.0) - lj * uv - li * vu + ugu;
 }
 
 // one tile of the PLASMA generator: x over the m*n elements
@@ -822,6 +656,16 @@ int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m
   const long long total = (long long)m * n;
   plgsy_tile_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(bump, m, n, A, lda, gM, m0, n0,
                                                                                        seed);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int gbx_dgen_lowrank_sym_tiled(int N, int NB, const double* lam, const double* U, const double* V, const double* G,
+                               int r, double* tiles, void* stream) {
+  if (N <= 0 || NB <= 0 || r < 0 || r > 8 || !lam || (r > 0 && (!U || !V || !G)) || !tiles) return GBX_ERR_ARG;
+  const int NT = (N + NB - 1) / NB;
+  if (NT > 65535) return GBX_ERR_ARG;
+  dim3 grid((unsigned)(((long long)NB * NB + 255) / 256), NT, NT);
+  gen_lowrank_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(N, NB, NT, lam, U, V, G, r, tiles);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
