@@ -195,6 +195,24 @@ int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes);
 int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec, double tol,
                     int maxiter, float* W, void* work, size_t work_bytes, gbx_refine_info* info, void* stream);
 
+/* ============================================================================================
+ * Batched solves of many independent SPD matrices of uneven sizes in one persistent launch
+ * (capturable in a CUDA graph: no host synchronisation, no allocation). No counterpart in the
+ * reference.
+ * ========================================================================================== */
+
+/* Host helper: the longest-processing-time order (largest matrix first) of a batch. */
+int gbx_batched_order(int batch, const int* n_host, int* order_host);
+
+/* For every matrix i (device arrays n, offA, offB, order): A_i = column-major n_i x n_i at
+ * A + offA[i] (lower triangle read), right-hand sides column-major n_i x nrhs at B + offB[i],
+ * overwritten with the solution. mode 0: FP64 factor + solve (A_i overwritten by L_i); mode 1: FP32
+ * factor into L32 (offA layout) + `refine` steps of FP64 iterative refinement (A_i untouched).
+ * info[i] = 0 or the first bad pivot. n_i <= 1024. `work` >= 256 bytes (the queue head). */
+int gbx_dposv_batched(int batch, const int* n, const long long* offA, const long long* offB, const int* order,
+                      double* A, double* B, int nrhs, int mode, int refine, float* L32, int* info, void* work,
+                      size_t work_bytes, void* stream);
+
 /* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
  * task is skipped, so the dependency wait of the second task can never be satisfied and must
  * run out after `timeout_ns`. Returns the status the kernel reported (GBX_ERR_TIMEOUT when the

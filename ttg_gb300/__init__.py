@@ -63,6 +63,8 @@ SIGNATURES = {
     "gbx_sprecond": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     "gbx_dsymm_tiled": (_i, [_i, _i, _vp, _i, _d, _vp, _d, _vp, _vp]),
     "gbx_dposv_mixed_bufferSize": (_i, [_i, _i, _i, _szp]),
+    "gbx_batched_order": (_i, [_i, _vp, _vp]),
+    "gbx_dposv_batched": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
     "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
 }
 
@@ -230,3 +232,54 @@ def gen_lowrank(tiles, N, NB, lam, U, V, G, stream=None):
     call("gbx_dgen_lowrank_sym_tiled", N, NB, _ptr(lam), _ptr(Uc) if r else None, _ptr(Vc) if r else None,
          _ptr(Gc) if r else None, r, _ptr(tiles), _stream(stream))
     return tiles
+
+
+class Batch:
+    """A packed batch of SPD systems on the device for gbx_dposv_batched.
+
+    mats: list of (n_i x n_i) numpy float64 arrays (symmetric); rhs: list of (nrhs, n_i) arrays."""
+
+    def __init__(self, mats, rhs, device):
+        import numpy as np
+        import torch
+        self.batch = len(mats)
+        self.nrhs = rhs[0].shape[0]
+        n = np.array([m.shape[0] for m in mats], dtype=np.int32)
+        offA = np.zeros(self.batch, dtype=np.int64)
+        offB = np.zeros(self.batch, dtype=np.int64)
+        if self.batch > 1:
+            offA[1:] = np.cumsum(n.astype(np.int64) ** 2)[:-1]
+            offB[1:] = np.cumsum(n.astype(np.int64) * self.nrhs)[:-1]
+        order = np.zeros(self.batch, dtype=np.int32)
+        call("gbx_batched_order", self.batch, n.ctypes.data_as(_vp), order.ctypes.data_as(_vp))
+        self.sizes = n
+        Ah = np.concatenate([np.asfortranarray(m).ravel(order="F") for m in mats])
+        Bh = np.concatenate([np.asarray(b, dtype=np.float64).reshape(self.nrhs, -1).ravel() for b in rhs])
+        to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        self.A0, self.B0 = to(Ah), to(Bh)
+        self.A, self.B = self.A0.clone(), self.B0.clone()
+        self.n, self.offA, self.offB, self.order = to(n), to(offA), to(offB), to(order)
+        self.L32 = torch.empty(Ah.size, dtype=torch.float32, device=device)
+        self.info = torch.zeros(self.batch, dtype=torch.int32, device=device)
+        self.work = torch.zeros(256, dtype=torch.uint8, device=device)
+        self.flops = float(np.sum(n.astype(np.float64) ** 3) / 3.0)
+
+    def reset(self):
+        self.A.copy_(self.A0)
+        self.B.copy_(self.B0)
+
+    def solve(self, mode="fp64", refine=2, stream=None):
+        """Launches the batched solve (asynchronous, capturable). mode: 'fp64' or 'fp32'."""
+        call("gbx_dposv_batched", self.batch, _ptr(self.n), _ptr(self.offA), _ptr(self.offB), _ptr(self.order),
+             _ptr(self.A), _ptr(self.B), self.nrhs, 0 if mode == "fp64" else 1, int(refine), _ptr(self.L32),
+             _ptr(self.info), _ptr(self.work), self.work.numel(), _stream(stream))
+
+    def solutions(self):
+        import numpy as np
+        Bh = self.B.cpu().numpy()
+        out, o = [], 0
+        for ni in self.sizes:
+            k = int(ni) * self.nrhs
+            out.append(Bh[o:o + k].reshape(self.nrhs, int(ni)))
+            o += k
+        return out
