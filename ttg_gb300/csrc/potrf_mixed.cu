@@ -201,6 +201,7 @@ __global__ void __launch_bounds__(kThr, 1)
   __shared__ uint32_t tmem_slot;
   __shared__ long long s_task;
   __shared__ int s_go, s_info;
+  __shared__ float s_colscale[kSubN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -322,23 +323,41 @@ __global__ void __launch_bounds__(kThr, 1)
         const int q = warp & 3;
         const int r = r0 + q * 32 + lane;  // row of C handled by this thread
         const int mrows = tdim(M, P), ncols = tdim(Nn, P);
+        float* C = P.W + sC * (long long)NB * NB;
+        // while the MMAs run: column scales of this sub-tile into shared memory, C lines into L2
+        for (int c = (warp - 4) * 32 + lane; c < kSubN; c += 128)
+          s_colscale[c] = (c0 + c < ncols) ? pow2f(__ldcg(P.rowexp + sB * NB + c0 + c)) : 0.f;
+        if (r0 + q * 32 < mrows)
+          for (int c = lane; c < kSubN && c0 + c < ncols; c += 32)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(C + (r0 + q * 32) + (long long)(c0 + c) * NB));
+        asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+        const float rscale = (r < mrows) ? pow2f(__ldcg(P.rowexp + sA * NB + r)) : 0.f;
+        const bool row_ok = r < mrows;
+        const bool syrk = tk.type == T_SYRK;
         if (mbar_wait(smem_u32(&done_bar), acc_phase, err, P.timeout_ns)) {
           tc_fence_after();
-          const int eA = (r < mrows) ? __ldcg(P.rowexp + sA * NB + r) : 0;
-          float* C = P.W + sC * (long long)NB * NB;
+          float cur[16], nxt[16];
+          auto load16 = [&](float (&dst)[16], int c) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int col = c0 + c + j;
+              dst[j] = (row_ok && col < ncols) ? __ldcg(C + r + (long long)col * NB) : 0.f;
+            }
+          };
+          load16(cur, 0);
           for (int c = 0; c < kSubN; c += 16) {
             uint32_t v[16];
             tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
+            if (c + 16 < kSubN) load16(nxt, c + 16);  // next chunk's loads are in flight during this chunk
             tmem_ld_wait();
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               const int col = c0 + c + j;
-              if (r < mrows && col < ncols && (tk.type != T_SYRK || r >= col)) {
-                const float scale = pow2f(eA + __ldcg(P.rowexp + sB * NB + col));
-                float* p = C + r + (long long)col * NB;
-                __stcg(p, __ldcg(p) - __uint_as_float(v[j]) * scale);
-              }
+              if (row_ok && col < ncols && (!syrk || r >= col))
+                __stcg(C + r + (long long)col * NB, cur[j] - __uint_as_float(v[j]) * (rscale * s_colscale[c + j]));
             }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) cur[j] = nxt[j];
           }
         }
       } else {
