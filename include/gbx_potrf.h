@@ -43,6 +43,7 @@ extern "C" {
 #define GBX_ERR_TIMEOUT (-3)
 #define GBX_ERR_WORKSPACE (-4)
 #define GBX_ERR_NOCONV (-5)
+#define GBX_ERR_NOALLOC_LIMIT (-6)
 
 /* Library version and the device architecture it was built for (e.g. 1030). */
 int gbx_version(void);
@@ -98,6 +99,18 @@ int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes);
 /* Factorises the tile-major lower matrix in place (asynchronous). The status is kept in the
  * workspace; read it with gbx_dpotrf_tiled_status. */
 int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream);
+
+/* Allocation-free variant of gbx_dpotrf_tiled, for callers that cannot call cudaMalloc (device
+ * memory owned by another allocator or budgeted up front; latency-critical paths that cannot take
+ * cudaMalloc's device synchronisation). No counterpart in the reference. Its scratch is a
+ * library-owned static device array of 525,376 bytes that every GPU loading the library keeps until
+ * the process exits; it limits the problem to 512 blocks per edge (N <= 65536 with 128-blocks:
+ * NB <= 128 gives blocks of NB, larger NB blocks of 128, 64 or 32) and larger problems return
+ * GBX_ERR_NOALLOC_LIMIT. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress): make it before any stream capture. All calls share the array, so calls
+ * that overlap on the GPU (other streams, other threads) race; serialise them. The factorisation
+ * status (0, first bad pivot, GBX_ERR_TIMEOUT) is written to the device int devInfo. Asynchronous. */
+int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* stream);
 
 /* Synchronises `stream` and returns the status of the last gbx_dpotrf_tiled on `work`:
  * 0, >0 (first bad pivot, 1-based global index) or GBX_ERR_TIMEOUT. */

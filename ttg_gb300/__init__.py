@@ -19,11 +19,13 @@ GBX_ERR_CUDA = -2
 GBX_ERR_TIMEOUT = -3
 GBX_ERR_WORKSPACE = -4
 GBX_ERR_NOCONV = -5
+GBX_ERR_NOALLOC_LIMIT = -6
 PREC = {"bf16": 0, "fp16": 1}
 
 _ERRNAMES = {GBX_ERR_ARG: "invalid argument", GBX_ERR_CUDA: "CUDA runtime error",
              GBX_ERR_TIMEOUT: "device-side wait timed out", GBX_ERR_WORKSPACE: "workspace too small",
-             GBX_ERR_NOCONV: "refinement did not reach the tolerance"}
+             GBX_ERR_NOCONV: "refinement did not reach the tolerance",
+             GBX_ERR_NOALLOC_LIMIT: "problem exceeds the allocation-free entry point's scratch"}
 
 _lib = None
 
@@ -54,6 +56,7 @@ SIGNATURES = {
     "gbx_dgen_uniform_sym_tiled": (_i, [_i, _i, _ull, _d, _vp, _vp]),
     "gbx_dplgsy_tile": (_i, [_d, _i, _i, _vp, _i, _i, _i, _i, _ull, _vp]),
     "gbx_dag_timeout_selftest": (_i, [_i, _vp, _vp, _sz, _u64, _vp]),
+    "gbx_dpotrf_tiled_noalloc": (_i, [_i, _i, _vp, _vp, _vp]),
     "gbx_gemm_bf16_nt_f32": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp]),
     "gbx_dgen_lowrank_sym_tiled": (_i, [_i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "gbx_potrf_mixed_bufferSize": (_i, [_i, _i, _szp]),

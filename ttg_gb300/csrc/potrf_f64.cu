@@ -669,6 +669,57 @@ int gbx_dgen_lowrank_sym_tiled(int N, int NB, const double* lam, const double* U
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
+// ---- allocation-free variant of gbx_dpotrf_tiled ---------------------------------------------------
+// Some callers cannot call cudaMalloc: code whose device memory belongs to another allocator or is
+// budgeted up front (a host framework's caching allocator, a fixed memory reservation), and code on
+// latency-critical paths where cudaMalloc/cudaFree's implicit device synchronisation is not
+// acceptable. For them the executor's scratch (run header + one completion counter per 128 x 128
+// block) lives in this file-scope device array instead of a caller workspace. Every GPU that loads
+// the library holds it until the process exits.
+}  // extern "C"
+
+namespace gbx {
+constexpr int kNoAllocMaxNTb = 512;  // at most 512 blocks per edge: N <= 65536 (blocks of 128)
+constexpr size_t kNoAllocBytes = sizeof(DagState) + (size_t)kNoAllocMaxNTb * (kNoAllocMaxNTb + 1) / 2 * sizeof(int);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];  // 525,376 bytes
+
+std::mutex g_noalloc_mtx;
+std::vector<void*> g_noalloc_ptr;  // device address of g_noalloc_scratch, per device
+
+// One-time set-up per device, with that device current: the symbol's device address. In host code
+// the array's name is only a host-side stand-in and must never be passed to a kernel.
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GBX_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_noalloc_mtx);
+  if ((int)g_noalloc_ptr.size() <= dev) g_noalloc_ptr.resize(dev + 1, nullptr);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return GBX_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GBX_OK;
+}
+}  // namespace gbx
+
+extern "C" {
+
+int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* stream) {
+  if (N < 0 || NB <= 0 || block_edge(NB) == 0 || !devInfo || (N > 0 && !tiles)) return GBX_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (N == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+  const BlockView V = tiled_view(N, NB, tiles);
+  const int NTb = (N + V.b - 1) / V.b;
+  if (NTb > kNoAllocMaxNTb) return GBX_ERR_NOALLOC_LIMIT;
+  void* scratch = nullptr;
+  if (int e = noalloc_scratch(&scratch)) return e;
+  // launch_dag clears the header and the counters this run uses (cudaMemsetAsync, no allocation)
+  if (int e = launch_dag(V, NTb, scratch, kNoAllocBytes, s, 0, gbx_get_wait_timeout_ns())) return e;
+  copy_info_kernel<<<1, 32, 0, s>>>((const DagState*)scratch, devInfo);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
 int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_bytes, uint64_t timeout_ns,
                              void* stream) {
   if (NB <= 0 || NB > kBlk || !tiles) return GBX_ERR_ARG;
