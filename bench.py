@@ -44,6 +44,10 @@ def parse():
     p.add_argument("--cpu-N", type=int, default=16384, help="bounded CPU sample size")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision configuration")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched configuration")
+    p.add_argument("--profile-case", choices=["dag", "mixed", "batched"], default=None,
+                   help="run one small case of one kernel (N=8192) for an ncu capture; prints no JSON")
     return p.parse_args()
 
 
@@ -293,6 +297,14 @@ def run_ours(args, ws, rank, local):
     if not args.no_e2e:
         line["e2e"] = run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps=max(1, min(args.steps, 2)))
 
+    if not args.no_mixed:
+        del T, A0
+        torch.cuda.empty_cache()
+        line["mixed"] = run_mixed(gbx, dev)
+    if not args.no_batched:
+        torch.cuda.empty_cache()
+        line["batched"] = run_batched(gbx, dev, reps=max(3, args.steps))
+
     if rank == 0 and not args.no_cpu:
         times, blas = cpu_run(args.cpu_N, NB, 2)
         sec = min(times)
@@ -329,6 +341,115 @@ def backward_error(gbx, A0, T, X, b0, N, NB, dev):
                 rowsum[m * NB:m * NB + rm] += blk.abs().sum(1)
                 rowsum[n * NB:n * NB + rn] += blk.abs().sum(0)
     return (r.abs().max() / (rowsum.max() * x.abs().max() + b0[0].abs().max())).item()
+
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_mixed(gbx, dev, N=32768, NB=512, nrhs=8, kappa=1e6):
+    """Mixed-precision factor + FP64 refinement (tensor-core bf16/fp16 factorisation, CG in FP64) of
+    A = H diag(lam) H^T (4 Householder reflectors, kappa = 1e6), 8 right-hand sides, against the
+    plain FP64 GPU path (factor + solve) of the same system."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from ttg_gb300 import workloads
+    A = workloads.householder_tiles(N, NB, 4, kappa, 42, dev)
+    B = torch.from_numpy(workloads.rhs(N, nrhs, 42)).to(dev)
+    out = {"config": {"workload": "potrf+refine N=%d NB=%d nrhs=%d, H diag(lam) H^T, 4 reflectors, kappa=%g"
+                                  % (N, NB, nrhs, kappa), "N": N, "NB": NB, "nrhs": nrhs, "kappa": kappa,
+                      "tolerance": 1e-14}}
+    # plain FP64 GPU path: the reference of the speed-up and of the forward error
+    T = A.clone()
+    X64 = B.clone()
+    work = torch.empty(gbx.potrf_workspace_bytes(N, NB), dtype=torch.uint8, device=dev)
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    e0, e1 = _events()
+    torch.cuda.synchronize()
+    e0.record()
+    gbx.call("gbx_dpotrf_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(work.data_ptr()), work.numel(), sp)
+    gbx.call("gbx_dpotrs_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), nrhs, ctypes.c_void_p(X64.data_ptr()), N, sp)
+    e1.record()
+    e1.synchronize()
+    assert gbx.potrf_status(work) == 0
+    plain_ms = e0.elapsed_time(e1)
+    del T, work
+    torch.cuda.empty_cache()
+    out["plain_fp64"] = {"ms": plain_ms, "tflops": N ** 3 / 3 / (plain_ms * 1e-3) / 1e12}
+    for prec in ("bf16", "fp16"):
+        W = torch.empty(A.numel(), dtype=torch.float32, device=dev)
+        X, info, st = gbx.dposv_mixed(A, N, NB, B, prec=prec, tol=1e-14, maxiter=300, W=W)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        X, info, st = gbx.dposv_mixed(A, N, NB, B, prec=prec, tol=1e-14, maxiter=300, W=W)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        fe = ((X - X64).abs().max() / X64.abs().max()).item()
+        out[prec] = {"ms": ms, "tflops": N ** 3 / 3 / (ms * 1e-3) / 1e12, "speedup_vs_plain_fp64": plain_ms / ms,
+                     "status": st, "iterations": info["iterations"], "factor_retries": info["factor_retries"],
+                     "shift": info["shift"], "backward_error": info["backward_error"],
+                     "forward_error_vs_fp64": fe, "cond_estimate_diag_tiles": info["cond_estimate"]}
+        del W
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_batched(gbx, dev, count=4096, reps=3):
+    """4096 SPD systems, sizes uniform over 32*{1..16}, (M+M^T)/2 + n I, 1 right-hand side each:
+    one persistent launch per solve, captured in a CUDA graph; FP64 and FP32 + 2 FP64 refinement
+    steps."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(42)
+    sizes = 32 * rng.integers(1, 17, size=count)
+    rhs = [rng.standard_normal((1, int(n))) for n in sizes]
+    b = gbx.Batch(None, rhs, dev, sizes=sizes, seed=42)
+    out = {"config": {"workload": "%d SPD systems, n uniform in 32*{1..16}, 1 rhs, one persistent launch in a CUDA graph"
+                                  % count, "count": count, "flops": b.flops}}
+    stream = torch.cuda.Stream()
+    for mode, refine in (("fp64", 0), ("fp32", 2)):
+        b.reset()
+        b.solve(mode=mode, refine=refine)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            b.solve(mode=mode, refine=refine, stream=stream)
+        times = []
+        for _ in range(reps + 1):
+            b.reset()
+            torch.cuda.synchronize()
+            e0, e1 = _events()
+            with torch.cuda.stream(stream):  # replay() launches on the current stream
+                e0.record()
+                g.replay()
+                e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = sum(times[1:]) / reps
+        # solution quality on a sample of the systems (checked on the host)
+        xs = b.solutions()
+        An = b.A0.cpu().numpy() if mode == "fp32" else None
+        worst = 0.0
+        if An is not None:
+            o = 0
+            offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+            for k in range(0, count, 97):
+                n = int(sizes[k])
+                Ak = An[offs[k]:offs[k] + n * n].reshape(n, n).T
+                r = rhs[k][0] - Ak @ xs[k][0]
+                worst = max(worst, np.abs(r).max() / (np.abs(Ak).sum(1).max() * np.abs(xs[k][0]).max()
+                                                      + np.abs(rhs[k][0]).max()))
+        out[mode] = {"ms": ms, "matrices_per_s": count / (ms * 1e-3), "tflops": b.flops / (ms * 1e-3) / 1e12,
+                     "refine_steps": refine, "info_nonzero": int((b.info != 0).sum().item())}
+        if An is not None:
+            out[mode]["backward_error_sampled"] = worst
+    return out
 
 
 def run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps):
@@ -369,8 +490,40 @@ def run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps):
             "api": "gbx_dpotrf_tiled + gbx_dpotrs_tiled (C ABI) with pinned host buffers"}
 
 
+def profile_case(case):
+    """One small case of one kernel (inputs larger than L2, a few GB at most), for ncu captures."""
+    import torch
+
+    import ttg_gb300 as gbx
+    from ttg_gb300 import workloads
+    dev = torch.device("cuda:0")
+    N, NB = 8192, 512
+    if case in ("dag", "mixed"):
+        A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
+        gbx.gen_uniform_sym(A, N, NB, seed=42)
+        for _ in range(2):  # the second launch is the captured one (-s 1 -c 1), or both (-c 2)
+            if case == "dag":
+                gbx.potrf_tiled(A.clone(), N, NB)
+            else:
+                W, work, st, cond = gbx.potrf_mixed(A, N, NB, prec="bf16")
+                assert st == 0
+    else:
+        import numpy as np
+        rng = np.random.default_rng(42)
+        sizes = 32 * rng.integers(1, 17, size=1024)
+        b = gbx.Batch(None, [np.ones((1, int(n))) for n in sizes], dev, sizes=sizes, seed=42)
+        for _ in range(2):
+            b.reset()
+            b.solve(mode="fp64")
+    torch.cuda.synchronize()
+    print("profile case %s done" % case)
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, ws, rank)

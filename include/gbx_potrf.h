@@ -214,6 +214,12 @@ int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, d
  * reference.
  * ========================================================================================== */
 
+/* Fills matrix k of a batch (device arrays n, offA) with (M + M^T)/2 + n_k I, M_ij uniform in
+ * [-0.5, 0.5) from the counter-based generator of gbx_dgen_uniform_sym_tiled with seed
+ * seed + k * 0x9e3779b97f4a7c15 (full column-major storage). */
+int gbx_dgen_uniform_sym_batched(int batch, const int* n, const long long* offA, unsigned long long seed, double* A,
+                                 void* stream);
+
 /* Host helper: the longest-processing-time order (largest matrix first) of a batch. */
 int gbx_batched_order(int batch, const int* n_host, int* order_host);
 
@@ -225,6 +231,12 @@ int gbx_batched_order(int batch, const int* n_host, int* order_host);
 int gbx_dposv_batched(int batch, const int* n, const long long* offA, const long long* offB, const int* order,
                       double* A, double* B, int nrhs, int mode, int refine, float* L32, int* info, void* work,
                       size_t work_bytes, void* stream);
+
+/* gbx_dposv_batched with an explicit number of CTAs (0 = every resident CTA slot): the knob of the
+ * batched autotuner (ttg_gb300/autotune.py). */
+int gbx_dposv_batched_ex(int batch, const int* n, const long long* offA, const long long* offB, const int* order,
+                         double* A, double* B, int nrhs, int mode, int refine, float* L32, int* info, int ctas,
+                         void* work, size_t work_bytes, void* stream);
 
 /* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
  * task is skipped, so the dependency wait of the second task can never be satisfied and must

@@ -73,3 +73,18 @@ def test_batched_in_cuda_graph(gbx, cuda):
         torch.cuda.synchronize()
         for A, r, x in zip(mats, rhs, b.solutions()):
             assert berr(A, x[0], r[0]) <= 1e-14
+
+
+def test_batched_device_generator_matches_oracle(gbx, cuda):
+    import oracle
+    sizes = [32, 100, 64]
+    rhs = [np.ones((1, n)) for n in sizes]
+    b = gbx.Batch(None, rhs, cuda, sizes=sizes, seed=42)
+    A = b.A0.cpu().numpy()
+    o = 0
+    for k, n in enumerate(sizes):
+        got = A[o:o + n * n].reshape(n, n).T  # column-major
+        sk = (42 + k * 0x9E3779B97F4A7C15) % (1 << 64)
+        ref = oracle.uniform_sym_full(n, sk, shift=n)
+        assert np.array_equal(got, ref)
+        o += n * n

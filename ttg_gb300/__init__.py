@@ -67,7 +67,9 @@ SIGNATURES = {
     "gbx_dsymm_tiled": (_i, [_i, _i, _vp, _i, _d, _vp, _d, _vp, _vp]),
     "gbx_dposv_mixed_bufferSize": (_i, [_i, _i, _i, _szp]),
     "gbx_batched_order": (_i, [_i, _vp, _vp]),
+    "gbx_dgen_uniform_sym_batched": (_i, [_i, _vp, _vp, _ull, _vp, _vp]),
     "gbx_dposv_batched": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
+    "gbx_dposv_batched_ex": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _sz, _vp]),
     "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
 }
 
@@ -240,14 +242,15 @@ def gen_lowrank(tiles, N, NB, lam, U, V, G, stream=None):
 class Batch:
     """A packed batch of SPD systems on the device for gbx_dposv_batched.
 
-    mats: list of (n_i x n_i) numpy float64 arrays (symmetric); rhs: list of (nrhs, n_i) arrays."""
+    mats: list of (n_i x n_i) numpy float64 arrays (symmetric), or None together with `sizes` and
+    `seed` to generate (M + M^T)/2 + n I on the device; rhs: list of (nrhs, n_i) arrays."""
 
-    def __init__(self, mats, rhs, device):
+    def __init__(self, mats, rhs, device, sizes=None, seed=42):
         import numpy as np
         import torch
-        self.batch = len(mats)
+        self.batch = len(mats) if mats is not None else len(sizes)
         self.nrhs = rhs[0].shape[0]
-        n = np.array([m.shape[0] for m in mats], dtype=np.int32)
+        n = np.array([m.shape[0] for m in mats] if mats is not None else list(sizes), dtype=np.int32)
         offA = np.zeros(self.batch, dtype=np.int64)
         offB = np.zeros(self.batch, dtype=np.int64)
         if self.batch > 1:
@@ -256,13 +259,19 @@ class Batch:
         order = np.zeros(self.batch, dtype=np.int32)
         call("gbx_batched_order", self.batch, n.ctypes.data_as(_vp), order.ctypes.data_as(_vp))
         self.sizes = n
-        Ah = np.concatenate([np.asfortranarray(m).ravel(order="F") for m in mats])
-        Bh = np.concatenate([np.asarray(b, dtype=np.float64).reshape(self.nrhs, -1).ravel() for b in rhs])
         to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
-        self.A0, self.B0 = to(Ah), to(Bh)
-        self.A, self.B = self.A0.clone(), self.B0.clone()
         self.n, self.offA, self.offB, self.order = to(n), to(offA), to(offB), to(order)
-        self.L32 = torch.empty(Ah.size, dtype=torch.float32, device=device)
+        total = int(np.sum(n.astype(np.int64) ** 2))
+        if mats is not None:
+            self.A0 = to(np.concatenate([np.asfortranarray(m).ravel(order="F") for m in mats]))
+        else:
+            self.A0 = torch.empty(total, dtype=torch.float64, device=device)
+            call("gbx_dgen_uniform_sym_batched", self.batch, _ptr(self.n), _ptr(self.offA), seed, _ptr(self.A0),
+                 _stream(None))
+        Bh = np.concatenate([np.asarray(b, dtype=np.float64).reshape(self.nrhs, -1).ravel() for b in rhs])
+        self.B0 = to(Bh)
+        self.A, self.B = self.A0.clone(), self.B0.clone()
+        self.L32 = torch.empty(total, dtype=torch.float32, device=device)
         self.info = torch.zeros(self.batch, dtype=torch.int32, device=device)
         self.work = torch.zeros(256, dtype=torch.uint8, device=device)
         self.flops = float(np.sum(n.astype(np.float64) ** 3) / 3.0)
@@ -271,11 +280,17 @@ class Batch:
         self.A.copy_(self.A0)
         self.B.copy_(self.B0)
 
-    def solve(self, mode="fp64", refine=2, stream=None):
+    def set_order(self, order):
+        """Replaces the queue order (a permutation of the matrix indices)."""
+        import numpy as np
+        import torch
+        self.order = torch.from_numpy(np.ascontiguousarray(order, dtype=np.int32)).to(self.n.device)
+
+    def solve(self, mode="fp64", refine=2, stream=None, ctas=0):
         """Launches the batched solve (asynchronous, capturable). mode: 'fp64' or 'fp32'."""
-        call("gbx_dposv_batched", self.batch, _ptr(self.n), _ptr(self.offA), _ptr(self.offB), _ptr(self.order),
+        call("gbx_dposv_batched_ex", self.batch, _ptr(self.n), _ptr(self.offA), _ptr(self.offB), _ptr(self.order),
              _ptr(self.A), _ptr(self.B), self.nrhs, 0 if mode == "fp64" else 1, int(refine), _ptr(self.L32),
-             _ptr(self.info), _ptr(self.work), self.work.numel(), _stream(stream))
+             _ptr(self.info), int(ctas), _ptr(self.work), self.work.numel(), _stream(stream))
 
     def solutions(self):
         import numpy as np

@@ -44,54 +44,6 @@ __device__ int factor(T* A, int n, int ld, T* sm) {
   return 0;
 }
 
-// x := (L L^T)^{-1} x for one right-hand side held in shared memory xs[0..n)
-// forward and backward substitution by 32-column panels: warp 0 solves the panel's triangle
-// (shuffle-free, __syncwarp), the whole CTA applies the panel to the remaining rows
-template <typename T>
-__device__ void solve_vec(const T* L, int n, int ld, T* xs) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int p0 = 0; p0 < n; p0 += 32) {  // L y = x
-    const int pw = min(32, n - p0);
-    if (warp == 0) {
-      for (int c = 0; c < pw; ++c) {
-        if (lane == c) xs[p0 + c] /= L[(p0 + c) + (long long)(p0 + c) * ld];
-        __syncwarp();
-        if (lane > c && lane < pw) xs[p0 + lane] -= L[(p0 + lane) + (long long)(p0 + c) * ld] * xs[p0 + c];
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    for (int i = p0 + pw + tid; i < n; i += blockDim.x) {
-      T s = T(0);
-      for (int c = 0; c < pw; ++c) s += L[i + (long long)(p0 + c) * ld] * xs[p0 + c];
-      xs[i] -= s;
-    }
-    __syncthreads();
-  }
-  const int last = ((n - 1) / 32) * 32;
-  for (int p0 = last; p0 >= 0; p0 -= 32) {  // L^T x = y
-    const int pw = min(32, n - p0);
-    // contributions of the already solved rows below the panel: xs[r] -= sum_i L(i, r) x_i
-    for (int r = warp; r < pw; r += blockDim.x / 32) {
-      T s = T(0);
-      for (int i = p0 + pw + lane; i < n; i += 32) s += L[i + (long long)(p0 + r) * ld] * xs[i];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) xs[p0 + r] -= s;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      for (int c = pw - 1; c >= 0; --c) {
-        if (lane == c) xs[p0 + c] /= L[(p0 + c) + (long long)(p0 + c) * ld];
-        __syncwarp();
-        if (lane < c) xs[p0 + lane] -= L[(p0 + c) + (long long)(p0 + lane) * ld] * xs[p0 + c];
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-  }
-}
-
 struct Params {
   int batch;
   const int* n;
@@ -102,13 +54,15 @@ struct Params {
   double* B;
   float* L32;    // fp32 factors (offA layout), fp32 + IR mode only
   int nrhs;
-  int mode;      // 0 plain FP64, 1 fp32 + IR
   int refine;    // IR steps
   int* info;     // per matrix: 0 or first bad pivot
   unsigned long long* head;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) batched_kernel(Params P) {
+// MODE 0: plain FP64 (one CTA per SM: 128 KB of shared memory for the FP64 block ops);
+// MODE 1: fp32 + IR (64 KB of shared memory, two CTAs per SM)
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, MODE == 0 ? 1 : 2) batched_kernel(Params P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_idx;
   __shared__ double xd[kMaxN];  // FP64 vector (solution / residual)
@@ -129,7 +83,7 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(Params P) {
     }
     double* A = P.A + P.offA[idx];
     double* B = P.B + P.offB[idx];
-    if (P.mode == 0) {
+    if constexpr (MODE == 0) {
       const int inf = factor<double>(A, n, n, (double*)smem_raw);
       if (threadIdx.x == 0) P.info[idx] = inf;
       if (inf) continue;
@@ -179,12 +133,50 @@ __global__ void __launch_bounds__(kThreads, 1) batched_kernel(Params P) {
 std::mutex g_mtx;
 int g_sms = 0;
 bool g_attr = false;
+constexpr size_t kSmem64 = (size_t)kBlk * kBlk * sizeof(double) + 64;
+constexpr size_t kSmem32 = (size_t)kBlk * kBlk * sizeof(float) + 64;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform_elem(uint64_t seed, long long i, long long j) {
+  const uint64_t r = mix64(mix64(seed) ^ (((uint64_t)i << 32) | (uint64_t)(uint32_t)j));
+  return __dsub_rn(__dmul_rn((double)(r >> 11), 1.0 / 9007199254740992.0), 0.5);
+}
+
+// matrix k of the batch: (M + M^T)/2 + n*I with M_ij uniform in [-0.5, 0.5) from the counter-based
+// generator with seed (seed + k * 0x9e3779b97f4a7c15); one CTA-strided loop per matrix
+__global__ void gen_batch_kernel(int batch, const int* n, const long long* offA, unsigned long long seed, double* A) {
+  for (int k = blockIdx.x; k < batch; k += gridDim.x) {
+    const int nk = n[k];
+    const uint64_t sk = seed + (uint64_t)k * 0x9e3779b97f4a7c15ULL;
+    double* out = A + offA[k];
+    for (long long e = threadIdx.x; e < (long long)nk * nk; e += blockDim.x) {
+      const int i = (int)(e % nk), j = (int)(e / nk);
+      double v;
+      if (i == j) v = __dadd_rn(uniform_elem(sk, i, i), (double)nk);
+      else v = __dmul_rn(0.5, __dadd_rn(uniform_elem(sk, i, j), uniform_elem(sk, j, i)));
+      out[e] = v;
+    }
+  }
+}
 
 }  // namespace batched
 }  // namespace gbx
 
 using namespace gbx;
 using namespace gbx::batched;
+
+extern "C" int gbx_dgen_uniform_sym_batched(int batch, const int* n, const long long* offA, unsigned long long seed,
+                                            double* A, void* stream) {
+  if (batch < 0 || (batch > 0 && (!n || !offA || !A))) return GBX_ERR_ARG;
+  if (batch == 0) return GBX_OK;
+  gen_batch_kernel<<<std::min(batch, 4096), 256, 0, (cudaStream_t)stream>>>(batch, n, offA, seed, A);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
 
 extern "C" int gbx_batched_order(int batch, const int* n_host, int* order_host) {
   if (batch < 0 || (batch > 0 && (!n_host || !order_host))) return GBX_ERR_ARG;
@@ -198,19 +190,28 @@ extern "C" int gbx_batched_order(int batch, const int* n_host, int* order_host) 
 extern "C" int gbx_dposv_batched(int batch, const int* n, const long long* offA, const long long* offB,
                                  const int* order, double* A, double* B, int nrhs, int mode, int refine, float* L32,
                                  int* info, void* work, size_t work_bytes, void* stream) {
-  if (batch < 0 || nrhs < 1 || (mode != 0 && mode != 1) || refine < 0) return GBX_ERR_ARG;
+  return gbx_dposv_batched_ex(batch, n, offA, offB, order, A, B, nrhs, mode, refine, L32, info, 0, work, work_bytes,
+                              stream);
+}
+
+extern "C" int gbx_dposv_batched_ex(int batch, const int* n, const long long* offA, const long long* offB,
+                                    const int* order, double* A, double* B, int nrhs, int mode, int refine, float* L32,
+                                    int* info, int ctas, void* work, size_t work_bytes, void* stream) {
+  if (batch < 0 || nrhs < 1 || (mode != 0 && mode != 1) || refine < 0 || ctas < 0) return GBX_ERR_ARG;
   if (batch == 0) return GBX_OK;
   if (!n || !offA || !offB || !order || !A || !B || !info || (mode == 1 && !L32)) return GBX_ERR_ARG;
   if (!work || work_bytes < 256) return GBX_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  const size_t smem = (size_t)kBlk * kBlk * sizeof(double) + 64;
   {
     std::lock_guard<std::mutex> lk(g_mtx);
     if (!g_attr) {
       int dev = 0;
       cudaGetDevice(&dev);
       if (cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
-      if (cudaFuncSetAttribute(batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      if (cudaFuncSetAttribute(batched_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem64) !=
+              cudaSuccess ||
+          cudaFuncSetAttribute(batched_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem32) !=
+              cudaSuccess)
         return GBX_ERR_CUDA;
       g_attr = true;
     }
@@ -226,11 +227,13 @@ extern "C" int gbx_dposv_batched(int batch, const int* n, const long long* offA,
   P.B = B;
   P.L32 = L32;
   P.nrhs = nrhs;
-  P.mode = mode;
   P.refine = refine;
   P.info = info;
   P.head = (unsigned long long*)work;
-  const int grid = std::max(1, std::min(g_sms, batch));
-  batched_kernel<<<grid, kThreads, smem, s>>>(P);
+  // default grid: every resident CTA slot (1 per SM in FP64, 2 per SM in fp32 + IR); `ctas` overrides it
+  int grid = ctas > 0 ? ctas : (mode == 0 ? g_sms : 2 * g_sms);
+  grid = std::max(1, std::min(grid, batch));
+  if (mode == 0) batched_kernel<0><<<grid, kThreads, kSmem64, s>>>(P);
+  else batched_kernel<1><<<grid, kThreads, kSmem32, s>>>(P);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }

@@ -87,9 +87,12 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
 }
 
 // ------------------------------------------------------------------------------------------------
-// block POTRF (lower, n <= 128) in shared memory; right-looking, one column per step.
-// Returns 0 or the 1-based local index of the first non-positive pivot (LAPACK info); the
-// strict upper triangle of A is not touched. smem: 128 * 128 doubles + 1 int.
+// block POTRF (lower, n <= 128) in shared memory, blocked by 32 columns:
+//   1. warp 0 factors the 32 x 32 diagonal block (warp-synchronous, no CTA barrier per column)
+//   2. every thread solves one row below the block against it (row-wise substitution)
+//   3. all threads apply the block's rank-32 update to the trailing lower triangle
+// Returns 0 or the 1-based local index of the first non-positive pivot (LAPACK info); the strict
+// upper triangle of A is not touched. smem: 128 * 128 elements + 1 int.
 // ------------------------------------------------------------------------------------------------
 template <typename T>
 __device__ int op_potrf(T* A, int lda, int n, T* sm) {
@@ -103,22 +106,56 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
   }
   __syncthreads();
   int info = 0;
-  for (int j = 0; j < n; ++j) {
-    if (tid == 0) {
-      const T d = S[j + kBlk * j];
-      if (!(d > T(0))) *flag = j + 1;
-      else S[j + kBlk * j] = sqrt(d);
+  for (int p0 = 0; p0 < n; p0 += 32) {
+    const int pw = min(32, n - p0);
+    if (warp == 0) {
+      const int r = p0 + lane;  // this lane's row of the diagonal block
+      for (int j = 0; j < pw; ++j) {
+        const int c = p0 + j;
+        if (lane == j) {
+          const T d = S[c + kBlk * c];
+          if (!(d > T(0))) {
+            if (*flag == 0) *flag = c + 1;
+          } else {
+            S[c + kBlk * c] = sqrt(d);
+          }
+        }
+        __syncwarp();
+        if (*flag) break;
+        const T ljj = S[c + kBlk * c];
+        if (lane > j && lane < pw) S[r + kBlk * c] = S[r + kBlk * c] / ljj;
+        __syncwarp();
+        if (lane > j && lane < pw) {
+          const T lrj = S[r + kBlk * c];
+          for (int cc = c + 1; cc <= r; ++cc) S[r + kBlk * cc] = fma(-lrj, S[cc + kBlk * c], S[r + kBlk * cc]);
+        }
+        __syncwarp();
+      }
     }
     __syncthreads();
     info = *flag;
     if (info) break;
-    const T djj = S[j + kBlk * j];
-    for (int i = j + 1 + tid; i < n; i += kThreads) S[i + kBlk * j] = S[i + kBlk * j] / djj;
-    __syncthreads();
-    for (int c = j + 1 + warp; c < n; c += kThreads / 32) {
-      const T lcj = S[c + kBlk * j];
-      for (int i = c + lane; i < n; i += 32) S[i + kBlk * c] = fma(-S[i + kBlk * j], lcj, S[i + kBlk * c]);
+    // rows below the block: x (row r, columns p0..p0+pw) := x * L_blk^{-T}
+    for (int r = p0 + pw + tid; r < n; r += kThreads) {
+      for (int j = 0; j < pw; ++j) {
+        const int c = p0 + j;
+        T s0 = S[r + kBlk * c];
+        for (int k = p0; k < c; ++k) s0 = fma(-S[r + kBlk * k], S[c + kBlk * k], s0);
+        S[r + kBlk * c] = s0 / S[c + kBlk * c];
+      }
     }
+    __syncthreads();
+    // trailing update: S(i, c) -= sum_k S(i, k) S(c, k), p0+pw <= c <= i < n, k in the block
+    const int t0 = p0 + pw, m = n - t0;
+    for (int c = t0 + warp; c < n; c += kThreads / 32) {
+      for (int i = c + lane; i < n; i += 32) {
+        T s0 = S[i + kBlk * c];
+#pragma unroll 8
+        for (int k = p0; k < p0 + pw; ++k) s0 = fma(-S[i + kBlk * k], S[c + kBlk * k], s0);
+        S[i + kBlk * c] = s0;
+      }
+    }
+    (void)m;
     __syncthreads();
   }
   for (int idx = tid; idx < kBlk * n; idx += kThreads) {
@@ -211,5 +248,66 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
   }
 }
 
+
+// Triangular solves of one right-hand side held in shared memory xs[0..n) against the lower
+// factor L (column-major, ld), by 32-column panels: warp 0 solves the panel's triangle with
+// __syncwarp only, then the whole CTA applies the panel to the other rows (two CTA barriers per
+// panel instead of two per column).
+template <typename T>
+__device__ void fwd_solve(const T* L, int n, int ld, T* xs) {  // L y = x
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int p0 = 0; p0 < n; p0 += 32) {
+    const int pw = min(32, n - p0);
+    if (warp == 0) {
+      for (int c = 0; c < pw; ++c) {
+        if (lane == c) xs[p0 + c] /= L[(p0 + c) + (long long)(p0 + c) * ld];
+        __syncwarp();
+        if (lane > c && lane < pw) xs[p0 + lane] -= L[(p0 + lane) + (long long)(p0 + c) * ld] * xs[p0 + c];
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int i = p0 + pw + tid; i < n; i += blockDim.x) {
+      T s = T(0);
+      for (int c = 0; c < pw; ++c) s += L[i + (long long)(p0 + c) * ld] * xs[p0 + c];
+      xs[i] -= s;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__device__ void bwd_solve(const T* L, int n, int ld, T* xs) {  // L^T x = y
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int last = ((n - 1) / 32) * 32;
+  for (int p0 = last; p0 >= 0; p0 -= 32) {
+    const int pw = min(32, n - p0);
+    // contributions of the already solved rows below the panel: xs[r] -= sum_i L(i, r) x_i
+    for (int r = warp; r < pw; r += blockDim.x / 32) {
+      T s = T(0);
+      for (int i = p0 + pw + lane; i < n; i += 32) s += L[i + (long long)(p0 + r) * ld] * xs[i];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) xs[p0 + r] -= s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int c = pw - 1; c >= 0; --c) {
+        if (lane == c) xs[p0 + c] /= L[(p0 + c) + (long long)(p0 + c) * ld];
+        __syncwarp();
+        if (lane < c) xs[p0 + lane] -= L[(p0 + c) + (long long)(p0 + lane) * ld] * xs[p0 + c];
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// x := (L L^T)^{-1} x
+template <typename T>
+__device__ void solve_vec(const T* L, int n, int ld, T* xs) {
+  fwd_solve<T>(L, n, ld, xs);
+  bwd_solve<T>(L, n, ld, xs);
+}
 
 }  // namespace gbx

@@ -212,35 +212,18 @@ __global__ void set_head_kernel(DagState* st, unsigned long long head) {
 }
 
 // ---- tiled solve: forward (L y = b) and backward (L^T x = y) sweeps over b x b blocks ---------
-// diag solve of one block for all nrhs columns: column-oriented substitution, the columns of L
-// read straight from L2.
+// diag solve of one block for all nrhs columns, panel-blocked (fwd_solve / bwd_solve)
 __global__ void __launch_bounds__(kThreads) trsv_diag_kernel(BlockView V, int K, double* X, int ldx, int nrhs,
                                                              int trans) {
   __shared__ double xs[kBlk];
   const int kb = V.dim(K);
   const double* L = V.ptr(K, K);
-  const long long ld = V.ld;
   for (int r = 0; r < nrhs; ++r) {
     double* x = X + (long long)r * ldx + (long long)K * V.b;
     for (int i = threadIdx.x; i < kb; i += blockDim.x) xs[i] = x[i];
     __syncthreads();
-    if (!trans) {
-      for (int j = 0; j < kb; ++j) {
-        const double xj = xs[j] / L[j + j * ld];
-        __syncthreads();
-        if (threadIdx.x == 0) xs[j] = xj;
-        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) xs[i] = fma(-L[i + j * ld], xj, xs[i]);
-        __syncthreads();
-      }
-    } else {
-      for (int j = kb - 1; j >= 0; --j) {
-        const double xj = xs[j] / L[j + j * ld];
-        __syncthreads();
-        if (threadIdx.x == 0) xs[j] = xj;
-        for (int i = threadIdx.x; i < j; i += blockDim.x) xs[i] = fma(-L[j + i * ld], xj, xs[i]);
-        __syncthreads();
-      }
-    }
+    if (!trans) fwd_solve<double>(L, kb, V.ld, xs);
+    else bwd_solve<double>(L, kb, V.ld, xs);
     for (int i = threadIdx.x; i < kb; i += blockDim.x) x[i] = xs[i];
     __syncthreads();
   }

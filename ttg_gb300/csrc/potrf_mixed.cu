@@ -142,7 +142,6 @@ __device__ int task_potrf(const Params& P, int K, float* sm) {
       op_trsm<float>(A + p0 + (long long)p0 * NB, NB, A + r0 + (long long)p0 * NB, NB, min(kBlk, n - r0), pb, sm);
   }
   // condition estimate of the diagonal tile from its factor's diagonal
-  __shared__ float s_min, s_max;
   if (threadIdx.x == 0) {
     float mn = 3.0e38f, mx = 0.f;
     for (int i = 0; i < n; ++i) {
@@ -150,8 +149,6 @@ __device__ int task_potrf(const Params& P, int K, float* sm) {
       mn = fminf(mn, d);
       mx = fmaxf(mx, d);
     }
-    s_min = mn;
-    s_max = mx;
     const float est = (mx / mn) * (mx / mn);
     atomicMax((int*)P.cond_est, __float_as_int(est));  // positive floats order like their bits
   }
@@ -167,29 +164,47 @@ __device__ void task_trsm(const Params& P, int M, int K, int rb, float* sm) {
   float* B = P.W + sM * (long long)NB * NB;
   const float* L = P.W + slot_of(K, K, P.NT) * (long long)NB * NB;
   op_trsm<float>(L, NB, B + r0, NB, m, ncols, sm);
-  // low-precision row-major copy with one power-of-two exponent per row
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int i = warp; i < m; i += kThr / 32) {
-    const int r = r0 + i;
-    float mx = 0.f;
-    for (int c = lane; c < ncols; c += 32) mx = fmaxf(mx, fabsf(__ldcg(B + r + (long long)c * NB)));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    int e = 0;
-    if (mx > 0.f) frexpf(mx, &e);  // mx * 2^-e in [0.5, 1)
-    const float inv = pow2f(-e);
+  // low-precision row-major copy with one power-of-two exponent per row: two threads per row,
+  // column halves; loads coalesced across rows (column-major tile), 16-byte row-major stores
+  __shared__ float s_half_max[kThr];
+  const int t = threadIdx.x, i = t & (kBlk - 1), half = t >> 7;  // 128 rows x 2 halves
+  const int r = r0 + i;
+  const int cbeg = half * (NB / 2), cend = cbeg + NB / 2;
+  float mx = 0.f;
+  if (i < m)
+    for (int c = cbeg; c < cend && c < ncols; ++c) mx = fmaxf(mx, fabsf(__ldcg(B + r + (long long)c * NB)));
+  s_half_max[t] = mx;
+  __syncthreads();
+  mx = fmaxf(s_half_max[i], s_half_max[i + kBlk]);
+  int e = 0;
+  if (mx > 0.f) frexpf(mx, &e);  // mx * 2^-e in [0.5, 1)
+  const float inv = pow2f(-e);
+  if (i < m) {
     const long long base = sM * (long long)NB * NB + (long long)r * NB;
-    if (P.f16) {
-      __half* dst = (__half*)P.Lb + base;
-      for (int c = lane; c < NB; c += 32)
-        dst[c] = __float2half_rn(c < ncols ? __ldcg(B + r + (long long)c * NB) * inv : 0.f);
-    } else {
-      __nv_bfloat16* dst = (__nv_bfloat16*)P.Lb + base;
-      for (int c = lane; c < NB; c += 32)
-        dst[c] = __float2bfloat16_rn(c < ncols ? __ldcg(B + r + (long long)c * NB) * inv : 0.f);
+    for (int c0 = cbeg; c0 < cend; c0 += 8) {
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = (c0 + j < ncols) ? __ldcg(B + r + (long long)(c0 + j) * NB) * inv : 0.f;
+      uint4 pk;
+      uint32_t* w = (uint32_t*)&pk;
+      if (P.f16) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          __half2 h = __floats2half2_rn(v[2 * j], v[2 * j + 1]);
+          w[j] = *(uint32_t*)&h;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+          w[j] = *(uint32_t*)&h;
+        }
+      }
+      *(uint4*)((uint16_t*)P.Lb + base + c0) = pk;
     }
-    if (lane == 0) P.rowexp[sM * NB + r] = e;
+    if (half == 0) P.rowexp[sM * NB + r] = e;
   }
+  __syncthreads();
 }
 
 // ---- the persistent kernel ------------------------------------------------------------------------

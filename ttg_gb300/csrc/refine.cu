@@ -95,16 +95,26 @@ __global__ void fwd_update_kernel(const float* W, const float* Y, float* X, int 
   const float* L = W + slot_of(M, K, NT) * (long long)NB * NB;
   float acc[kMaxRhs];
   for (int j = 0; j < nrhs; ++j) acc[j] = 0.f;
-  for (int c = 0; c < kn; ++c) {
+  int c = 0;
+  for (; c + 8 <= kn; c += 8) {  // eight independent loads in flight per thread
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(L + i + (long long)(c + u) * NB);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      for (int j = 0; j < nrhs; ++j) acc[j] = fmaf(v[u], ys_f[j * NB + c + u], acc[j]);
+  }
+  for (; c < kn; ++c) {
     const float v = __ldg(L + i + (long long)c * NB);
     for (int j = 0; j < nrhs; ++j) acc[j] = fmaf(v, ys_f[j * NB + c], acc[j]);
   }
   for (int j = 0; j < nrhs; ++j) X[(long long)j * N + row] -= acc[j];
 }
 
-// backward step, diagonal part: z_K = L_KK^{-T} y_K; thread per output row i (coalesced over i)
+// backward step, diagonal part: z_K = L_KK^{-T} y_K. A CTA owns 32 output rows (lanes, coalesced
+// over i); its 8 warps split the column range and reduce through shared memory.
 __global__ void bwd_diag_kernel(const float* Inv, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs) {
-  extern __shared__ float ys_f[];  // [nrhs][NB]
+  extern __shared__ float ys_f[];  // [nrhs][NB] then [8 warps][nrhs][32] partial sums
   const int n = tdim(K, N, NB, NT);
   const float* out = Inv + (long long)K * NB * NB;
   for (int idx = threadIdx.x; idx < n * nrhs; idx += blockDim.x) {
@@ -112,15 +122,27 @@ __global__ void bwd_diag_kernel(const float* Inv, const float* Y, float* X, int 
     ys_f[j * NB + r] = Y[(long long)j * N + (long long)K * NB + r];
   }
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  float* part = ys_f + nrhs * NB;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
   float acc[kMaxRhs];
   for (int j = 0; j < nrhs; ++j) acc[j] = 0.f;
-  for (int c = i; c < n; ++c) {  // L^{-T} upper: (L^{-T})(i, c) = Out(i, c), c >= i
-    const float v = __ldg(out + i + (long long)c * NB);
-    for (int j = 0; j < nrhs; ++j) acc[j] = fmaf(v, ys_f[j * NB + c], acc[j]);
+  if (i < n) {
+    const int span = (n - i + nw - 1) / nw;
+    const int cb = i + warp * span, ce = min(n, cb + span);
+    for (int c = cb; c < ce; ++c) {  // L^{-T} upper: (L^{-T})(i, c) = Out(i, c), c >= i
+      const float v = __ldg(out + i + (long long)c * NB);
+      for (int j = 0; j < nrhs; ++j) acc[j] = fmaf(v, ys_f[j * NB + c], acc[j]);
+    }
   }
-  for (int j = 0; j < nrhs; ++j) X[(long long)j * N + (long long)K * NB + i] = acc[j];
+  for (int j = 0; j < nrhs; ++j) part[(warp * nrhs + j) * 32 + lane] = acc[j];
+  __syncthreads();
+  if (warp == 0 && i < n)
+    for (int j = 0; j < nrhs; ++j) {
+      float s = 0.f;
+      for (int w = 0; w < nw; ++w) s += part[(w * nrhs + j) * 32 + lane];
+      X[(long long)j * N + (long long)K * NB + i] = s;
+    }
 }
 
 // backward step, column update: y_J -= L_KJ^T z_K for every J < K; warp per output element c
@@ -323,7 +345,7 @@ int launch_ok() { return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CU
 int set_attrs() {
   static int done = 0;  // benign race: every caller sets the same values
   if (done) return GBX_OK;
-  const int big = 64 * 1024 + 1024;
+  const int big = 96 * 1024;
   if (cudaFuncSetAttribute(fwd_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(fwd_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(bwd_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
@@ -367,7 +389,8 @@ extern "C" int gbx_sprecond(int N, int NB, const float* W, const float* Inv, int
   }
   for (int K = NT - 1; K >= 0; --K) {  // L^T z = y
     const int kn = tdim(K, N, NB, NT);
-    bwd_diag_kernel<<<(kn + 127) / 128, 128, vs, s>>>(Inv, Y, X, N, NB, NT, K, nrhs);
+    bwd_diag_kernel<<<(kn + 31) / 32, 256, vs + (size_t)8 * nrhs * 32 * sizeof(float), s>>>(Inv, Y, X, N, NB, NT, K,
+                                                                                           nrhs);
     if (K > 0) {
       const long long above = (long long)K * NB;
       bwd_update_kernel<<<(unsigned)std::min<long long>((above + 7) / 8, 4096), 256, vs, s>>>(W, X, Y, N, NB, NT, K,
