@@ -54,6 +54,15 @@ int gbx_built_arch(void);
 void gbx_set_wait_timeout_ns(uint64_t ns);
 uint64_t gbx_get_wait_timeout_ns(void);
 
+/* Per-task timeline of the persistent executors (gbx_dpotrf_tiled, gbx_potrf_mixed and their
+ * variants), the counterpart of the reference's PaRSEC task tracing (bin/pbt_to_ctf.py). While a
+ * device buffer is set, every task of a later launch appends a record: buf[0] counts records,
+ * record i is buf[2+4i .. 5+4i] = {start ns, end ns (globaltimer), key = type<<60 | a<<40 | b<<20 | c
+ * (type 0 POTRF(a), 1 TRSM(a,b), 2 SYRK(a,b), 3 GEMM(a,b,c)), sub-task << 32 | CTA}. Records beyond
+ * `capacity` are dropped (the count keeps growing). Pass NULL to stop tracing. The caller zeroes
+ * buf[0] before a launch. ttg_gb300.trace_to_chrome() writes Chrome trace JSON. */
+void gbx_set_trace_buffer(unsigned long long* buf, int capacity);
+
 /* ============================================================================================
  * Tile kernels: drop-in replacements for the four vendor-library calls of the device bodies
  * of the potrf flowgraph. FP64, column-major tiles.

@@ -288,3 +288,27 @@ def test_full_size_solve_backward_error(gbx, cuda):
     r = A @ x - b
     berr = (r.abs().max() / (A.abs().sum(1).max() * x.abs().max() + b.abs().max())).item()
     assert berr <= 1e-14
+
+
+def test_task_timeline_trace(gbx, cuda, tmp_path):
+    """The per-task timeline records every executed task of the persistent executor."""
+    import json
+    import torch
+    N, NB = 1024, 256  # 128-blocks: NTb = 8
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=1)
+    buf = torch.zeros(2 + 4 * 1000, dtype=torch.int64, device=cuda)
+    gbx.lib().gbx_set_trace_buffer(_vp(buf), 1000)
+    try:
+        gbx.potrf_tiled(A, N, NB)
+    finally:
+        gbx.lib().gbx_set_trace_buffer(None, 0)
+    recs = gbx.trace_records(buf)
+    ntb = 8
+    assert len(recs) == ntb + ntb * (ntb - 1) + ntb * (ntb - 1) * (ntb - 2) // 6
+    assert all(r["end_ns"] >= r["start_ns"] for r in recs)
+    pot = {r["a"]: r for r in recs if r["type"] == "POTRF"}
+    trsm = [r for r in recs if r["type"] == "TRSM"]
+    assert all(t["start_ns"] >= pot[t["b"]]["end_ns"] for t in trsm)  # dependency order is visible
+    gbx.trace_to_chrome(recs, str(tmp_path / "t.json"))
+    assert len(json.load(open(tmp_path / "t.json"))["traceEvents"]) == len(recs)

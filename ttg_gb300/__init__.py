@@ -42,6 +42,7 @@ SIGNATURES = {
     "gbx_version": (_i, []),
     "gbx_built_arch": (_i, []),
     "gbx_set_wait_timeout_ns": (None, [_u64]),
+    "gbx_set_trace_buffer": (None, [_vp, _i]),
     "gbx_get_wait_timeout_ns": (_u64, []),
     "gbx_dpotrf_tile_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dpotrf_tile": (_i, [_i, _vp, _i, _vp, _sz, _vp, _vp]),
@@ -301,3 +302,34 @@ class Batch:
             out.append(Bh[o:o + k].reshape(self.nrhs, int(ni)))
             o += k
         return out
+
+
+TASK_NAMES = ["POTRF", "TRSM", "SYRK", "GEMM"]
+
+
+def trace_records(buf):
+    """Decodes a trace buffer (CUDA uint64 tensor given to gbx_set_trace_buffer) into dicts."""
+    import numpy as np
+    a = buf.cpu().numpy().view(np.uint64)
+    n = min(int(a[0]), (len(a) - 2) // 4)
+    rec = a[2:2 + 4 * n].reshape(n, 4)
+    out = []
+    for t0, t1, key, sc in rec:
+        key, sc = int(key), int(sc)
+        typ = key >> 60
+        out.append({"start_ns": int(t0), "end_ns": int(t1), "type": TASK_NAMES[typ], "a": (key >> 40) & 0xFFFFF,
+                    "b": (key >> 20) & 0xFFFFF, "c": key & 0xFFFFF, "sub": sc >> 32, "cta": sc & 0xFFFFFFFF})
+    return out
+
+
+def trace_to_chrome(records, path):
+    """Writes records (trace_records) as Chrome trace JSON (one row per CTA)."""
+    import json
+    if not records:
+        json.dump({"traceEvents": []}, open(path, "w"))
+        return
+    t0 = min(r["start_ns"] for r in records)
+    ev = [{"name": "%s(%d,%d,%d)" % (r["type"], r["a"], r["b"], r["c"]), "cat": r["type"], "ph": "X",
+           "ts": (r["start_ns"] - t0) / 1e3, "dur": (r["end_ns"] - r["start_ns"]) / 1e3, "pid": 0, "tid": r["cta"],
+           "args": {"sub": r["sub"]}} for r in records]
+    json.dump({"traceEvents": ev}, open(path, "w"))

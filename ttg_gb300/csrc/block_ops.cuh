@@ -191,21 +191,40 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
     }
     __syncthreads();
     if (p0 > 0) {
+      // P -= X(:, 0:p0) L(p0:p0+pw, 0:p0)^T, k in chunks of kKC; the next chunk is prefetched into
+      // registers while the current one is multiplied (hides the L2 latency)
       T acc[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-      for (int k0 = 0; k0 < p0; k0 += kKC) {
-        for (int idx = tid; idx < kKC * kBlk; idx += kThreads) {
+      T rx[kKC * kBlk / kThreads], rl[(kKC * kPW + kThreads - 1) / kThreads];
+      auto gload = [&](int k0) {
+#pragma unroll
+        for (int u = 0; u < kKC * kBlk / kThreads; ++u) {
+          const int idx = tid + u * kThreads;
           const int r = idx & (kBlk - 1), kk = idx >> 7;
-          Xc[idx] = (r < m) ? __ldcg(B + r + (long long)(k0 + kk) * ldb) : T(0);
+          rx[u] = (r < m && k0 + kk < p0) ? __ldcg(B + r + (long long)(k0 + kk) * ldb) : T(0);
         }
-        for (int idx = tid; idx < kKC * kPW; idx += kThreads) {
+#pragma unroll
+        for (int u = 0; u < (kKC * kPW + kThreads - 1) / kThreads; ++u) {
+          const int idx = tid + u * kThreads;
           const int c = idx & 31, kk = idx >> 5;
-          Lc[idx] = (c < pw) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : T(0);
+          rl[u] = (idx < kKC * kPW && c < pw && k0 + kk < p0) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : T(0);
         }
+      };
+      auto sstore = [&]() {
+#pragma unroll
+        for (int u = 0; u < kKC * kBlk / kThreads; ++u) Xc[tid + u * kThreads] = rx[u];
+#pragma unroll
+        for (int u = 0; u < (kKC * kPW + kThreads - 1) / kThreads; ++u)
+          if (tid + u * kThreads < kKC * kPW) Lc[tid + u * kThreads] = rl[u];
+      };
+      gload(0);
+      for (int k0 = 0; k0 < p0; k0 += kKC) {
+        sstore();
         __syncthreads();
+        if (k0 + kKC < p0) gload(k0 + kKC);
 #pragma unroll
         for (int kk = 0; kk < kKC; ++kk) {
           T a[4], b[4];
@@ -255,14 +274,20 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
 // panel instead of two per column).
 template <typename T>
 __device__ void fwd_solve(const T* L, int n, int ld, T* xs) {  // L y = x
+  __shared__ T tri[32 * 33];  // the panel's 32 x 32 triangle, staged once per panel
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int p0 = 0; p0 < n; p0 += 32) {
     const int pw = min(32, n - p0);
+    for (int idx = tid; idx < 32 * 32; idx += blockDim.x) {
+      const int r = idx & 31, c = idx >> 5;
+      tri[r + 33 * c] = (r < pw && c < pw && r >= c) ? L[(p0 + r) + (long long)(p0 + c) * ld] : T(0);
+    }
+    __syncthreads();
     if (warp == 0) {
       for (int c = 0; c < pw; ++c) {
-        if (lane == c) xs[p0 + c] /= L[(p0 + c) + (long long)(p0 + c) * ld];
+        if (lane == c) xs[p0 + c] /= tri[c + 33 * c];
         __syncwarp();
-        if (lane > c && lane < pw) xs[p0 + lane] -= L[(p0 + lane) + (long long)(p0 + c) * ld] * xs[p0 + c];
+        if (lane > c && lane < pw) xs[p0 + lane] -= tri[lane + 33 * c] * xs[p0 + c];
         __syncwarp();
       }
     }
@@ -278,6 +303,7 @@ __device__ void fwd_solve(const T* L, int n, int ld, T* xs) {  // L y = x
 
 template <typename T>
 __device__ void bwd_solve(const T* L, int n, int ld, T* xs) {  // L^T x = y
+  __shared__ T tri[32 * 33];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int last = ((n - 1) / 32) * 32;
   for (int p0 = last; p0 >= 0; p0 -= 32) {
@@ -290,12 +316,16 @@ __device__ void bwd_solve(const T* L, int n, int ld, T* xs) {  // L^T x = y
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0) xs[p0 + r] -= s;
     }
+    for (int idx = tid; idx < 32 * 32; idx += blockDim.x) {
+      const int r = idx & 31, c = idx >> 5;
+      tri[r + 33 * c] = (r < pw && c < pw && r >= c) ? L[(p0 + r) + (long long)(p0 + c) * ld] : T(0);
+    }
     __syncthreads();
     if (warp == 0) {
       for (int c = pw - 1; c >= 0; --c) {
-        if (lane == c) xs[p0 + c] /= L[(p0 + c) + (long long)(p0 + c) * ld];
+        if (lane == c) xs[p0 + c] /= tri[c + 33 * c];
         __syncwarp();
-        if (lane < c) xs[p0 + lane] -= L[(p0 + c) + (long long)(p0 + lane) * ld] * xs[p0 + c];
+        if (lane < c) xs[p0 + lane] -= tri[c + 33 * lane] * xs[p0 + c];
         __syncwarp();
       }
     }

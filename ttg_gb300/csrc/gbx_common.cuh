@@ -55,6 +55,26 @@ __device__ __forceinline__ void signal_done(int* cnt) {
   atomicAdd(cnt, 1);
 }
 
+// ---- optional per-task timeline ----------------------------------------------------------------
+// buf[0] counts records; record i (i >= 0) occupies buf[2 + 4i .. 5 + 4i]:
+//   start ns, end ns (globaltimer), key = type << 60 | a << 40 | b << 20 | c, sub << 32 | cta
+struct TraceBuf {
+  unsigned long long* buf;
+  int cap;
+};
+__device__ __forceinline__ void trace_record(const TraceBuf& tb, uint64_t t0, int type, int a, int b, int c, int sub) {
+  if (!tb.buf) return;
+  const unsigned long long i = atomicAdd(tb.buf, 1ULL);
+  if (i >= (unsigned long long)tb.cap) return;
+  unsigned long long* r = tb.buf + 2 + 4 * i;
+  r[0] = t0;
+  r[1] = globaltimer_ns();
+  r[2] = ((unsigned long long)type << 60) | ((unsigned long long)(a & 0xFFFFF) << 40) |
+         ((unsigned long long)(b & 0xFFFFF) << 20) | (unsigned long long)(c & 0xFFFFF);
+  r[3] = ((unsigned long long)(unsigned)sub << 32) | (unsigned long long)blockIdx.x;
+}
+TraceBuf current_trace();  // set by gbx_set_trace_buffer (host)
+
 // ---- addressing of b x b blocks inside NB x NB tiles of the tile-major lower storage ---------
 // A plain column-major matrix is the special case of a single tile (NT = 1) whose leading
 // dimension is the matrix's lda.

@@ -77,6 +77,7 @@ __host__ __device__ inline TaskKey dag_decode(long long t, int NTb) {
 }
 
 struct DagParams {
+  TraceBuf trace;
   BlockView V;
   int NTb;
   long long ntasks;
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     }
     __syncthreads();
     if (!s_go) break;
+    const uint64_t t_start = P.trace.buf ? globaltimer_ns() : 0;
     switch (tk.type) {
       case T_POTRF: {
         const int K = tk.a;
@@ -170,7 +172,10 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) signal_done(target);
+    if (threadIdx.x == 0) {
+      signal_done(target);
+      trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);
+    }
   }
 }
 
@@ -392,6 +397,11 @@ struct DevInfo {
 };
 std::mutex g_mtx;
 std::vector<DevInfo> g_dev;
+TraceBuf g_trace{nullptr, 0};
+TraceBuf current_trace() {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  return g_trace;
+}
 uint64_t g_timeout_ns = 20ull * 1000 * 1000 * 1000;
 
 int device_info(DevInfo& out) {
@@ -451,6 +461,7 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   P.st = st;
   P.cnt = (int*)((char*)work + sizeof(DagState));
   P.timeout_ns = timeout_ns;
+  P.trace = current_trace();
   long long grid = (long long)di.sms * di.dag_blocks_per_sm;
   grid = std::max(1LL, std::min(grid, P.ntasks));
   potrf_dag_f64_kernel<<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(P);
@@ -494,6 +505,11 @@ int gbx_built_arch(void) {
 #else
   return 0;
 #endif
+}
+
+void gbx_set_trace_buffer(unsigned long long* buf, int capacity) {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  g_trace = TraceBuf{capacity > 0 ? buf : nullptr, capacity > 0 ? capacity : 0};
 }
 
 void gbx_set_wait_timeout_ns(uint64_t ns) {

@@ -86,6 +86,7 @@ __host__ __device__ inline TileKey decode(long long t, int NT) {
 }
 
 struct Params {
+  TraceBuf trace;
   float* W;
   void* Lb;  // bf16 or fp16, row-major per tile
   int* rowexp;
@@ -275,6 +276,7 @@ __global__ void __launch_bounds__(kThr, 1)
     }
     __syncthreads();
     if (!s_go) break;
+    const uint64_t t_start = P.trace.buf ? globaltimer_ns() : 0;
 
     if (tk.type == T_POTRF) {
       const int info = task_potrf(P, tk.a, (float*)smem);
@@ -387,7 +389,10 @@ __global__ void __launch_bounds__(kThr, 1)
       target = P.cnt + tri_index(M, Nn, NT);
     }
     __syncthreads();
-    if (threadIdx.x == 0 && target) signal_done(target);
+    if (threadIdx.x == 0 && target) {
+      signal_done(target);
+      trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, sub);
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -496,6 +501,7 @@ extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int pre
   P.cnt = (int*)(base + w.cnt);
   P.cond_est = (float*)(base + w.cond);
   P.timeout_ns = gbx_get_wait_timeout_ns();
+  P.trace = current_trace();
   potrf_mixed_kernel<<<g_sms, kThr, kSmemBytes, s>>>(ta, tb, P);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
