@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--no-batched", action="store_true", help="skip the batched configuration")
     p.add_argument("--profile-case", choices=["dag", "mixed", "batched"], default=None,
                    help="run one small case of one kernel (N=8192) for an ncu capture; prints no JSON")
+    p.add_argument("--profile-N", type=int, default=8192, help="matrix order of --profile-case dag/mixed")
     return p.parse_args()
 
 
@@ -303,7 +304,8 @@ def run_ours(args, ws, rank, local):
         line["mixed"] = run_mixed(gbx, dev)
     if not args.no_batched:
         torch.cuda.empty_cache()
-        line["batched"] = run_batched(gbx, dev, reps=max(3, args.steps))
+        line["batched"] = run_batched(gbx, dev, reps=max(3, args.steps), cpu=rank == 0 and not args.no_cpu)
+    line["config_small"] = run_config1(gbx, dev, cpu=rank == 0 and not args.no_cpu)
 
     if rank == 0 and not args.no_cpu:
         times, blas = cpu_run(args.cpu_N, NB, 2)
@@ -400,7 +402,7 @@ def run_mixed(gbx, dev, N=32768, NB=512, nrhs=8, kappa=1e6):
     return out
 
 
-def run_batched(gbx, dev, count=4096, reps=3):
+def run_batched(gbx, dev, count=4096, reps=3, cpu=True):
     """4096 SPD systems, sizes uniform over 32*{1..16}, (M+M^T)/2 + n I, 1 right-hand side each:
     one persistent launch per solve, captured in a CUDA graph; FP64 and FP32 + 2 FP64 refinement
     steps."""
@@ -449,6 +451,74 @@ def run_batched(gbx, dev, count=4096, reps=3):
                      "refine_steps": refine, "info_nonzero": int((b.info != 0).sum().item())}
         if An is not None:
             out[mode]["backward_error_sampled"] = worst
+    if cpu:
+        # CPU counterpart: LAPACK dpotrf + dpotrs per matrix (OpenBLAS, one thread per matrix), all
+        # host cores over the matrices, largest first; the whole batch (not a sample)
+        import oracle
+        blas = oracle.load_openblas()
+        A_cpu = b.A0.cpu().numpy().copy()
+        B0 = np.concatenate([r.ravel() for r in rhs])
+        oracle.dposv_batched(sizes[:64], A_cpu[:int(np.sum(sizes[:64].astype(np.int64) ** 2))].copy(),
+                             B0[:int(np.sum(sizes[:64]))].copy(), use_blas=blas)  # warm-up
+        B_cpu = B0.copy()
+        t0 = time.perf_counter()
+        info = oracle.dposv_batched(sizes, A_cpu, B_cpu, nrhs=1, nthreads=cpu_cores(), use_blas=blas)
+        sec = time.perf_counter() - t0
+        assert not info.any()
+        out["cpu_baseline"] = {"value": count / sec, "unit": "matrices/s", "tflops": b.flops / sec / 1e12,
+                               "cores": cpu_cores(), "kind": "port",
+                               "sample": "the whole batch, FP64 dpotrf+dpotrs per matrix (%s), one matrix per thread"
+                                         % ("OpenBLAS" if blas else "plain loops")}
+    return out
+
+
+def run_config1(gbx, dev, cpu=True, reps=5):
+    """The reference's own CPU-runnable case, N=2048 NB=128 (FP64 factor only): the GPU executor and the
+    CPU restatement of the flowgraph on all host cores, both with the same seeded matrix."""
+    import numpy as np
+    import torch
+    N, NB = 2048, 128
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
+    gbx.gen_uniform_sym(A, N, NB, seed=42)
+    T = A.clone()
+    work = None
+    times = []
+    for i in range(reps + 1):
+        T.copy_(A)
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        work = gbx.potrf_tiled(T, N, NB, workspace=work, check=False)
+        e1.record()
+        e1.synchronize()
+        if i:
+            times.append(e0.elapsed_time(e1))
+    assert gbx.potrf_status(work) == 0
+    ms = statistics.median(times)
+    out = {"config": {"workload": "potrf FP64 N=%d NB=%d, (M+M^T)/2 + N*I seed 42" % (N, NB), "N": N, "NB": NB},
+           "gpu": {"ms": ms, "tflops": flops_factor(N) / (ms * 1e-3) / 1e12, "reps": reps}}
+    if cpu:
+        import oracle
+        blas = oracle.load_openblas()
+        ct, cg = [], []
+        for i in range(reps + 1):
+            t0 = time.perf_counter()
+            base = oracle.uniform_sym_tiles(N, NB, 42)
+            t1 = time.perf_counter()
+            st, _, _ = oracle.potrf_tiled(base, N, NB, nthreads=cpu_cores(), use_blas=blas)
+            t2 = time.perf_counter()
+            assert st == 0
+            if i:
+                ct.append(t2 - t1)
+                cg.append(t2 - t0)
+        sec = statistics.median(ct)
+        out["cpu_baseline"] = {"value": flops_factor(N) / sec / 1e12, "unit": "TFLOP/s", "ms": sec * 1e3,
+                               "ms_with_generation": statistics.median(cg) * 1e3, "cores": cpu_cores(),
+                               "kind": "port", "sample": "the whole N=%d factorisation, median of %d, %s tile kernels"
+                                                         % (N, reps, "OpenBLAS" if blas else "plain-loop")}
+        # the CPU and GPU factors of the same matrix agree
+        L = torch.from_numpy(base.reshape(-1)).to(dev)
+        out["max_abs_diff_gpu_vs_cpu"] = (L - T).abs().max().item()
     return out
 
 
@@ -490,14 +560,14 @@ def run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps):
             "api": "gbx_dpotrf_tiled + gbx_dpotrs_tiled (C ABI) with pinned host buffers"}
 
 
-def profile_case(case):
+def profile_case(case, N=8192):
     """One small case of one kernel (inputs larger than L2, a few GB at most), for ncu captures."""
     import torch
 
     import ttg_gb300 as gbx
     from ttg_gb300 import workloads
     dev = torch.device("cuda:0")
-    N, NB = 8192, 512
+    NB = 512
     if case in ("dag", "mixed"):
         A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
         gbx.gen_uniform_sym(A, N, NB, seed=42)
@@ -522,7 +592,7 @@ def profile_case(case):
 def main():
     args = parse()
     if args.profile_case:
-        profile_case(args.profile_case)
+        profile_case(args.profile_case, args.profile_N)
         return
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":

@@ -53,6 +53,9 @@ def lib():
         L.orc_check_dpotrf.argtypes = [ctypes.c_int, _dp, _dp]
         L.orc_frob_residual.restype = ctypes.c_double
         L.orc_frob_residual.argtypes = [ctypes.c_int, _dp, _dp]
+        L.orc_dposv_batched.argtypes = [ctypes.c_int, _ip, _i64p, _i64p, _dp, _dp, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, _ip]
+        L.orc_gen_uniform_sym_batched.argtypes = [ctypes.c_int, _ip, _i64p, ctypes.c_uint64, _dp]
         _lib = L
     return _lib
 
@@ -167,3 +170,29 @@ def frob_residual(L, A0):
     Lf = np.asfortranarray(L, dtype=np.float64)
     Af = np.asfortranarray(A0, dtype=np.float64)
     return lib().orc_frob_residual(N, _p(Lf), _p(Af))
+
+
+def batched_offsets(sizes, nrhs=1):
+    n = np.asarray(sizes, dtype=np.int32)
+    offA = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)]).astype(np.int64)
+    offB = np.concatenate([[0], np.cumsum(n.astype(np.int64) * nrhs)]).astype(np.int64)
+    return n, offA, offB
+
+
+def gen_uniform_sym_batched(sizes, seed=42):
+    """All matrices of the batched generator, concatenated column-major (offsets from batched_offsets)."""
+    n, offA, _ = batched_offsets(sizes)
+    A = np.empty(int(offA[-1]), dtype=np.float64)
+    lib().orc_gen_uniform_sym_batched(len(n), n.ctypes.data_as(_ip), offA.ctypes.data_as(_i64p), seed, _p(A))
+    return A
+
+
+def dposv_batched(sizes, A, B, nrhs=1, nthreads=0, use_blas=False):
+    """In place: A (concatenated column-major matrices) := factors, B := solutions. Returns info array."""
+    n, offA, offB = batched_offsets(sizes, nrhs)
+    assert A.dtype == np.float64 and A.flags.c_contiguous and A.size >= offA[-1]
+    assert B.dtype == np.float64 and B.flags.c_contiguous and B.size >= offB[-1]
+    info = np.zeros(len(n), dtype=np.int32)
+    lib().orc_dposv_batched(len(n), n.ctypes.data_as(_ip), offA.ctypes.data_as(_i64p), offB.ctypes.data_as(_i64p),
+                            _p(A), _p(B), nrhs, nthreads, 1 if use_blas else 0, info.ctypes.data_as(_ip))
+    return info

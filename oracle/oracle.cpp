@@ -530,3 +530,60 @@ extern "C" double orc_frob_residual(int N, const double* L, const double* A0) {
   }
   return std::sqrt(r2) / (N * std::sqrt(a2));
 }
+
+// ------------------------------------------------------------------------------------------------
+// batched solves: one LAPACK-style dpotrf + dpotrs per matrix, matrices spread over a thread pool
+// (the CPU counterpart of many independent small systems; the reference has no batched path)
+// ------------------------------------------------------------------------------------------------
+extern "C" void orc_dposv_batched(int batch, const int* n, const int64_t* offA, const int64_t* offB, double* A,
+                                  double* B, int nrhs, int nthreads, int use_blas, int* info) {
+  if (batch <= 0) return;
+  if (use_blas && !orc_blas_loaded()) use_blas = 0;
+  std::vector<int> order(batch);
+  for (int k = 0; k < batch; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return n[a] > n[b]; });
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (;;) {
+      const int t = next.fetch_add(1);
+      if (t >= batch) return;
+      const int k = order[t], nk = n[k];
+      double* a = A + offA[k];
+      double* b = B + offB[k];
+      int inf = 0;
+      if (use_blas) {
+        g_blas.potrf("L", &nk, a, &nk, &inf, 1);
+        if (inf == 0) {
+          const double one = 1.0;
+          g_blas.trsm("L", "L", "N", "N", &nk, &nrhs, &one, a, &nk, b, &nk, 1, 1, 1, 1);
+          g_blas.trsm("L", "L", "T", "N", &nk, &nrhs, &one, a, &nk, b, &nk, 1, 1, 1, 1);
+        }
+      } else {
+        inf = orc_potrf_tile(nk, a, nk);
+        if (inf == 0)
+          for (int r = 0; r < nrhs; ++r) {
+            double* x = b + (int64_t)r * nk;
+            for (int64_t j = 0; j < nk; ++j) {
+              x[j] /= a[j + j * nk];
+              for (int64_t i = j + 1; i < nk; ++i) x[i] -= a[i + j * nk] * x[j];
+            }
+            for (int64_t i = nk - 1; i >= 0; --i) {
+              double s = x[i];
+              for (int64_t q = i + 1; q < nk; ++q) s -= a[q + i * nk] * x[q];
+              x[i] = s / a[i + i * nk];
+            }
+          }
+      }
+      info[k] = inf;
+    }
+  };
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nthreads; ++t) pool.emplace_back(work);
+  for (auto& th : pool) th.join();
+}
+
+extern "C" void orc_gen_uniform_sym_batched(int batch, const int* n, const int64_t* offA, uint64_t seed, double* A) {
+  for (int k = 0; k < batch; ++k)
+    orc_gen_uniform_sym_colmajor(n[k], seed + (uint64_t)k * 0x9e3779b97f4a7c15ULL, (double)n[k], A + offA[k], n[k]);
+}

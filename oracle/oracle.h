@@ -80,6 +80,16 @@ double orc_check_dpotrf(int N, const double* L, const double* A0);
 /* ||A0 - L L^T||_F / (N ||A0||_F), A0 full symmetric col-major, L lower col-major */
 double orc_frob_residual(int N, const double* L, const double* A0);
 
+/* ---- batched solves (the per-matrix LAPACK loop a CPU user runs for many small systems) ---- */
+/* matrix k: n[k] x n[k] column-major at A + offA[k] (lower triangle read, factor written in place),
+ * right-hand sides n[k] x nrhs at B + offB[k] (overwritten by the solution). Matrices are taken
+ * largest first by nthreads workers (0 = all cores); use_blas: OpenBLAS dpotrf + dtrsm, else the
+ * plain-loop tile kernels. info[k] = 0 or the LAPACK info of the failed factorisation. */
+void orc_dposv_batched(int batch, const int* n, const int64_t* offA, const int64_t* offB, double* A,
+                       double* B, int nrhs, int nthreads, int use_blas, int* info);
+/* matrix k of the batched generator: (M+M^T)/2 + n*I, M from seed + k * 0x9e3779b97f4a7c15 */
+void orc_gen_uniform_sym_batched(int batch, const int* n, const int64_t* offA, uint64_t seed, double* A);
+
 #ifdef __cplusplus
 }
 #endif

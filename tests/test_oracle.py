@@ -121,3 +121,42 @@ def test_potrs_oracle():
     b = np.random.default_rng(1).standard_normal(N)
     x = oracle.potrs_tiled(t, N, NB, b)[:, 0]
     assert np.linalg.norm(A @ x - b) / (np.linalg.norm(A) * np.linalg.norm(x)) < 1e-15
+
+
+@pytest.mark.parametrize("use_blas", [False, True])
+def test_batched_oracle_against_numpy(use_blas):
+    if use_blas and not oracle.load_openblas():
+        pytest.skip("no OpenBLAS")
+    sizes = [1, 7, 32, 65, 96, 3, 128]
+    nrhs = 2
+    A = oracle.gen_uniform_sym_batched(sizes, seed=5)
+    n, offA, offB = oracle.batched_offsets(sizes, nrhs)
+    rng = np.random.default_rng(3)
+    B = rng.standard_normal(int(offB[-1]))
+    A0, B0 = A.copy(), B.copy()
+    info = oracle.dposv_batched(sizes, A, B, nrhs=nrhs, nthreads=3, use_blas=use_blas)
+    assert not info.any()
+    for k, nk in enumerate(sizes):
+        Ak = A0[offA[k]:offA[k + 1]].reshape(nk, nk).T
+        assert np.array_equal(Ak, Ak.T)
+        # generator: (M+M^T)/2 + n I from seed + k * golden-ratio constant
+        sk = (5 + k * 0x9e3779b97f4a7c15) % 2 ** 64
+        assert Ak[0, 0] == lib_elem(sk, 0, 0) + nk
+        Bk = B0[offB[k]:offB[k + 1]].reshape(nrhs, nk).T
+        Xk = B[offB[k]:offB[k + 1]].reshape(nrhs, nk).T
+        assert np.allclose(Xk, np.linalg.solve(Ak, Bk), rtol=1e-12, atol=1e-14)
+        Lk = np.tril(A[offA[k]:offA[k + 1]].reshape(nk, nk).T)
+        assert np.allclose(Lk, np.linalg.cholesky(Ak), rtol=1e-12, atol=1e-14)
+
+
+def lib_elem(seed, i, j):
+    return oracle.lib().orc_uniform_elem(seed, i, j)
+
+
+def test_batched_oracle_reports_bad_matrix():
+    sizes = [4, 6]
+    A = oracle.gen_uniform_sym_batched(sizes, seed=1)
+    A[16 + 2 + 2 * 6] = -5.0  # diagonal entry (2,2) of matrix 1
+    B = np.ones(10)
+    info = oracle.dposv_batched(sizes, A, B)
+    assert info[0] == 0 and info[1] == 3

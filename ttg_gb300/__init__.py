@@ -304,7 +304,8 @@ class Batch:
         return out
 
 
-TASK_NAMES = ["POTRF", "TRSM", "SYRK", "GEMM"]
+TASK_NAMES = ["POTRF", "TRSM", "SYRK", "GEMM", "potrf:gemm-updates", "potrf:block-potrf", "potrf:block-trsm",
+              "?", "?", "?", "?", "?", "?", "?", "?", "?"]
 
 
 def trace_records(buf):

@@ -94,6 +94,25 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
 // Returns 0 or the 1-based local index of the first non-positive pivot (LAPACK info); the strict
 // upper triangle of A is not touched. smem: 128 * 128 elements + 1 int.
 // ------------------------------------------------------------------------------------------------
+// One row of a 32-column panel held in registers: x := x * L_blk^{-T} (row-wise forward
+// substitution against the panel's lower triangle Lp, column-major with leading dimension ldp).
+template <typename T>
+__device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, int pw) {
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    if (c < pw) {
+      T s0 = x[c], s1 = T(0);
+#pragma unroll
+      for (int c2 = 0; c2 + 1 < c; c2 += 2) {
+        s0 = fma(-x[c2], Lp[c + ldp * c2], s0);
+        s1 = fma(-x[c2 + 1], Lp[c + ldp * (c2 + 1)], s1);
+      }
+      if (c & 1) s0 = fma(-x[c - 1], Lp[c + ldp * (c - 1)], s0);
+      x[c] = (s0 + s1) / Lp[c + ldp * c];
+    }
+  }
+}
+
 template <typename T>
 __device__ int op_potrf(T* A, int lda, int n, T* sm) {
   T* S = sm;                              // col-major, ld 128
@@ -109,53 +128,86 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
   for (int p0 = 0; p0 < n; p0 += 32) {
     const int pw = min(32, n - p0);
     if (warp == 0) {
-      const int r = p0 + lane;  // this lane's row of the diagonal block
-      for (int j = 0; j < pw; ++j) {
-        const int c = p0 + j;
-        if (lane == j) {
-          const T d = S[c + kBlk * c];
-          if (!(d > T(0))) {
-            if (*flag == 0) *flag = c + 1;
-          } else {
-            S[c + kBlk * c] = sqrt(d);
+      // 32 x 32 diagonal block: lane = row, the row in registers, columns exchanged by shuffles
+      T x[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) x[c] = (lane < pw && c <= lane) ? S[(p0 + lane) + kBlk * (p0 + c)] : T(0);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j < pw) {
+          const T d = __shfl_sync(0xffffffffu, x[j], j);
+          if (!(d > T(0))) {  // same value in every lane: the whole warp leaves together
+            if (lane == 0) *flag = p0 + j + 1;
+            break;
+          }
+          const T ljj = sqrt(d);
+          if (lane == j) x[j] = ljj;
+          else if (lane > j) x[j] = x[j] / ljj;
+#pragma unroll
+          for (int cc = j + 1; cc < 32; ++cc) {
+            const T lcj = __shfl_sync(0xffffffffu, x[j], cc);
+            if (lane >= cc) x[cc] = fma(-x[j], lcj, x[cc]);
           }
         }
-        __syncwarp();
-        if (*flag) break;
-        const T ljj = S[c + kBlk * c];
-        if (lane > j && lane < pw) S[r + kBlk * c] = S[r + kBlk * c] / ljj;
-        __syncwarp();
-        if (lane > j && lane < pw) {
-          const T lrj = S[r + kBlk * c];
-          for (int cc = c + 1; cc <= r; ++cc) S[r + kBlk * cc] = fma(-lrj, S[cc + kBlk * c], S[r + kBlk * cc]);
-        }
-        __syncwarp();
       }
+      __syncwarp();
+      if (*flag == 0 && lane < pw)
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          if (c <= lane) S[(p0 + lane) + kBlk * (p0 + c)] = x[c];
     }
     __syncthreads();
     info = *flag;
     if (info) break;
-    // rows below the block: x (row r, columns p0..p0+pw) := x * L_blk^{-T}
+    // rows below the block: each thread solves one row in registers
     for (int r = p0 + pw + tid; r < n; r += kThreads) {
-      for (int j = 0; j < pw; ++j) {
-        const int c = p0 + j;
-        T s0 = S[r + kBlk * c];
-        for (int k = p0; k < c; ++k) s0 = fma(-S[r + kBlk * k], S[c + kBlk * k], s0);
-        S[r + kBlk * c] = s0 / S[c + kBlk * c];
-      }
+      T x[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) x[c] = c < pw ? S[r + kBlk * (p0 + c)] : T(0);
+      row_solve32<T>(x, S + p0 + kBlk * p0, kBlk, pw);
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        if (c < pw) S[r + kBlk * (p0 + c)] = x[c];
     }
     __syncthreads();
-    // trailing update: S(i, c) -= sum_k S(i, k) S(c, k), p0+pw <= c <= i < n, k in the block
-    const int t0 = p0 + pw, m = n - t0;
-    for (int c = t0 + warp; c < n; c += kThreads / 32) {
-      for (int i = c + lane; i < n; i += 32) {
-        T s0 = S[i + kBlk * c];
-#pragma unroll 8
-        for (int k = p0; k < p0 + pw; ++k) s0 = fma(-S[i + kBlk * k], S[c + kBlk * k], s0);
-        S[i + kBlk * c] = s0;
+    // trailing update S(i, c) -= sum_k S(i, k) S(c, k), p0+pw <= c <= i < n, in 4 x 4 register blocks
+    const int t0 = p0 + pw, t = n - t0;
+    if (t > 0) {
+      const int nb4 = (t + 3) / 4;
+      const int nblk = nb4 * (nb4 + 1) / 2;
+      for (int q = tid; q < nblk; q += kThreads) {
+        int bj = 0, rem = q;  // lower 4 x 4 block (bi >= bj)
+        while (rem >= nb4 - bj) {
+          rem -= nb4 - bj;
+          ++bj;
+        }
+        const int bi = bj + rem;
+        const int i0 = t0 + 4 * bi, c0 = t0 + 4 * bj;
+        T acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+        for (int k = p0; k < p0 + pw; ++k) {
+          T vi[4], vc[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) vi[a] = (i0 + a < n) ? S[(i0 + a) + kBlk * k] : T(0);
+#pragma unroll
+          for (int b = 0; b < 4; ++b) vc[b] = (c0 + b < n) ? S[(c0 + b) + kBlk * k] : T(0);
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = fma(vi[a], vc[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int i = i0 + a, c = c0 + b;
+            if (i < n && c < n && i >= c) S[i + kBlk * c] -= acc[a][b];
+          }
       }
     }
-    (void)m;
     __syncthreads();
   }
   for (int idx = tid; idx < kBlk * n; idx += kThreads) {
@@ -172,12 +224,24 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
 // 128 x 32 x p0 GEMM, 4 x 4 micro-tiles), then each thread solves its own row across the panel.
 // smem: panel 32*128 + X chunk 16*128 + L chunk 16*32 + diagonal 32*32 doubles = 60 KB
 // ------------------------------------------------------------------------------------------------
+// k-chunk of the TRSM update: 64 for float (enough FMAs per chunk to cover the L2 latency of the
+// next chunk's prefetch), 16 for double (the FP64 pipe already hides it)
+template <typename T>
+struct TrsmChunk {
+  static constexpr int value = sizeof(T) == 4 ? 64 : kKC;
+};
+template <typename T>
+constexpr size_t op_trsm_smem_elems() {
+  return (size_t)kPW * kBlk + (size_t)TrsmChunk<T>::value * kBlk + (size_t)TrsmChunk<T>::value * kPW + kPW * kPW;
+}
+
 template <typename T>
 __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, int n, T* sm) {
+  constexpr int KC = TrsmChunk<T>::value;
   T* P = sm;                    // [kPW][128]  panel, P[c*128 + r]
-  T* Xc = P + kPW * kBlk;       // [kKC][128]
-  T* Lc = Xc + kKC * kBlk;      // [kKC][kPW]
-  T* Ld = Lc + kKC * kPW;       // [kPW][kPW]  Ld[c2*32 + c] = L(p0+c, p0+c2)
+  T* Xc = P + kPW * kBlk;       // [KC][128]
+  T* Lc = Xc + KC * kBlk;       // [KC][kPW]
+  T* Ld = Lc + KC * kPW;        // [kPW][kPW]  Ld[c2*32 + c] = L(p0+c, p0+c2)
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   for (int p0 = 0; p0 < n; p0 += kPW) {
     const int pw = min(kPW, n - p0);
@@ -191,42 +255,42 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
     }
     __syncthreads();
     if (p0 > 0) {
-      // P -= X(:, 0:p0) L(p0:p0+pw, 0:p0)^T, k in chunks of kKC; the next chunk is prefetched into
+      // P -= X(:, 0:p0) L(p0:p0+pw, 0:p0)^T, k in chunks of KC; the next chunk is prefetched into
       // registers while the current one is multiplied (hides the L2 latency)
       T acc[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-      T rx[kKC * kBlk / kThreads], rl[(kKC * kPW + kThreads - 1) / kThreads];
+      T rx[KC * kBlk / kThreads], rl[(KC * kPW + kThreads - 1) / kThreads];
       auto gload = [&](int k0) {
 #pragma unroll
-        for (int u = 0; u < kKC * kBlk / kThreads; ++u) {
+        for (int u = 0; u < KC * kBlk / kThreads; ++u) {
           const int idx = tid + u * kThreads;
           const int r = idx & (kBlk - 1), kk = idx >> 7;
           rx[u] = (r < m && k0 + kk < p0) ? __ldcg(B + r + (long long)(k0 + kk) * ldb) : T(0);
         }
 #pragma unroll
-        for (int u = 0; u < (kKC * kPW + kThreads - 1) / kThreads; ++u) {
+        for (int u = 0; u < (KC * kPW + kThreads - 1) / kThreads; ++u) {
           const int idx = tid + u * kThreads;
           const int c = idx & 31, kk = idx >> 5;
-          rl[u] = (idx < kKC * kPW && c < pw && k0 + kk < p0) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : T(0);
+          rl[u] = (idx < KC * kPW && c < pw && k0 + kk < p0) ? __ldcg(L + (p0 + c) + (long long)(k0 + kk) * ldl) : T(0);
         }
       };
       auto sstore = [&]() {
 #pragma unroll
-        for (int u = 0; u < kKC * kBlk / kThreads; ++u) Xc[tid + u * kThreads] = rx[u];
+        for (int u = 0; u < KC * kBlk / kThreads; ++u) Xc[tid + u * kThreads] = rx[u];
 #pragma unroll
-        for (int u = 0; u < (kKC * kPW + kThreads - 1) / kThreads; ++u)
-          if (tid + u * kThreads < kKC * kPW) Lc[tid + u * kThreads] = rl[u];
+        for (int u = 0; u < (KC * kPW + kThreads - 1) / kThreads; ++u)
+          if (tid + u * kThreads < KC * kPW) Lc[tid + u * kThreads] = rl[u];
       };
       gload(0);
-      for (int k0 = 0; k0 < p0; k0 += kKC) {
+      for (int k0 = 0; k0 < p0; k0 += KC) {
         sstore();
         __syncthreads();
-        if (k0 + kKC < p0) gload(k0 + kKC);
+        if (k0 + KC < p0) gload(k0 + KC);
 #pragma unroll
-        for (int kk = 0; kk < kKC; ++kk) {
+        for (int kk = 0; kk < KC; ++kk) {
           T a[4], b[4];
 #pragma unroll
           for (int i = 0; i < 4; ++i) a[i] = Xc[kk * kBlk + tx + 32 * i];
@@ -245,18 +309,14 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
         for (int j = 0; j < 4; ++j) P[(ty + 8 * j) * kBlk + tx + 32 * i] -= acc[i][j];
       __syncthreads();
     }
-    if (tid < m && tid < kBlk) {
+    if (tid < m && tid < kBlk) {  // each thread solves its row of the panel in registers
       const int r = tid;
-      for (int c = 0; c < pw; ++c) {
-        T s0 = P[c * kBlk + r], s1 = T(0);
-        int c2 = 0;
-        for (; c2 + 1 < c; c2 += 2) {
-          s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
-          s1 = fma(-P[(c2 + 1) * kBlk + r], Ld[(c2 + 1) * kPW + c], s1);
-        }
-        if (c2 < c) s0 = fma(-P[c2 * kBlk + r], Ld[c2 * kPW + c], s0);
-        P[c * kBlk + r] = (s0 + s1) / Ld[c * kPW + c];
-      }
+      T x[kPW];
+#pragma unroll
+      for (int c = 0; c < kPW; ++c) x[c] = P[c * kBlk + r];
+      row_solve32<T>(x, Ld, kPW, pw);  // Ld holds L(p0+c, p0+c2) at c + 32*c2
+#pragma unroll
+      for (int c = 0; c < kPW; ++c) P[c * kBlk + r] = x[c];
     }
     __syncthreads();
     for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {

@@ -419,7 +419,7 @@ int device_info(DevInfo& out) {
                              (int)(4 * kKC * kBlk * sizeof(double))) != cudaSuccess)
       return GBX_ERR_CUDA;
     if (cudaFuncSetAttribute(trsm_rlt_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)((kPW * kBlk + kKC * kBlk + kKC * kPW + kPW * kPW) * sizeof(double))) != cudaSuccess)
+                             (int)(op_trsm_smem_elems<double>() * sizeof(double))) != cudaSuccess)
       return GBX_ERR_CUDA;
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, potrf_dag_f64_kernel, kThreads, kDagSmemBytes) !=
@@ -546,7 +546,7 @@ int gbx_dtrsm_rlt_tile(int m, int n, const double* L, int ldl, double* B, int ld
   if (!L || !B) return GBX_ERR_ARG;
   DevInfo di;
   if (int e = device_info(di)) return e;
-  const size_t smem = (kPW * kBlk + kKC * kBlk + kKC * kPW + kPW * kPW) * sizeof(double);
+  const size_t smem = op_trsm_smem_elems<double>() * sizeof(double);
   trsm_rlt_grid_kernel<<<(m + kBlk - 1) / kBlk, kThreads, smem, (cudaStream_t)stream>>>(m, n, L, ldl, B, ldb);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }

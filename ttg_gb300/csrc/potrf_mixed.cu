@@ -131,17 +131,32 @@ __device__ __forceinline__ float pow2f(int e) {
 __device__ int task_potrf(const Params& P, int K, float* sm) {
   const int n = tdim(K, P), NB = P.NB;
   float* A = P.W + slot_of(K, K, P.NT) * (long long)NB * NB;
+  uint64_t ph[3] = {0, 0, 0};  // time in the three phases (tracing only)
   for (int p0 = 0; p0 < n; p0 += kBlk) {
     const int pb = min(kBlk, n - p0);
+    uint64_t t = P.trace.buf ? globaltimer_ns() : 0;
     if (p0 > 0)
       for (int r0 = p0; r0 < n; r0 += kBlk)
         op_gemm_nt<float>(A + r0, NB, A + p0, NB, A + r0 + (long long)p0 * NB, NB, min(kBlk, n - r0), pb, p0,
                           r0 == p0, sm);
+    if (P.trace.buf) {
+      const uint64_t u = globaltimer_ns();
+      ph[0] += u - t;
+      t = u;
+    }
     const int info = op_potrf<float>(A + p0 + (long long)p0 * NB, NB, pb, sm);
     if (info) return p0 + info;
+    if (P.trace.buf) {
+      const uint64_t u = globaltimer_ns();
+      ph[1] += u - t;
+      t = u;
+    }
     for (int r0 = p0 + kBlk; r0 < n; r0 += kBlk)
       op_trsm<float>(A + p0 + (long long)p0 * NB, NB, A + r0 + (long long)p0 * NB, NB, min(kBlk, n - r0), pb, sm);
+    if (P.trace.buf) ph[2] += globaltimer_ns() - t;
   }
+  if (P.trace.buf && threadIdx.x == 0)
+    for (int q = 0; q < 3; ++q) trace_record(P.trace, globaltimer_ns() - ph[q], 4 + q, K, 0, 0, 0);
   // condition estimate of the diagonal tile from its factor's diagonal
   if (threadIdx.x == 0) {
     float mn = 3.0e38f, mx = 0.f;

@@ -351,7 +351,8 @@ int set_attrs() {
       cudaFuncSetAttribute(bwd_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(bwd_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(symm_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(symm_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(symm_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
     return GBX_ERR_CUDA;
   done = 1;
   return GBX_OK;
@@ -360,8 +361,9 @@ int set_attrs() {
 
 extern "C" int gbx_spotri_diag(int N, int NB, const float* W, float* Inv, void* stream) {
   if (N <= 0 || NB <= 0 || NB > 1024 || !W || !Inv) return GBX_ERR_ARG;
+  if (int e = set_attrs()) return e;
   const int NT = (N + NB - 1) / NB;
-  const size_t smem = (kPW * kBlk + kKC * kBlk + kKC * kPW + kPW * kPW) * sizeof(float);
+  const size_t smem = op_trsm_smem_elems<float>() * sizeof(float);
   dim3 grid(NT, (NB + kBlk - 1) / kBlk);
   diag_inverse_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(W, Inv, N, NB, NT);
   return launch_ok();
