@@ -10,17 +10,48 @@ constexpr int kBlk = 128;      // largest block edge handled by one CTA
 constexpr int kKC = 16;        // k-chunk of the GEMM staging
 constexpr int kPW = 32;        // panel width of the TRSM
 
+// four consecutive elements from shared memory in 16-byte loads (p 16-byte aligned)
+__device__ __forceinline__ void lds4(const float* p, float (&v)[4]) {
+  const float4 f = *(const float4*)p;
+  v[0] = f.x;
+  v[1] = f.y;
+  v[2] = f.z;
+  v[3] = f.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&v)[4]) {
+  const double2 a = *(const double2*)p, b = *(const double2*)(p + 2);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = b.x;
+  v[3] = b.y;
+}
+
+// pivot of the Cholesky column: l = sqrt(d) and 1/l. FP32: hardware reciprocal square root with
+// one Newton step (r <- r (3 - d r^2) / 2), a few ulp, short latency on the factor's serial chain;
+// FP64: IEEE sqrt and division.
+__device__ __forceinline__ void chol_pivot(float d, float& l, float& inv) {
+  float r = rsqrtf(d);
+  r = r * fmaf(-0.5f * d * r, r, 1.5f);
+  inv = r;
+  l = d * r;
+}
+__device__ __forceinline__ void chol_pivot(double d, double& l, double& inv) {
+  l = sqrt(d);
+  inv = 1.0 / l;
+}
+
 // ------------------------------------------------------------------------------------------------
 // block GEMM:  C(m x n) := C - A(m x k) * B(n x k)^T   (lower: only i >= j of C is written)
-// 256 threads, each owning an 8 x 8 micro-tile (rows tx+16i, cols ty+16j); k staged through
-// shared memory in double-buffered chunks of 16 with a register prefetch of the next chunk.
-// smem: 2 * 2 * 16 * 128 doubles = 64 KB
+// 256 threads, each owning an 8 x 8 micro-tile (rows 4tx..4tx+3 and 64+4tx..64+4tx+3, the same
+// pattern of columns from ty), read from shared memory with 16-byte vector loads; k staged through
+// double-buffered chunks of 16 with a register prefetch of the next chunk.
+// smem: 2 * 2 * 16 * 128 elements (64 KB in FP64)
 // ------------------------------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb, T* C,
                                            int ldc, int m, int n, int k, bool lower, T* sm) {
   T* As = sm;                       // [2][kKC][kBlk]
-  T* Bs = sm + 2 * kKC * kBlk;           // [2][kKC][kBlk]
+  T* Bs = sm + 2 * kKC * kBlk;      // [2][kKC][kBlk]
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int lrow = tid & 127, lk0 = tid >> 7;
   T acc[8][8];
@@ -57,15 +88,18 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
       const T* bs = Bs + buf * kKC * kBlk;
 #pragma unroll
       for (int kk = 0; kk < kKC; ++kk) {
-        T a[8], b[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) a[i] = as[kk * kBlk + tx + 16 * i];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) b[j] = bs[kk * kBlk + ty + 16 * j];
+        T a0[4], a1[4], b0[4], b1[4];
+        lds4(as + kk * kBlk + 4 * tx, a0);
+        lds4(as + kk * kBlk + 64 + 4 * tx, a1);
+        lds4(bs + kk * kBlk + 4 * ty, b0);
+        lds4(bs + kk * kBlk + 64 + 4 * ty, b1);
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
-          for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < 8; ++j) {
+            const T ai = i < 4 ? a0[i & 3] : a1[i & 3], bj = j < 4 ? b0[j & 3] : b1[j & 3];
+            acc[i][j] = fma(ai, bj, acc[i][j]);
+          }
       }
       if (c + 1 < nchunks) sstore(buf ^ 1);
       __syncthreads();
@@ -73,10 +107,10 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
   }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const int col = ty + 16 * j;
+    const int col = (j < 4 ? 0 : 60) + 4 * ty + j;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      const int row = tx + 16 * i;
+      const int row = (i < 4 ? 0 : 60) + 4 * tx + i;
       if (row < m && col < n && (!lower || row >= col)) {
         T* p = C + row + (long long)col * ldc;
         __stcg(p, __ldcg(p) - acc[i][j]);
@@ -108,7 +142,7 @@ __device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, in
         s1 = fma(-x[c2 + 1], Lp[c + ldp * (c2 + 1)], s1);
       }
       if (c & 1) s0 = fma(-x[c - 1], Lp[c + ldp * (c - 1)], s0);
-      x[c] = (s0 + s1) / Lp[c + ldp * c];
+      x[c] = (s0 + s1) * (T(1) / Lp[c + ldp * c]);  // the reciprocal does not depend on x: off the chain
     }
   }
 }
@@ -140,13 +174,17 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
             if (lane == 0) *flag = p0 + j + 1;
             break;
           }
-          const T ljj = sqrt(d);
-          if (lane == j) x[j] = ljj;
-          else if (lane > j) x[j] = x[j] / ljj;
+          T ljj, inv;
+          chol_pivot(d, ljj, inv);
+          // column j of L in every lane (0 above the diagonal); selects, not branches, so the
+          // warp never diverges inside the column loop
+          const T lij = lane == j ? ljj : (lane > j ? x[j] * inv : T(0));
+          x[j] = lij;
 #pragma unroll
           for (int cc = j + 1; cc < 32; ++cc) {
-            const T lcj = __shfl_sync(0xffffffffu, x[j], cc);
-            if (lane >= cc) x[cc] = fma(-x[j], lcj, x[cc]);
+            const T lcj = __shfl_sync(0xffffffffu, lij, cc);
+            const T upd = fma(-lij, lcj, x[cc]);
+            x[cc] = lane >= cc ? upd : x[cc];
           }
         }
       }
@@ -290,12 +328,10 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
         __syncthreads();
         if (k0 + KC < p0) gload(k0 + KC);
 #pragma unroll
-        for (int kk = 0; kk < KC; ++kk) {
+        for (int kk = 0; kk < KC; ++kk) {  // rows 4tx..4tx+3 x columns 4ty..4ty+3, vector loads
           T a[4], b[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) a[i] = Xc[kk * kBlk + tx + 32 * i];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) b[j] = Lc[kk * kPW + ty + 8 * j];
+          lds4(Xc + kk * kBlk + 4 * tx, a);
+          lds4(Lc + kk * kPW + 4 * ty, b);
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -306,7 +342,7 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) P[(ty + 8 * j) * kBlk + tx + 32 * i] -= acc[i][j];
+        for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + 4 * tx + i] -= acc[i][j];
       __syncthreads();
     }
     if (tid < m && tid < kBlk) {  // each thread solves its row of the panel in registers
