@@ -289,8 +289,13 @@ def run_ours(args, ws, rank, local):
     peak = measure_fp64_gemm_peak(dev)
     dag_s = statistics.mean(dag_ms) * 1e-3
     achieved = flops_factor(N) / dag_s / 1e12
+    # DRAM traffic of one launch: ncu capture at N=16384 NB=512 (45.007 GB read + 44.713 GB written),
+    # scaled to this N by the number of block tasks (~N^3); N=32768 is too large to capture
+    traffic = (45.007e9 + 44.713e9) * (N / 16384.0) ** 3 if NB == 512 else None
     line["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                        "frac": achieved / peak, "traffic": None,
+                        "frac": achieved / peak, "traffic": traffic,
+                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
+                                          "N=16384 NB=512, scaled by block tasks (N^3)",
                         "kernel": "potrf_dag_f64_kernel",
                         "peak_source": "cuBLAS FP64 GEMM 4096^3 measured in this run (no FP64 entry in the "
                                        "measured-peaks file)"}
