@@ -310,6 +310,9 @@ def run_ours(args, ws, rank, local):
     if not args.no_batched:
         torch.cuda.empty_cache()
         line["batched"] = run_batched(gbx, dev, reps=max(3, args.steps), cpu=rank == 0 and not args.no_cpu)
+    if not args.no_batched:
+        torch.cuda.empty_cache()
+        line["batched_mixed"] = run_batched_mixed(gbx, dev, cpu=rank == 0 and not args.no_cpu)
     line["config_small"] = run_config1(gbx, dev, cpu=rank == 0 and not args.no_cpu)
 
     if rank == 0 and not args.no_cpu:
@@ -474,6 +477,91 @@ def run_batched(gbx, dev, count=4096, reps=3, cpu=True):
                                "cores": cpu_cores(), "kind": "port",
                                "sample": "the whole batch, FP64 dpotrf+dpotrs per matrix (%s), one matrix per thread"
                                          % ("OpenBLAS" if blas else "plain loops")}
+    return out
+
+
+def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, cpu_sample=16):
+    """Batched mixed precision: 256 SPD systems, n uniform in 128*{4..32}, H diag(lam) H^T with 2
+    reflectors (matrix k: seed 42 + k), kappa = 1e4, 4 right-hand sides each; one tensor-core
+    factorisation launch for the whole batch + batched FP64 PCG to backward error 1e-14. Against the
+    plain FP64 GPU path run matrix by matrix (gbx_dpotrf_tiled + gbx_dpotrs_tiled)."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    from ttg_gb300 import workloads
+    sizes = workloads.batch_sizes(count, 4, 32, 128, seed=42)
+    A, B = workloads.householder_batch(sizes, NB, 2, kappa, 42, dev, nrhs=nrhs)
+    flops = float(np.sum(sizes.astype(np.float64) ** 3) / 3)
+    out = {"config": {"workload": "%d SPD systems, n uniform in 128*{4..32}, H diag(lam) H^T (2 reflectors), "
+                                  "kappa=%g, %d rhs each, NB=%d" % (count, kappa, nrhs, NB),
+                      "count": count, "nrhs": nrhs, "kappa": kappa, "NB": NB, "flops": flops, "tolerance": 1e-14}}
+    offs, total = gbx.batched_tile_offsets(sizes, NB)
+    # plain FP64 GPU path, one matrix at a time
+    T = torch.empty_like(A)
+    X64 = B.clone()
+    work = torch.empty(gbx.potrf_workspace_bytes(int(sizes.max()), NB), dtype=torch.uint8, device=dev)
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    T.copy_(A)
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    vo = 0
+    for k, n in enumerate(sizes):
+        n = int(n)
+        tk = ctypes.c_void_p(T.data_ptr() + int(offs[k]) * 8)
+        gbx.call("gbx_dpotrf_tiled", n, NB, tk, ctypes.c_void_p(work.data_ptr()), work.numel(), sp)
+        gbx.call("gbx_dpotrs_tiled", n, NB, tk, nrhs, ctypes.c_void_p(X64.data_ptr() + vo * 8), n, sp)
+        vo += n * nrhs
+    e1.record()
+    e1.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    del T, work
+    torch.cuda.empty_cache()
+    out["plain_fp64_per_matrix"] = {"ms": plain_ms, "tflops": flops / (plain_ms * 1e-3) / 1e12}
+    for prec in ("fp16", "bf16"):
+        W = torch.empty(total, dtype=torch.float32, device=dev)
+        X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300, W=W)
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300, W=W)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        it = [i["iterations"] for i in infos]
+        be = [i["backward_error"] for i in infos]
+        fe = ((X - X64).abs().max() / X64.abs().max()).item()
+        out[prec] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "matrices_per_s": count / (ms * 1e-3),
+                     "speedup_vs_plain_fp64": plain_ms / ms, "status": st, "iterations_max": int(max(it)),
+                     "iterations_mean": float(np.mean(it)), "factor_retries": int(sum(i["factor_retries"] for i in infos)),
+                     "backward_error_max": float(max(be)), "forward_error_vs_fp64": fe}
+        del W
+        torch.cuda.empty_cache()
+    if cpu:
+        # CPU counterpart: LAPACK dpotrf + dpotrs per matrix (OpenBLAS, one matrix per thread) on a
+        # bounded sample: the first `cpu_sample` matrices of the batch
+        import oracle
+        blas = oracle.load_openblas()
+        ss = sizes[:cpu_sample]
+        An = A[:int(offs[cpu_sample])].cpu().numpy() if cpu_sample < count else A.cpu().numpy()
+        dense = []
+        for k, n in enumerate(ss):
+            n = int(n)
+            nt = (n + NB - 1) // NB
+            L = oracle.tiles_to_lower(An[int(offs[k]):int(offs[k]) + nt * (nt + 1) // 2 * NB * NB], n, NB)
+            dense.append(np.ascontiguousarray((L + np.tril(L, -1).T).T).ravel())
+        Ac = np.concatenate(dense)
+        Bc = B[:int(np.sum(ss) * nrhs)].cpu().numpy().copy()
+        t0 = time.perf_counter()
+        info = oracle.dposv_batched(ss, Ac, Bc, nrhs=nrhs, nthreads=cpu_cores(), use_blas=blas)
+        sec = time.perf_counter() - t0
+        assert not info.any()
+        sflops = float(np.sum(ss.astype(np.float64) ** 3) / 3)
+        out["cpu_baseline"] = {"value": sflops / sec / 1e12, "unit": "TFLOP/s", "cores": cpu_cores(), "kind": "port",
+                               "sample": "first %d matrices of the batch, FP64 dpotrf+dpotrs per matrix (%s), one "
+                                         "matrix per thread" % (cpu_sample, "OpenBLAS" if blas else "plain loops")}
     return out
 
 

@@ -207,6 +207,19 @@ typedef struct gbx_refine_info {
   float cond_estimate;   /* largest diagonal-tile condition estimate seen by the factorisation */
 } gbx_refine_info;
 
+/* Batched mixed-precision factorisation: the flowgraphs of many SPD matrices of uneven orders
+ * n[k] (host array) in ONE persistent launch whose device queue holds every matrix's tile tasks,
+ * largest matrix first. A and W: the matrices' tile-major lower storage (tile NB) concatenated in
+ * batch order (matrix k's tile slots follow matrix k-1's). sel (host, optional): factorise only the
+ * matrices with sel[k] != 0. A breakdown stops only its own matrix; gbx_potrf_mixed_batched_info
+ * returns per-matrix info (0 or the first bad pivot) and condition estimates, and synchronises.
+ * No counterpart in the reference. */
+int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes);
+int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
+                            const unsigned char* sel, void* work, size_t work_bytes, void* stream);
+int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info, float* cond_est,
+                                 void* stream);
+
 /* Bytes of workspace gbx_dposv_mixed needs. */
 int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes);
 
@@ -216,6 +229,17 @@ int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes);
  * down, GBX_ERR_NOCONV if `maxiter` iterations did not reach `tol`, or another error. */
 int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec, double tol,
                     int maxiter, float* W, void* work, size_t work_bytes, gbx_refine_info* info, void* stream);
+
+/* Batched gbx_dposv_mixed: matrices as for gbx_potrf_mixed_batched, right-hand sides and solutions
+ * of matrix k column-major n[k] x nrhs, concatenated in batch order. One factorisation launch for
+ * the batch (matrices that break down are factorised again, alone, with a growing diagonal shift),
+ * then preconditioned CG in FP64 where every step is one launch over the matrices that have not yet
+ * met `tol`. info (optional) receives one record per matrix. Returns 0 when every matrix met `tol`,
+ * GBX_ERR_NOCONV otherwise (or another error). No counterpart in the reference. */
+int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes);
+int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B, double* X,
+                            int prec, double tol, int maxiter, float* W, void* work, size_t work_bytes,
+                            gbx_refine_info* info, void* stream);
 
 /* ============================================================================================
  * Batched solves of many independent SPD matrices of uneven sizes in one persistent launch

@@ -62,3 +62,19 @@ def test_wait_timeout_setting(gbx):
     L.gbx_set_wait_timeout_ns(12345)
     assert L.gbx_get_wait_timeout_ns() == 12345
     L.gbx_set_wait_timeout_ns(old)
+
+
+def test_batched_mixed_workspace_without_gpu(gbx):
+    L = gbx.lib()
+    n = (ctypes.c_int * 3)(700, 256, 1300)
+    sz, one = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert L.gbx_dposv_mixed_batched_bufferSize(0, n, 256, 2, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_bufferSize(3, n, 200, 2, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_bufferSize(3, n, 256, 17, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
+    bad = (ctypes.c_int * 2)(100, 0)
+    assert L.gbx_potrf_mixed_batched_bufferSize(2, bad, 256, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_bufferSize(3, n, 256, 2, ctypes.byref(sz)) == 0
+    slots = sum((k + 255) // 256 * ((k + 255) // 256 + 1) // 2 for k in (700, 256, 1300))
+    assert sz.value > slots * 256 * 256 * 2  # at least the low-precision copies
+    assert L.gbx_dposv_mixed_bufferSize(700, 256, 2, ctypes.byref(one)) == 0
+    assert 0 < one.value < sz.value

@@ -95,3 +95,80 @@ def test_dsymm_tiled_matches_dense(gbx, cuda):
     Ad = torch.from_numpy(dense_from_tiles(A.cpu().numpy(), N, NB)).to(cuda)
     ref = 2.0 * Y0 - (Ad @ X.T).T
     assert (Y - ref).abs().max().item() <= 1e-12 * ref.abs().max().item()
+
+
+def batch_dense(A, sizes, NB, k):
+    import numpy as np
+    offs, _ = __import__("ttg_gb300").batched_tile_offsets(sizes, NB)
+    n = int(sizes[k])
+    nt = (n + NB - 1) // NB
+    t = A[int(offs[k]):int(offs[k]) + nt * (nt + 1) // 2 * NB * NB].cpu().numpy()
+    return dense_from_tiles(t, n, NB)
+
+
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+def test_dposv_mixed_batched_uneven(gbx, cuda, prec):
+    """Uneven (ragged) orders in one batch, kappa = 1e4: every matrix to backward error 1e-14, and the
+    factor of each matrix equal to the single-matrix launch's factor bit for bit (same tile order)."""
+    import torch
+    NB, nrhs = 256, 2
+    sizes = np.array([700, 256, 1300, 1024, 90, 513])
+    A, B = workloads.householder_batch(sizes, NB, 2, 1e4, 7, cuda, nrhs=nrhs)
+    X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300)
+    assert st == 0, infos
+    Xn, Bn = X.cpu().numpy(), B.cpu().numpy()
+    off = 0
+    for k, n in enumerate(sizes):
+        n = int(n)
+        Ad = batch_dense(A, sizes, NB, k)
+        Xk = Xn[off:off + n * nrhs].reshape(nrhs, n)
+        Bk = Bn[off:off + n * nrhs].reshape(nrhs, n)
+        off += n * nrhs
+        assert infos[k]["backward_error"] <= 1e-14, (k, infos[k])
+        for j in range(nrhs):
+            r = Bk[j] - Ad @ Xk[j]
+            be = np.abs(r).max() / (np.abs(Ad).sum(1).max() * np.abs(Xk[j]).max() + np.abs(Bk[j]).max())
+            assert be <= 1.5e-14, (k, be)
+    # the batched factorisation against one launch per matrix
+    offs, total = gbx.batched_tile_offsets(sizes, NB)
+    Wb = torch.empty(total, dtype=torch.float32, device=cuda)
+    n32 = np.ascontiguousarray(sizes.astype(np.int32))
+    import ctypes
+    need = ctypes.c_size_t(0)
+    gbx.call("gbx_potrf_mixed_batched_bufferSize", len(sizes), n32.ctypes.data_as(ctypes.c_void_p), NB,
+             ctypes.byref(need))
+    work = torch.empty(need.value, dtype=torch.uint8, device=cuda)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    gbx.call("gbx_potrf_mixed_batched", len(sizes), n32.ctypes.data_as(ctypes.c_void_p), NB,
+             ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(Wb.data_ptr()), gbx.PREC[prec], 0.0, None,
+             ctypes.c_void_p(work.data_ptr()), need.value, s)
+    info = np.zeros(len(sizes), dtype=np.int32)
+    gbx.call("gbx_potrf_mixed_batched_info", ctypes.c_void_p(work.data_ptr()), len(sizes),
+             n32.ctypes.data_as(ctypes.c_void_p), NB, info.ctypes.data_as(ctypes.c_void_p), None, s)
+    assert not info.any()
+    for k, n in enumerate(sizes):
+        n = int(n)
+        nt = (n + NB - 1) // NB
+        o = int(offs[k])
+        Ak = A[o:o + nt * (nt + 1) // 2 * NB * NB].clone()
+        W1, _, st1, _ = gbx.potrf_mixed(Ak, n, NB, prec=prec)
+        assert st1 == 0
+        Wk = Wb[o:o + W1.numel()]
+        Lb = oracle.tiles_to_lower(Wk.double().cpu().numpy(), n, NB)
+        L1 = oracle.tiles_to_lower(W1.double().cpu().numpy(), n, NB)
+        assert np.array_equal(Lb, L1), k
+
+
+def test_dposv_mixed_batched_reports_non_spd_member(gbx, cuda):
+    """One indefinite matrix in the batch: it is reported (no factor after every shift), the others
+    are solved."""
+    import torch
+    NB, nrhs = 256, 1
+    sizes = np.array([512, 300, 600])
+    A, B = workloads.householder_batch(sizes, NB, 2, 1e2, 3, cuda, nrhs=nrhs)
+    offs, _ = gbx.batched_tile_offsets(sizes, NB)
+    A[int(offs[1])] = -10.0  # A_00 of matrix 1
+    X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec="fp16", tol=1e-14)
+    assert st == gbx.GBX_ERR_NOCONV
+    assert infos[1]["backward_error"] == float("inf") and infos[1]["factor_retries"] == 8
+    assert infos[0]["backward_error"] <= 1e-14 and infos[2]["backward_error"] <= 1e-14

@@ -72,6 +72,11 @@ SIGNATURES = {
     "gbx_dposv_batched": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
     "gbx_dposv_batched_ex": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _sz, _vp]),
     "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
+    "gbx_potrf_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _szp]),
+    "gbx_potrf_mixed_batched": (_i, [_i, _vp, _i, _vp, _vp, _i, _d, _vp, _vp, _sz, _vp]),
+    "gbx_potrf_mixed_batched_info": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
+    "gbx_dposv_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _i, _szp]),
+    "gbx_dposv_mixed_batched": (_i, [_i, _vp, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
 }
 
 
@@ -227,6 +232,41 @@ def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=N
     if st < 0 and st != GBX_ERR_NOCONV:
         raise GbxError("gbx_dposv_mixed", st)
     return X, info.as_dict(), st
+
+
+def batched_tile_offsets(sizes, NB):
+    """Element offset of every matrix's first tile slot in a concatenated tile-major batch, and the total."""
+    import numpy as np
+    nt = (np.asarray(sizes, dtype=np.int64) + NB - 1) // NB
+    slots = nt * (nt + 1) // 2
+    off = np.concatenate([[0], np.cumsum(slots)]) * NB * NB
+    return off[:-1], int(off[-1])
+
+
+def dposv_mixed_batched(A_tiles, sizes, NB, B, nrhs, prec="fp16", tol=1e-14, maxiter=200, stream=None, work=None,
+                        W=None):
+    """Batched mixed-precision solve. A_tiles: concatenated tile-major lower matrices (CUDA float64,
+    batched_tile_offsets layout); B: concatenated column-major n_k x nrhs right-hand sides (CUDA
+    float64). Returns (X, list of per-matrix info dicts, status)."""
+    import numpy as np
+    import torch
+    n = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32))
+    batch = len(n)
+    need = _sz(0)
+    call("gbx_dposv_mixed_batched_bufferSize", batch, n.ctypes.data_as(ctypes.c_void_p), NB, nrhs,
+         ctypes.byref(need))
+    if work is None or work.numel() < need.value:
+        work = torch.empty(need.value, dtype=torch.uint8, device=A_tiles.device)
+    if W is None:
+        W = torch.empty(A_tiles.numel(), dtype=torch.float32, device=A_tiles.device)
+    X = torch.empty_like(B)
+    infos = (RefineInfo * batch)()
+    st = lib().gbx_dposv_mixed_batched(batch, n.ctypes.data_as(ctypes.c_void_p), NB, _ptr(A_tiles), nrhs, _ptr(B),
+                                       _ptr(X), PREC[prec], float(tol), int(maxiter), _ptr(W), _ptr(work),
+                                       need.value, ctypes.cast(infos, ctypes.c_void_p), _stream(stream))
+    if st < 0 and st != GBX_ERR_NOCONV:
+        raise GbxError("gbx_dposv_mixed_batched", st)
+    return X, [i.as_dict() for i in infos], st
 
 
 def gen_lowrank(tiles, N, NB, lam, U, V, G, stream=None):

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "block_ops.cuh"
 #include "gbx_common.cuh"
@@ -36,10 +37,13 @@ using namespace gbx::tc;
 
 constexpr int kThr = 256;            // 8 warps: 0 TMA, 1 MMA, 4..7 epilogue (tensor tasks); all (SIMT tasks)
 constexpr int kSubM = 128, kSubN = 256, kBK = 64, kStages = 4;
+constexpr int kTrsmRows = 64;   // rows of a TRSM sub-task
+constexpr int kMaxNB = 512;     // largest tile of the mixed path (the TRSM block lives in shared memory)
 constexpr uint32_t kABytes = kSubM * kBK * 2, kBBytes = kSubN * kBK * 2, kStageBytes = kABytes + kBBytes;
 constexpr size_t kTcSmem = (size_t)kStages * kStageBytes;  // 192 KB (1024-aligned ring)
 constexpr size_t kSimtSmem = (size_t)kBlk * kBlk * sizeof(float) + 64;
-constexpr size_t kSmemBytes = (kTcSmem > kSimtSmem ? kTcSmem : kSimtSmem) + 1024;
+constexpr size_t kTrsmSmem = (size_t)(kMaxNB * kTrsmRows + 32 * kMaxNB) * sizeof(float);
+constexpr size_t kSmemBytes = std::max(std::max(kTcSmem, kSimtSmem), kTrsmSmem) + 1024;
 
 enum : int { T_POTRF = 0, T_TRSM = 1, T_SYRK = 2, T_GEMM = 3 };
 
@@ -85,27 +89,56 @@ __host__ __device__ inline TileKey decode(long long t, int NT) {
   return TileKey{T_GEMM, n + (int)o, n, k};
 }
 
+// one matrix of the launch: its tile slots start at slot0 of the concatenated W / Lb / rowexp
+// arrays, its completion counters at cnt0
+struct MixMat {
+  long long slot0;
+  int N, NT, cnt0, id;  // id: index into the per-matrix info / condition arrays
+};
+// a run of consecutive queue positions [start, next segment's start) holding the sub-task slots
+// local0.. of one matrix's own task order. Segments are ordered by phase (phase p of a matrix: its
+// tasks from POTRF(p) up to POTRF(p+1)), then by matrix, so the matrices of a batch advance side by
+// side; every matrix still sees its own tasks in its own order, which keeps in-order grabbing free
+// of deadlock.
+struct MixSeg {
+  long long start, local0;
+  int mat, pad;
+};
+
 struct Params {
   TraceBuf trace;
   float* W;
   void* Lb;  // bf16 or fp16, row-major per tile
   int* rowexp;
-  int N, NB, NT;
+  int NB;
   int f16;     // 1: fp16 operands, 0: bf16
   int sub_g;   // GEMM sub-tasks per tile = (NB/128)*(NB/256)
-  int sub_t;   // TRSM sub-tasks per tile = NB/128
+  int sub_t;   // TRSM sub-tasks per tile = NB/64
+  int slots;   // queue slots per tile task = max of the sub-task counts
   int sub_s;   // SYRK sub-tasks per tile (lower 128 x 256 sub-tiles)
-  long long ntasks;  // tile tasks * sub_g
+  long long ntasks;  // sub-task slots of all matrices
+  const MixMat* mats;
+  int nmats;
+  const MixSeg* segs;  // ordered by start
+  int nsegs;
   DagState* st;
   int* cnt;
-  float* cond_est;  // max over diagonal tiles of (max L_ii / min L_ii)^2
+  int* minfo;       // per matrix: 0 or the first bad pivot (1-based, global row)
+  float* cond_est;  // per matrix: max over diagonal tiles of (max L_ii / min L_ii)^2
   uint64_t timeout_ns;
+};
+
+// the matrix a task belongs to, as every thread of the CTA sees it
+struct Cur {
+  long long slot0;
+  int N, NT, id;
+  int* cnt;
 };
 
 __device__ __forceinline__ long long slot_of(int m, int n, int NT) {
   return (long long)n * NT - (long long)n * (n - 1) / 2 + (m - n);
 }
-__device__ __forceinline__ int tdim(int t, const Params& P) { return t == P.NT - 1 ? P.N - (P.NT - 1) * P.NB : P.NB; }
+__device__ __forceinline__ int tdim(int t, const Cur& c, int NB) { return t == c.NT - 1 ? c.N - (c.NT - 1) * NB : NB; }
 
 // i-th lower 128 x 256 sub-tile of a diagonal tile (rows 128*si, cols 256*sj with 256*sj < 128*(si+1))
 __device__ __forceinline__ void syrk_sub(int idx, int NB, int& si, int& sj) {
@@ -128,9 +161,9 @@ __device__ __forceinline__ float pow2f(int e) {
 }
 
 // ---- FP32 SIMT tasks ---------------------------------------------------------------------------
-__device__ int task_potrf(const Params& P, int K, float* sm) {
-  const int n = tdim(K, P), NB = P.NB;
-  float* A = P.W + slot_of(K, K, P.NT) * (long long)NB * NB;
+__device__ int task_potrf(const Params& P, const Cur& cm, int K, float* sm) {
+  const int NB = P.NB, n = tdim(K, cm, NB);
+  float* A = P.W + (cm.slot0 + slot_of(K, K, cm.NT)) * (long long)NB * NB;
   uint64_t ph[3] = {0, 0, 0};  // time in the three phases (tracing only)
   for (int p0 = 0; p0 < n; p0 += kBlk) {
     const int pb = min(kBlk, n - p0);
@@ -166,41 +199,146 @@ __device__ int task_potrf(const Params& P, int K, float* sm) {
       mx = fmaxf(mx, d);
     }
     const float est = (mx / mn) * (mx / mn);
-    atomicMax((int*)P.cond_est, __float_as_int(est));  // positive floats order like their bits
+    atomicMax((int*)(P.cond_est + cm.id), __float_as_int(est));  // positive floats order like their bits
   }
   __syncthreads();
   return 0;
 }
 
-__device__ void task_trsm(const Params& P, int M, int K, int rb, float* sm) {
-  const int NB = P.NB, r0 = rb * kBlk, mrows = tdim(M, P), ncols = tdim(K, P);
+// TRSM(M, K) sub-task rb: rows 64 rb .. 64 rb + 63 of W(M,K) := W(M,K) L_KK^{-T}, then their scaled
+// low-precision row-major copy. The 64 x NB block stays in shared memory for the whole solve:
+// per 32-column panel, each of 64 threads solves its row in registers against the panel's
+// triangle, then all 256 threads apply the panel to the columns right of it (right-looking rank-32
+// update, 4 x 4 register micro-tiles with 16-byte shared loads).
+// smem: block [NB][64] + L panel [32][512] = 192 KB for NB = 512
+__device__ void task_trsm(const Params& P, const Cur& cm, int M, int K, int rb, float* sm) {
+  const int NB = P.NB, r0 = rb * kTrsmRows, mrows = tdim(M, cm, NB), n = tdim(K, cm, NB);
   if (r0 >= mrows) return;
-  const int m = min(kBlk, mrows - r0);
-  const long long sM = slot_of(M, K, P.NT);
-  float* B = P.W + sM * (long long)NB * NB;
-  const float* L = P.W + slot_of(K, K, P.NT) * (long long)NB * NB;
-  op_trsm<float>(L, NB, B + r0, NB, m, ncols, sm);
-  // low-precision row-major copy with one power-of-two exponent per row: two threads per row,
-  // column halves; loads coalesced across rows (column-major tile), 16-byte row-major stores
-  __shared__ float s_half_max[kThr];
-  const int t = threadIdx.x, i = t & (kBlk - 1), half = t >> 7;  // 128 rows x 2 halves
-  const int r = r0 + i;
-  const int cbeg = half * (NB / 2), cend = cbeg + NB / 2;
-  float mx = 0.f;
-  if (i < m)
-    for (int c = cbeg; c < cend && c < ncols; ++c) mx = fmaxf(mx, fabsf(__ldcg(B + r + (long long)c * NB)));
-  s_half_max[t] = mx;
+  const int m = min(kTrsmRows, mrows - r0);
+  const long long sM = cm.slot0 + slot_of(M, K, cm.NT);
+  float* B = P.W + sM * (long long)NB * NB + r0;
+  const float* L = P.W + (cm.slot0 + slot_of(K, K, cm.NT)) * (long long)NB * NB;
+  float* Bs = sm;                      // Bs[c * 64 + r]
+  float* Ls = sm + kMaxNB * kTrsmRows;  // Ls[c * 512 + ii] = L(p0 + ii, p0 + c)
+  const int tid = threadIdx.x;
+  // the block into shared memory: 16-byte loads, eight in flight per thread; rows past the
+  // matrix edge are zero (the tile slot holds NB rows, so the loads stay inside it)
+  for (int f0 = 0; f0 < n * (kTrsmRows / 4); f0 += 8 * kThr) {
+    float4 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int f = f0 + u * kThr + tid, c = f >> 4, r4 = (f & 15) * 4;
+      v[u] = f < n * (kTrsmRows / 4) ? __ldcg((const float4*)(B + r4 + (long long)c * NB)) : make_float4(0, 0, 0, 0);
+      if (r4 + 0 >= m) v[u].x = 0.f;
+      if (r4 + 1 >= m) v[u].y = 0.f;
+      if (r4 + 2 >= m) v[u].z = 0.f;
+      if (r4 + 3 >= m) v[u].w = 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int f = f0 + u * kThr + tid;
+      if (f < n * (kTrsmRows / 4)) *(float4*)(Bs + 4 * f) = v[u];
+    }
+  }
+  const int tr = tid & 15, tc = tid >> 4;  // update micro-tile: rows 4tr.., columns 4tc.. of a 64-column chunk
+  for (int p0 = 0; p0 < n; p0 += 32) {
+    const int pw = min(32, n - p0), span = n - p0;
+    __syncthreads();  // the previous panel's update is complete
+    // the panel's columns of L, rows p0.. : 16-byte loads, eight in flight per thread (rows past
+    // the edge stay inside the tile slot and are never read back)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int f = (h * 8 + u) * kThr + tid, c = f >> 7, ii = (f & 127) * 4;
+        if (c < pw && ii < span) v[u] = __ldcg((const float4*)(L + (p0 + ii) + (long long)(p0 + c) * NB));
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int f = (h * 8 + u) * kThr + tid, c = f >> 7, ii = (f & 127) * 4;
+        if (c < pw && ii < span) *(float4*)(Ls + c * kMaxNB + ii) = v[u];
+      }
+    }
+    __syncthreads();
+    if (tid < kTrsmRows) {
+      float x[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) x[c] = c < pw ? Bs[(p0 + c) * kTrsmRows + tid] : 0.f;
+      row_solve32<float>(x, Ls, kMaxNB, pw);
+#pragma unroll
+      for (int c = 0; c < 32; ++c)
+        if (c < pw) Bs[(p0 + c) * kTrsmRows + tid] = x[c];
+    }
+    __syncthreads();
+    // Bs(:, p0+jj) -= Bs(:, p0:p0+pw) * L(p0+jj, p0:p0+pw)^T for jj in [pw, span), chunks of 128
+    // columns; a thread owns rows 4tr..4tr+3 x columns jj..jj+7 (three 16-byte loads per 32 FMAs)
+    for (int j0 = pw; j0 < span; j0 += 128) {
+      const int jj = j0 + 8 * tc;
+      if (jj >= span) continue;
+      float acc[4][8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+      if (pw == 32 && jj + 8 <= span) {
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) {
+          float a[4], b0[4], b1[4];
+          lds4(Bs + (p0 + k) * kTrsmRows + 4 * tr, a);
+          lds4(Ls + k * kMaxNB + jj, b0);
+          lds4(Ls + k * kMaxNB + jj + 4, b1);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              acc[i][j] = fmaf(a[i], b0[j], acc[i][j]);
+              acc[i][j + 4] = fmaf(a[i], b1[j], acc[i][j + 4]);
+            }
+        }
+      } else {  // ragged panel or chunk edge
+        for (int k = 0; k < pw; ++k) {
+          float a[4], b[8];
+          lds4(Bs + (p0 + k) * kTrsmRows + 4 * tr, a);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) b[j] = jj + j < span ? Ls[k * kMaxNB + jj + j] : 0.f;
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (jj + j < span)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) Bs[(p0 + jj + j) * kTrsmRows + 4 * tr + i] -= acc[i][j];
+    }
+  }
   __syncthreads();
-  mx = fmaxf(s_half_max[i], s_half_max[i + kBlk]);
+  for (int idx = tid; idx < n * kTrsmRows; idx += kThr) {  // the solved block back to W
+    const int r = idx & (kTrsmRows - 1), c = idx >> 6;
+    if (r < m) __stcg(B + r + (long long)c * NB, Bs[idx]);
+  }
+  // low-precision row-major copy with one power-of-two exponent per row: four threads per row,
+  // column quarters, 16-byte row-major stores
+  __shared__ float s_q_max[kThr];
+  const int r = tid & (kTrsmRows - 1), q = tid >> 6;
+  const int cbeg = q * (NB / 4), cend = cbeg + NB / 4;
+  float mx = 0.f;
+  for (int c = cbeg; c < cend && c < n; ++c) mx = fmaxf(mx, fabsf(Bs[c * kTrsmRows + r]));
+  s_q_max[tid] = mx;
+  __syncthreads();
+  mx = fmaxf(fmaxf(s_q_max[r], s_q_max[r + 64]), fmaxf(s_q_max[r + 128], s_q_max[r + 192]));
   int e = 0;
   if (mx > 0.f) frexpf(mx, &e);  // mx * 2^-e in [0.5, 1)
   const float inv = pow2f(-e);
-  if (i < m) {
-    const long long base = sM * (long long)NB * NB + (long long)r * NB;
+  if (r < m) {
+    const long long base = sM * (long long)NB * NB + (long long)(r0 + r) * NB;
     for (int c0 = cbeg; c0 < cend; c0 += 8) {
       float v[8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = (c0 + j < ncols) ? __ldcg(B + r + (long long)(c0 + j) * NB) * inv : 0.f;
+      for (int j = 0; j < 8; ++j) v[j] = (c0 + j < n) ? Bs[(c0 + j) * kTrsmRows + r] * inv : 0.f;
       uint4 pk;
       uint32_t* w = (uint32_t*)&pk;
       if (P.f16) {
@@ -218,7 +356,7 @@ __device__ void task_trsm(const Params& P, int M, int K, int rb, float* sm) {
       }
       *(uint4*)((uint16_t*)P.Lb + base + c0) = pk;
     }
-    if (half == 0) P.rowexp[sM * NB + r] = e;
+    if (q == 0) P.rowexp[sM * NB + r0 + r] = e;
   }
   __syncthreads();
 }
@@ -230,8 +368,8 @@ __global__ void __launch_bounds__(kThr, 1)
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
   __shared__ uint32_t tmem_slot;
-  __shared__ long long s_task;
-  __shared__ int s_go, s_info;
+  __shared__ long long s_task, s_slot0;
+  __shared__ int s_go, s_info, s_N, s_NT, s_cnt0, s_id;
   __shared__ float s_colscale[kSubN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -246,7 +384,7 @@ __global__ void __launch_bounds__(kThr, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  const int NB = P.NB, NT = P.NT;
+  const int NB = P.NB;
   const int nkb = NB / kBK;
   uint32_t prod_it = 0, cons_it = 0, acc_phase = 0;  // pipeline positions, identical in every role
   int* err = &P.st->status;
@@ -256,58 +394,98 @@ __global__ void __launch_bounds__(kThr, 1)
     if (threadIdx.x == 0) {
       long long t = -1;
       if (!ld_volatile(&P.st->abort)) t = (long long)atomicAdd(&P.st->head, 1ULL);
-      s_task = (t >= 0 && t < P.ntasks) ? t : -1;
+      if (t >= 0 && t < P.ntasks) {
+        int lo = 0, hi = P.nsegs - 1;  // last segment with start <= t
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (P.segs[mid].start <= t) lo = mid;
+          else hi = mid - 1;
+        }
+        const MixSeg sg = P.segs[lo];
+        const MixMat mm = P.mats[sg.mat];
+        s_task = sg.local0 + (t - sg.start);
+        s_slot0 = mm.slot0;
+        s_N = mm.N;
+        s_NT = mm.NT;
+        s_cnt0 = mm.cnt0;
+        s_id = mm.id;
+      } else {
+        s_task = -1;
+      }
     }
     __syncthreads();
     const long long t = s_task;
     if (t < 0) break;
-    const TileKey tk = decode(t / P.sub_g, NT);
-    const int sub = (int)(t % P.sub_g);
+    Cur cm;
+    cm.slot0 = s_slot0;
+    cm.N = s_N;
+    cm.NT = s_NT;
+    cm.id = s_id;
+    cm.cnt = P.cnt + s_cnt0;
+    const int NT = cm.NT;
+    const TileKey tk = decode(t / P.slots, NT);
+    const int sub = (int)(t % P.slots);
     const int nsub = tk.type == T_POTRF ? 1 : tk.type == T_TRSM ? P.sub_t : tk.type == T_SYRK ? P.sub_s : P.sub_g;
     if (sub >= nsub) continue;  // unused slot of a task with fewer sub-tasks (uniform across the CTA)
     int* target = nullptr;
     if (threadIdx.x == 0) {
       bool ok = true;
       const int Sg = P.sub_g, St = P.sub_t, Ss = P.sub_s;
+      int* cnt = cm.cnt;
       switch (tk.type) {
         case T_POTRF:
-          ok = wait_geq(P.cnt + tri_index(tk.a, tk.a, NT), Ss * tk.a, P.st, P.timeout_ns);
+          ok = wait_geq(cnt + tri_index(tk.a, tk.a, NT), Ss * tk.a, P.st, P.timeout_ns);
           break;
         case T_TRSM:
-          ok = wait_geq(P.cnt + tri_index(tk.b, tk.b, NT), Ss * tk.b + 1, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.a, tk.b, NT), Sg * tk.b, P.st, P.timeout_ns);
+          ok = wait_geq(cnt + tri_index(tk.b, tk.b, NT), Ss * tk.b + 1, P.st, P.timeout_ns) &&
+               wait_geq(cnt + tri_index(tk.a, tk.b, NT), Sg * tk.b, P.st, P.timeout_ns);
           break;
         case T_SYRK:
-          ok = wait_geq(P.cnt + tri_index(tk.b, tk.a, NT), Sg * tk.a + St, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.b, tk.b, NT), Ss * tk.a, P.st, P.timeout_ns);
+          ok = wait_geq(cnt + tri_index(tk.b, tk.a, NT), Sg * tk.a + St, P.st, P.timeout_ns) &&
+               wait_geq(cnt + tri_index(tk.b, tk.b, NT), Ss * tk.a, P.st, P.timeout_ns);
           break;
         default:
-          ok = wait_geq(P.cnt + tri_index(tk.a, tk.c, NT), Sg * tk.c + St, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.b, tk.c, NT), Sg * tk.c + St, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.a, tk.b, NT), Sg * tk.c, P.st, P.timeout_ns);
+          ok = wait_geq(cnt + tri_index(tk.a, tk.c, NT), Sg * tk.c + St, P.st, P.timeout_ns) &&
+               wait_geq(cnt + tri_index(tk.b, tk.c, NT), Sg * tk.c + St, P.st, P.timeout_ns) &&
+               wait_geq(cnt + tri_index(tk.a, tk.b, NT), Sg * tk.c, P.st, P.timeout_ns);
           break;
       }
-      s_go = ok;
+      s_go = ok ? (ld_volatile(P.minfo + cm.id) ? 2 : 1) : 0;  // 2: the matrix already failed, skip the work
     }
     __syncthreads();
     if (!s_go) break;
+    if (s_go == 2) {  // a failed matrix: keep its counters moving so that its later tasks never wait
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int* c = cm.cnt;
+        if (tk.type == T_POTRF) signal_done(c + tri_index(tk.a, tk.a, NT));
+        else if (tk.type == T_TRSM) signal_done(c + tri_index(tk.a, tk.b, NT));
+        else if (tk.type == T_SYRK) signal_done(c + tri_index(tk.b, tk.b, NT));
+        else signal_done(c + tri_index(tk.a, tk.b, NT));
+      }
+      continue;
+    }
     const uint64_t t_start = P.trace.buf ? globaltimer_ns() : 0;
 
     if (tk.type == T_POTRF) {
-      const int info = task_potrf(P, tk.a, (float*)smem);
+      const int info = task_potrf(P, cm, tk.a, (float*)smem);
       if (threadIdx.x == 0) s_info = info;
       __syncthreads();
       if (s_info) {
-        if (threadIdx.x == 0) {
-          atomicCAS(&P.st->status, 0, tk.a * NB + s_info);
-          atomicExch(&P.st->abort, 1);
+        if (P.nmats == 1) {  // one matrix: stop the whole launch
+          if (threadIdx.x == 0) {
+            atomicCAS(P.minfo + cm.id, 0, tk.a * NB + s_info);
+            atomicCAS(&P.st->status, 0, tk.a * NB + s_info);
+            atomicExch(&P.st->abort, 1);
+          }
+          break;
         }
-        break;
+        if (threadIdx.x == 0) atomicCAS(P.minfo + cm.id, 0, tk.a * NB + s_info);  // others go on
       }
-      target = P.cnt + tri_index(tk.a, tk.a, NT);
+      target = cm.cnt + tri_index(tk.a, tk.a, NT);
     } else if (tk.type == T_TRSM) {
-      task_trsm(P, tk.a, tk.b, sub, (float*)smem);
-      target = P.cnt + tri_index(tk.a, tk.b, NT);
+      task_trsm(P, cm, tk.a, tk.b, sub, (float*)smem);
+      target = cm.cnt + tri_index(tk.a, tk.b, NT);
     } else {
       // tensor-core update of a 128 x 256 sub-tile of C = W(M,N) with L(M,K) L(N,K)^T
       int M, Nn, K, si, sj;
@@ -323,7 +501,8 @@ __global__ void __launch_bounds__(kThr, 1)
         sj = sub % (NB / kSubN);
       }
       const int r0 = si * kSubM, c0 = sj * kSubN;
-      const long long sA = slot_of(M, K, NT), sB = slot_of(Nn, K, NT), sC = slot_of(M, Nn, NT);
+      const long long sA = cm.slot0 + slot_of(M, K, NT), sB = cm.slot0 + slot_of(Nn, K, NT),
+                      sC = cm.slot0 + slot_of(M, Nn, NT);
       if (warp == 0 && lane == 0) {
         // operands were written by other CTAs with ordinary stores: order them before the async-proxy reads
         asm volatile("fence.proxy.async.global;" ::: "memory");
@@ -354,7 +533,7 @@ __global__ void __launch_bounds__(kThr, 1)
       } else if (warp >= 4) {
         const int q = warp & 3;
         const int r = r0 + q * 32 + lane;  // row of C handled by this thread
-        const int mrows = tdim(M, P), ncols = tdim(Nn, P);
+        const int mrows = tdim(M, cm, NB), ncols = tdim(Nn, cm, NB);
         float* C = P.W + sC * (long long)NB * NB;
         // while the MMAs run: column scales of this sub-tile into shared memory, C lines into L2
         for (int c = (warp - 4) * 32 + lane; c < kSubN; c += 128)
@@ -401,7 +580,7 @@ __global__ void __launch_bounds__(kThr, 1)
       if (warp != 1) cons_it += nkb;
       acc_phase ^= 1;
       tc_fence_before();
-      target = P.cnt + tri_index(M, Nn, NT);
+      target = cm.cnt + tri_index(M, Nn, NT);
     }
     __syncthreads();
     if (threadIdx.x == 0 && target) {
@@ -431,20 +610,43 @@ __global__ void shift_diag_kernel(float* W, int N, int NB, int NT, float shift) 
   for (int i = threadIdx.x; i < n; i += blockDim.x) W[slot * NB * NB + i + (long long)i * NB] *= 1.f + shift;
 }
 
-struct Ws {  // workspace layout
-  size_t state, cnt, cond, rowexp, lb, total;
+// workspace layout for a batch (one matrix is the batch of one): run state, completion counters,
+// per-matrix condition estimates and info, the matrix table, row exponents, low-precision copies
+struct Ws {
+  size_t state, cnt, cond, minfo, mats, segs, rowexp, lb, total;
+  long long slots, cnts, nsegs;
 };
-inline Ws layout(int N, int NB) {
-  const int NT = (N + NB - 1) / NB;
-  const size_t nslots = (size_t)NT * (NT + 1) / 2;
+inline size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+inline Ws layout_batch(int batch, const int* n, int NB) {
+  long long slots = 0, nsegs = 0;
+  for (int k = 0; k < batch; ++k) {
+    const long long nt = (n[k] + NB - 1) / NB;
+    slots += nt * (nt + 1) / 2;
+    nsegs += 4 * nt;  // queue segments: at most four task groups per phase, nt phases
+  }
   Ws w;
+  w.nsegs = nsegs;
+  w.slots = slots;
+  w.cnts = slots;  // one counter per tile
   w.state = 0;
   w.cnt = sizeof(DagState);
-  w.cond = w.cnt + (((size_t)nslots * sizeof(int) + 255) / 256) * 256;
-  w.rowexp = w.cond + 256;
-  w.lb = w.rowexp + (((nslots * NB * sizeof(int)) + 1023) / 1024) * 1024;
-  w.total = w.lb + nslots * (size_t)NB * NB * 2;
+  w.cond = up(w.cnt + (size_t)w.cnts * sizeof(int), 256);
+  w.minfo = up(w.cond + (size_t)batch * sizeof(float), 256);
+  w.mats = up(w.minfo + (size_t)batch * sizeof(int), 256);
+  w.segs = up(w.mats + (size_t)batch * sizeof(MixMat), 256);
+  w.rowexp = up(w.segs + (size_t)nsegs * sizeof(MixSeg), 1024);
+  w.lb = up(w.rowexp + (size_t)slots * NB * sizeof(int), 1024);
+  w.total = w.lb + (size_t)slots * NB * NB * 2;
   return w;
+}
+inline Ws layout(int N, int NB) { return layout_batch(1, &N, NB); }
+
+int sub_syrk(int NB) {
+  int ss = 0;
+  for (int j = 0; j < NB / kSubN; ++j)
+    for (int i = 0; i < NB / kSubM; ++i)
+      if (kSubN * j < kSubM * (i + 1)) ++ss;
+  return ss;
 }
 
 std::mutex g_mtx;
@@ -457,21 +659,15 @@ int g_sms = 0;
 using namespace gbx;
 using namespace gbx::mixed;
 
-extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes) {
-  if (N <= 0 || NB <= 0 || NB % 256 || NB > 1024 || !bytes) return GBX_ERR_ARG;
-  *bytes = layout(N, NB).total;
-  return GBX_OK;
-}
-
-extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work,
-                               size_t work_bytes, void* stream) {
-  if (N <= 0 || NB <= 0 || NB % 256 || NB > 1024 || !A || !W || !work || (prec != 0 && prec != 1))
-    return GBX_ERR_ARG;
-  const Ws w = layout(N, NB);
+namespace gbx {
+namespace mixed {
+// factorises the selected matrices of a batch (sel[k] != 0; all when sel is null) in one launch.
+// A, W: the matrices' tile-major lower storage concatenated in batch order (matrix k's slots follow
+// matrix k-1's). The table is ordered largest first so the longest critical paths start first.
+int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
+                 const unsigned char* sel, void* work, size_t work_bytes, cudaStream_t s) {
+  const Ws w = layout_batch(batch, n, NB);
   if (work_bytes < w.total) return GBX_ERR_WORKSPACE;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int NT = (N + NB - 1) / NB;
-  const long long nslots = (long long)NT * (NT + 1) / 2;
   {
     std::lock_guard<std::mutex> lk(g_mtx);
     if (!g_attr) {
@@ -484,41 +680,160 @@ extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int pre
       g_attr = true;
     }
   }
+  const int sub_g = (NB / kSubM) * (NB / kSubN);
+  const int sub_t = NB / kTrsmRows;
+  const int nslot = std::max(std::max(sub_g, sub_t), sub_syrk(NB));
+  // matrix table: slot / counter offsets in batch order, queue order largest first
+  std::vector<long long> slot0(batch);
+  long long acc = 0;
+  for (int k = 0; k < batch; ++k) {
+    slot0[k] = acc;
+    const long long nt = (n[k] + NB - 1) / NB;
+    acc += nt * (nt + 1) / 2;
+  }
+  std::vector<int> order;
+  for (int k = 0; k < batch; ++k)
+    if (!sel || sel[k]) order.push_back(k);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return n[a] > n[b]; });
+  std::vector<MixMat> mats(order.size());
+  int maxNT = 0;
+  for (size_t q = 0; q < order.size(); ++q) {
+    const int k = order[q];
+    const int nt = (n[k] + NB - 1) / NB;
+    mats[q].slot0 = slot0[k];
+    mats[q].N = n[k];
+    mats[q].NT = nt;
+    mats[q].cnt0 = (int)slot0[k];
+    mats[q].id = k;
+    maxNT = std::max(maxNT, nt);
+  }
+  // queue: phase by phase; within a phase, group by group (1: the updates of the next panel's
+  // column, 2: its POTRF, 3: its TRSMs, 4: the trailing updates), within a group the matrices
+  // largest first. The CTAs then find whole groups of independent tasks of many matrices instead
+  // of one matrix's dependent chain.
+  std::vector<MixSeg> segs;
+  long long task0 = 0;
+  auto group_range = [&](int nt, int p, int g, long long& first, long long& last) {
+    if (p == 0) {  // POTRF(0), then TRSM(m, 0)
+      first = g == 2 ? 0 : g == 3 ? 1 : 0;
+      last = g == 2 ? 1 : g == 3 ? nt : 0;
+      return;
+    }
+    const long long k = p - 1, R = nt - 1, r = nt - k - 1;
+    const long long base = nt + seg_prefix(k, R), len = seg_prefix(k + 1, R) - seg_prefix(k, R);
+    const long long lo[5] = {0, 0, r, r + 1, 2 * r}, hi[5] = {0, r, r + 1, 2 * r, len};
+    first = base + lo[g];
+    last = base + hi[g];
+  };
+  for (int p = 0; p < maxNT; ++p)
+    for (int g = 1; g <= 4; ++g)
+      for (size_t q = 0; q < mats.size(); ++q) {
+        const int nt = mats[q].NT;
+        if (nt <= p) continue;
+        long long first, last;
+        group_range(nt, p, g, first, last);
+        if (last <= first) continue;
+        segs.push_back(MixSeg{task0, first * nslot, (int)q, 0});
+        task0 += (last - first) * nslot;
+      }
+  if ((long long)segs.size() > w.nsegs) return GBX_ERR_WORKSPACE;  // the table must fit its reserved space
   char* base = (char*)work;
-  if (cudaMemsetAsync(base, 0, w.rowexp, s) != cudaSuccess) return GBX_ERR_CUDA;  // state, counters, cond
-  if (cudaMemsetAsync(base + w.lb, 0, w.total - w.lb, s) != cudaSuccess) return GBX_ERR_CUDA;
-  const long long nel = nslots * (long long)NB * NB;
-  convert_kernel<<<g_sms * 8, 256, 0, s>>>(A, W, nel);
-  if (shift != 0.0) shift_diag_kernel<<<NT, 256, 0, s>>>(W, N, NB, NT, (float)shift);
+  // state, counters, condition estimates and info are cleared for every matrix; the copies and
+  // exponents of the selected matrices are all rewritten by their TRSM tasks before any read
+  if (cudaMemsetAsync(base, 0, w.mats, s) != cudaSuccess) return GBX_ERR_CUDA;
+  if (mats.empty()) return GBX_OK;
+  if (cudaMemcpyAsync(base + w.mats, mats.data(), mats.size() * sizeof(MixMat), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(base + w.segs, segs.data(), segs.size() * sizeof(MixSeg), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
+    return GBX_ERR_CUDA;
+  // rows of a ragged tile's low-precision copy past the matrix edge are never written; the tensor
+  // cores read them, but they only reach rows / columns of C that the epilogue does not store
+  for (const MixMat& m : mats) {
+    const long long nsl = (long long)m.NT * (m.NT + 1) / 2, nel = nsl * (long long)NB * NB;
+    convert_kernel<<<std::min<long long>(g_sms * 8, (nel + 255) / 256), 256, 0, s>>>(
+        A + m.slot0 * (long long)NB * NB, W + m.slot0 * (long long)NB * NB, nel);
+    if (shift != 0.0)
+      shift_diag_kernel<<<m.NT, 256, 0, s>>>(W + m.slot0 * (long long)NB * NB, m.N, NB, m.NT, (float)shift);
+  }
   CUtensorMap ta, tb;
   const bool bf16 = prec == 0;
-  if (int e = tc::make_tmap_kmajor_16b(&ta, base + w.lb, (uint64_t)nslots * NB, (uint64_t)NB, (uint64_t)NB, kSubM, bf16))
+  if (int e = tc::make_tmap_kmajor_16b(&ta, base + w.lb, (uint64_t)w.slots * NB, (uint64_t)NB, (uint64_t)NB, kSubM, bf16))
     return e;
-  if (int e = tc::make_tmap_kmajor_16b(&tb, base + w.lb, (uint64_t)nslots * NB, (uint64_t)NB, (uint64_t)NB, kSubN, bf16))
+  if (int e = tc::make_tmap_kmajor_16b(&tb, base + w.lb, (uint64_t)w.slots * NB, (uint64_t)NB, (uint64_t)NB, kSubN, bf16))
     return e;
   Params P;
   P.W = W;
   P.Lb = base + w.lb;
   P.rowexp = (int*)(base + w.rowexp);
-  P.N = N;
   P.NB = NB;
-  P.NT = NT;
   P.f16 = prec == 1;
-  P.sub_g = (NB / kSubM) * (NB / kSubN);
-  P.sub_t = NB / kSubM;
-  int ss = 0;
-  for (int j = 0; j < NB / kSubN; ++j)
-    for (int i = 0; i < NB / kSubM; ++i)
-      if (kSubN * j < kSubM * (i + 1)) ++ss;
-  P.sub_s = ss;
-  P.ntasks = num_tile_tasks(NT) * P.sub_g;
+  P.sub_g = sub_g;
+  P.sub_t = sub_t;
+  P.slots = nslot;
+  P.sub_s = sub_syrk(NB);
+  P.ntasks = task0;
+  P.mats = (const MixMat*)(base + w.mats);
+  P.nmats = (int)mats.size();
+  P.segs = (const MixSeg*)(base + w.segs);
+  P.nsegs = (int)segs.size();
   P.st = (DagState*)base;
   P.cnt = (int*)(base + w.cnt);
+  P.minfo = (int*)(base + w.minfo);
   P.cond_est = (float*)(base + w.cond);
   P.timeout_ns = gbx_get_wait_timeout_ns();
   P.trace = current_trace();
   potrf_mixed_kernel<<<g_sms, kThr, kSmemBytes, s>>>(ta, tb, P);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+}  // namespace mixed
+}  // namespace gbx
+
+extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes) {
+  if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !bytes) return GBX_ERR_ARG;
+  *bytes = layout(N, NB).total;
+  return GBX_OK;
+}
+
+extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work,
+                               size_t work_bytes, void* stream) {
+  if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !A || !W || !work || (prec != 0 && prec != 1))
+    return GBX_ERR_ARG;
+  return launch_batch(1, &N, NB, A, W, prec, shift, nullptr, work, work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes) {
+  if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > kMaxNB || !bytes) return GBX_ERR_ARG;
+  for (int k = 0; k < batch; ++k)
+    if (n[k] <= 0) return GBX_ERR_ARG;
+  *bytes = layout_batch(batch, n, NB).total;
+  return GBX_OK;
+}
+
+extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec,
+                                       double shift, const unsigned char* sel, void* work, size_t work_bytes,
+                                       void* stream) {
+  size_t need = 0;
+  if (int e = gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &need)) return e;
+  if (!A || !W || !work || (prec != 0 && prec != 1)) return GBX_ERR_ARG;
+  return launch_batch(batch, n, NB, A, W, prec, shift, sel, work, work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info,
+                                            float* cond_est, void* stream) {
+  if (!work || batch <= 0 || !n || NB <= 0) return GBX_ERR_ARG;
+  const Ws w = layout_batch(batch, n, NB);
+  cudaStream_t s = (cudaStream_t)stream;
+  int st = 0;
+  if (cudaMemcpyAsync(&st, work, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GBX_ERR_CUDA;
+  if (info && cudaMemcpyAsync(info, (const char*)work + w.minfo, batch * sizeof(int), cudaMemcpyDeviceToHost, s) !=
+                  cudaSuccess)
+    return GBX_ERR_CUDA;
+  if (cond_est && cudaMemcpyAsync(cond_est, (const char*)work + w.cond, batch * sizeof(float), cudaMemcpyDeviceToHost,
+                                  s) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
+  return st < 0 ? st : GBX_OK;  // < 0: the launch itself failed (timeout)
 }
 
 extern "C" int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, void* stream) {

@@ -24,6 +24,12 @@ extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes);
 extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work,
                                size_t work_bytes, void* stream);
 extern "C" int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, void* stream);
+extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes);
+extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec,
+                                       double shift, const unsigned char* sel, void* work, size_t work_bytes,
+                                       void* stream);
+extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info,
+                                            float* cond_est, void* stream);
 
 namespace gbx {
 namespace refine {
@@ -35,10 +41,22 @@ __device__ __forceinline__ long long slot_of(int m, int n, int NT) {
 }
 __host__ __device__ __forceinline__ int tdim(int t, int N, int NB, int NT) { return t == NT - 1 ? N - (NT - 1) * NB : NB; }
 
+// One matrix of a batched call: its tiles start at tile slot slot0 of A (FP64) and W (FP32), its
+// diagonal-tile inverses at tile inv0 of Inv, its vectors (N x nrhs, column-major, leading
+// dimension N) at element vec0 of every vector array. A single matrix is the table {0, 0, 0, N, NT}.
+struct RMat {
+  long long slot0, inv0, vec0;
+  int N, NT;
+};
+
+// Every kernel body below works on one matrix (pointers already offset to it); the single-matrix
+// kernels call it directly, the batched kernels with the matrix list[blockIdx.z] of the table.
+#define GBX_MAT_OF_BLOCK() const RMat& mt = mats[list[blockIdx.z]]
+
 // Out = L_KK^{-T} (column-major), i.e. row r of Out holds column r of L_KK^{-1}; 128 rows per CTA
-__global__ void __launch_bounds__(kThreads, 1) diag_inverse_kernel(const float* W, float* Inv, int N, int NB, int NT) {
-  extern __shared__ __align__(16) float sm_f[];
+__device__ void diag_inverse_body(const float* W, float* Inv, int N, int NB, int NT, float* sm) {
   const int K = blockIdx.x, r0 = blockIdx.y * kBlk;
+  if (K >= NT) return;
   const int n = tdim(K, N, NB, NT);
   if (r0 >= n) return;
   const int m = min(kBlk, n - r0);
@@ -49,21 +67,33 @@ __global__ void __launch_bounds__(kThreads, 1) diag_inverse_kernel(const float* 
   }
   __syncthreads();
   const float* L = W + slot_of(K, K, NT) * (long long)NB * NB;
-  op_trsm<float>(L, NB, out + r0, NB, m, n, sm_f);
+  op_trsm<float>(L, NB, out + r0, NB, m, n, sm);
+}
+__global__ void __launch_bounds__(kThreads, 1) diag_inverse_kernel(const float* W, float* Inv, int N, int NB, int NT) {
+  extern __shared__ __align__(16) float sm_f[];
+  diag_inverse_body(W, Inv, N, NB, NT, sm_f);
+}
+__global__ void __launch_bounds__(kThreads, 1)
+    diag_inverse_batched(const RMat* mats, const int* list, const float* W, float* Inv, int NB) {
+  extern __shared__ __align__(16) float sm_f[];
+  GBX_MAT_OF_BLOCK();
+  diag_inverse_body(W + mt.slot0 * NB * NB, Inv + mt.inv0 * NB * NB, mt.N, NB, mt.NT, sm_f);
 }
 
 // forward step, diagonal part: y_K = L_KK^{-1} x_K (Out^T x_K), in place in x
 // one warp per output element c (lanes over r), all right-hand sides
-__global__ void fwd_diag_kernel(const float* Inv, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs) {
-  extern __shared__ float xs_f[];  // [nrhs][NB]
+__device__ void fwd_diag_body(const float* Inv, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs,
+                              float* xs_f) {
+  if (K >= NT) return;
   const int n = tdim(K, N, NB, NT);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (blockIdx.x * nw >= n) return;
   const float* out = Inv + (long long)K * NB * NB;
   for (int idx = threadIdx.x; idx < n * nrhs; idx += blockDim.x) {
     const int r = idx % n, j = idx / n;
     xs_f[j * NB + r] = X[(long long)j * N + (long long)K * NB + r];
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int c = blockIdx.x * nw + warp; c < n; c += gridDim.x * nw) {
     float acc[kMaxRhs];
     for (int j = 0; j < nrhs; ++j) acc[j] = 0.f;
@@ -79,17 +109,29 @@ __global__ void fwd_diag_kernel(const float* Inv, const float* X, float* Y, int 
     }
   }
 }
+__global__ void fwd_diag_kernel(const float* Inv, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs) {
+  extern __shared__ float xs_f[];  // [nrhs][NB]
+  fwd_diag_body(Inv, X, Y, N, NB, NT, K, nrhs, xs_f);
+}
+__global__ void fwd_diag_batched(const RMat* mats, const int* list, const float* Inv, const float* X, float* Y, int NB,
+                                 int K, int nrhs) {
+  extern __shared__ float xs_f[];
+  GBX_MAT_OF_BLOCK();
+  fwd_diag_body(Inv + mt.inv0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, K, nrhs, xs_f);
+}
 
 // forward step, column update: x_M -= L_MK y_K for every M > K; thread per row, y_K in smem
-__global__ void fwd_update_kernel(const float* W, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs) {
-  extern __shared__ float ys_f[];  // [nrhs][NB]
+__device__ void fwd_update_body(const float* W, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs,
+                                float* ys_f) {
+  const long long row0 = (long long)(K + 1) * NB + (long long)blockIdx.x * blockDim.x;
+  if (K >= NT || row0 >= N) return;  // whole CTA past the matrix
   const int kn = tdim(K, N, NB, NT);
   for (int idx = threadIdx.x; idx < kn * nrhs; idx += blockDim.x) {
     const int r = idx % kn, j = idx / kn;
     ys_f[j * NB + r] = Y[(long long)j * N + (long long)K * NB + r];
   }
   __syncthreads();
-  const long long row = (long long)(K + 1) * NB + (long long)blockIdx.x * blockDim.x + threadIdx.x;  // global row
+  const long long row = row0 + threadIdx.x;  // global row
   if (row >= N) return;
   const int M = (int)(row / NB), i = (int)(row % NB);
   const float* L = W + slot_of(M, K, NT) * (long long)NB * NB;
@@ -110,12 +152,24 @@ __global__ void fwd_update_kernel(const float* W, const float* Y, float* X, int 
   }
   for (int j = 0; j < nrhs; ++j) X[(long long)j * N + row] -= acc[j];
 }
+__global__ void fwd_update_kernel(const float* W, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs) {
+  extern __shared__ float ys_f[];  // [nrhs][NB]
+  fwd_update_body(W, Y, X, N, NB, NT, K, nrhs, ys_f);
+}
+__global__ void fwd_update_batched(const RMat* mats, const int* list, const float* W, const float* Y, float* X, int NB,
+                                   int K, int nrhs) {
+  extern __shared__ float ys_f[];
+  GBX_MAT_OF_BLOCK();
+  fwd_update_body(W + mt.slot0 * NB * NB, Y + mt.vec0, X + mt.vec0, mt.N, NB, mt.NT, K, nrhs, ys_f);
+}
 
 // backward step, diagonal part: z_K = L_KK^{-T} y_K. A CTA owns 32 output rows (lanes, coalesced
 // over i); its 8 warps split the column range and reduce through shared memory.
-__global__ void bwd_diag_kernel(const float* Inv, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs) {
-  extern __shared__ float ys_f[];  // [nrhs][NB] then [8 warps][nrhs][32] partial sums
+__device__ void bwd_diag_body(const float* Inv, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs,
+                              float* ys_f) {
+  if (K >= NT) return;
   const int n = tdim(K, N, NB, NT);
+  if (blockIdx.x * 32 >= n) return;
   const float* out = Inv + (long long)K * NB * NB;
   for (int idx = threadIdx.x; idx < n * nrhs; idx += blockDim.x) {
     const int r = idx % n, j = idx / n;
@@ -144,18 +198,29 @@ __global__ void bwd_diag_kernel(const float* Inv, const float* Y, float* X, int 
       X[(long long)j * N + (long long)K * NB + i] = s;
     }
 }
+__global__ void bwd_diag_kernel(const float* Inv, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs) {
+  extern __shared__ float ys_f[];  // [nrhs][NB] then [8 warps][nrhs][32] partial sums
+  bwd_diag_body(Inv, Y, X, N, NB, NT, K, nrhs, ys_f);
+}
+__global__ void bwd_diag_batched(const RMat* mats, const int* list, const float* Inv, const float* Y, float* X, int NB,
+                                 int K, int nrhs) {
+  extern __shared__ float ys_f[];
+  GBX_MAT_OF_BLOCK();
+  bwd_diag_body(Inv + mt.inv0 * NB * NB, Y + mt.vec0, X + mt.vec0, mt.N, NB, mt.NT, K, nrhs, ys_f);
+}
 
 // backward step, column update: y_J -= L_KJ^T z_K for every J < K; warp per output element c
-__global__ void bwd_update_kernel(const float* W, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs) {
-  extern __shared__ float zs_f[];  // [nrhs][NB]
+__device__ void bwd_update_body(const float* W, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs,
+                                float* zs_f) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const long long total = (long long)K * NB;  // rows of y_0 .. y_{K-1}
+  if (K >= NT || (long long)blockIdx.x * nw >= total) return;
   const int kn = tdim(K, N, NB, NT);
   for (int idx = threadIdx.x; idx < kn * nrhs; idx += blockDim.x) {
     const int r = idx % kn, j = idx / kn;
     zs_f[j * NB + r] = X[(long long)j * N + (long long)K * NB + r];
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const long long total = (long long)K * NB;  // rows of y_0 .. y_{K-1}
   for (long long g = (long long)blockIdx.x * nw + warp; g < total; g += (long long)gridDim.x * nw) {
     const int J = (int)(g / NB), c = (int)(g % NB);
     const float* L = W + slot_of(K, J, NT) * (long long)NB * NB;
@@ -173,6 +238,16 @@ __global__ void bwd_update_kernel(const float* W, const float* X, float* Y, int 
     }
   }
 }
+__global__ void bwd_update_kernel(const float* W, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs) {
+  extern __shared__ float zs_f[];  // [nrhs][NB]
+  bwd_update_body(W, X, Y, N, NB, NT, K, nrhs, zs_f);
+}
+__global__ void bwd_update_batched(const RMat* mats, const int* list, const float* W, const float* X, float* Y, int NB,
+                                   int K, int nrhs) {
+  extern __shared__ float zs_f[];
+  GBX_MAT_OF_BLOCK();
+  bwd_update_body(W + mt.slot0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, K, nrhs, zs_f);
+}
 
 __global__ void d2s_kernel(const double* in, float* out, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -183,21 +258,29 @@ __global__ void s2d_kernel(const float* in, double* out, long long n) {
     out[i] = (double)in[i];
 }
 
-// ---- FP64 symmetric product Y := alpha A X + beta Y (A lower tiles) -----------------------------
-// part 1: Y_m += A_mn X_n over the stored lower part (thread per row); diagonal tiles use j <= i
-// part 2: Y_n += A_mn^T X_m over the strictly lower part (warp per column)
-__global__ void symm_rows_kernel(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
-                                 double alpha) {
-  extern __shared__ double xs_d[];  // [nrhs][512]
-  const int slot = blockIdx.x, rb = blockIdx.y;
-  int n = 0;
+// tile (m, n) of lower slot `slot` (column-major slot order); false past the last slot
+__device__ __forceinline__ bool slot_tile(int slot, int NT, int& m, int& n) {
+  if (slot >= NT * (NT + 1) / 2) return false;
+  n = 0;
   long long first = 0;
   while (first + (NT - n) <= slot) {
     first += NT - n;
     ++n;
   }
-  const int m = n + (int)(slot - first);
+  m = n + (int)(slot - first);
+  return true;
+}
+
+// ---- FP64 symmetric product Y := alpha A X + beta Y (A lower tiles) -----------------------------
+// part 1: Y_m += A_mn X_n over the stored lower part (thread per row); diagonal tiles use j <= i
+// part 2: Y_n += A_mn^T X_m over the strictly lower part (warp per column)
+__device__ void symm_rows_body(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
+                               double alpha, double* xs_d) {
+  const int slot = blockIdx.x, rb = blockIdx.y;
+  int m, n;
+  if (!slot_tile(slot, NT, m, n)) return;
   const int mrows = tdim(m, N, NB, NT), ncols = tdim(n, N, NB, NT);
+  if (rb * (int)blockDim.x >= mrows) return;
   const int i = rb * blockDim.x + threadIdx.x;
   const double* T = A + (long long)slot * NB * NB;
   double acc[kMaxRhs];
@@ -221,21 +304,27 @@ __global__ void symm_rows_kernel(const double* A, const double* X, double* Y, in
   if (i < mrows)
     for (int j = 0; j < nrhs; ++j) atomicAdd(Y + (long long)j * N + (long long)m * NB + i, alpha * acc[j]);
 }
-
-__global__ void symm_cols_kernel(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
+__global__ void symm_rows_kernel(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
                                  double alpha) {
   extern __shared__ double xs_d[];  // [nrhs][512]
+  symm_rows_body(A, X, Y, N, NB, NT, nrhs, alpha, xs_d);
+}
+__global__ void symm_rows_batched(const RMat* mats, const int* list, const double* A, const double* X, double* Y, int NB,
+                                  int nrhs, double alpha) {
+  extern __shared__ double xs_d[];
+  GBX_MAT_OF_BLOCK();
+  symm_rows_body(A + mt.slot0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xs_d);
+}
+
+__device__ void symm_cols_body(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
+                               double alpha, double* xs_d) {
   const int slot = blockIdx.x;
-  int n = 0;
-  long long first = 0;
-  while (first + (NT - n) <= slot) {
-    first += NT - n;
-    ++n;
-  }
-  const int m = n + (int)(slot - first);
+  int m, n;
+  if (!slot_tile(slot, NT, m, n)) return;
   const int mrows = tdim(m, N, NB, NT), ncols = tdim(n, N, NB, NT);
   const double* T = A + (long long)slot * NB * NB;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if ((int)blockIdx.y * nw >= ncols) return;
   for (int r0 = 0; r0 < mrows; r0 += 512) {
     const int rw = min(512, mrows - r0);
     __syncthreads();
@@ -261,6 +350,172 @@ __global__ void symm_cols_kernel(const double* A, const double* X, double* Y, in
     }
   }
 }
+__global__ void symm_cols_kernel(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
+                                 double alpha) {
+  extern __shared__ double xs_d[];  // [nrhs][512]
+  symm_cols_body(A, X, Y, N, NB, NT, nrhs, alpha, xs_d);
+}
+__global__ void symm_cols_batched(const RMat* mats, const int* list, const double* A, const double* X, double* Y, int NB,
+                                  int nrhs, double alpha) {
+  extern __shared__ double xs_d[];
+  GBX_MAT_OF_BLOCK();
+  symm_cols_body(A + mt.slot0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xs_d);
+}
+
+// ---- the same product in double-float arithmetic (FP32 pairs) for the refinement's residuals ----
+// A = Ah + Al with Ah = fl32(A), Al = fl32(A - Ah) (48 significant bits, split once per solve), x split
+// the same way per tile; a product a*x accumulates as the exact FP32 product pair of Ah*xh
+// (TwoProduct by FMA) plus the cross terms Ah*xl + Al*xh, and the sum is carried as a TwoSum pair.
+// Error about 2^-47 relative to sum |a x|, far below the 1e-14 backward-error target, at FP32 rates
+// (GB300 runs FP32 FMAs ~67x faster than FP64 ones). Intrinsics keep the compiler from contracting
+// the error-free transformations.
+__global__ void split_kernel(const double* A, float* hi, float* lo, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double a = A[i];
+    const float h = __double2float_rn(a);
+    hi[i] = h;
+    lo[i] = __double2float_rn(a - (double)h);
+  }
+}
+
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float xh, float xl) {
+  const float p = __fmul_rn(ah, xh);
+  const float e = __fmaf_rn(ah, xh, -p);                        // ah*xh = p + e exactly
+  const float c = __fmaf_rn(ah, xl, __fmaf_rn(al, xh, e));      // low-order part of the product
+  const float t = __fadd_rn(sh, p);                             // TwoSum(sh, p) = t + err
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, c));
+}
+
+// x (FP64) of one tile row/column range into split smem arrays [nrhs][512] hi and lo
+__device__ __forceinline__ void load_split(const double* X, int N, long long off, int w, int nrhs, float* xh, float* xl) {
+  for (int idx = threadIdx.x; idx < w * nrhs; idx += blockDim.x) {
+    const int c = idx % w, j = idx / w;
+    const double v = X[(long long)j * N + off + c];
+    const float h = __double2float_rn(v);
+    xh[j * 512 + c] = h;
+    xl[j * 512 + c] = __double2float_rn(v - (double)h);
+  }
+}
+
+// NR: compile-time bound on nrhs, so that the accumulators live in registers
+template <int NR>
+__device__ void symm_rows_df_body(const float* Ah, const float* Al, const double* X, double* Y, int N, int NB, int NT,
+                                  int nrhs, double alpha, float* sm) {
+  const int slot = blockIdx.x, rb = blockIdx.y;
+  int m, n;
+  if (!slot_tile(slot, NT, m, n)) return;
+  const int mrows = tdim(m, N, NB, NT), ncols = tdim(n, N, NB, NT);
+  if (rb * (int)blockDim.x >= mrows) return;
+  float* xh = sm;
+  float* xl = sm + nrhs * 512;
+  const int i = rb * blockDim.x + threadIdx.x;
+  const long long tb = (long long)slot * NB * NB;
+  float sh[NR], sl[NR];
+#pragma unroll
+  for (int j = 0; j < NR; ++j) sh[j] = sl[j] = 0.f;
+  for (int c0 = 0; c0 < ncols; c0 += 512) {
+    const int cw = min(512, ncols - c0);
+    __syncthreads();
+    load_split(X, N, (long long)n * NB + c0, cw, nrhs, xh, xl);
+    __syncthreads();
+    if (i < mrows) {
+      const int cend = (m == n) ? min(cw, i - c0 + 1) : cw;
+      for (int c = 0; c < cend; ++c) {
+        const long long e = tb + i + (long long)(c0 + c) * NB;
+        const float ah = __ldg(Ah + e), al = __ldg(Al + e);
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+          if (j < nrhs) df_fma(sh[j], sl[j], ah, al, xh[j * 512 + c], xl[j * 512 + c]);
+      }
+    }
+  }
+  if (i < mrows)
+#pragma unroll
+    for (int j = 0; j < NR; ++j)
+      if (j < nrhs) atomicAdd(Y + (long long)j * N + (long long)m * NB + i, alpha * ((double)sh[j] + (double)sl[j]));
+}
+
+template <int NR>
+__device__ void symm_cols_df_body(const float* Ah, const float* Al, const double* X, double* Y, int N, int NB, int NT,
+                                  int nrhs, double alpha, float* sm) {
+  const int slot = blockIdx.x;
+  int m, n;
+  if (!slot_tile(slot, NT, m, n)) return;
+  const int mrows = tdim(m, N, NB, NT), ncols = tdim(n, N, NB, NT);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if ((int)blockIdx.y * nw >= ncols) return;
+  float* xh = sm;
+  float* xl = sm + nrhs * 512;
+  const long long tb = (long long)slot * NB * NB;
+  for (int r0 = 0; r0 < mrows; r0 += 512) {
+    const int rw = min(512, mrows - r0);
+    __syncthreads();
+    load_split(X, N, (long long)m * NB + r0, rw, nrhs, xh, xl);
+    __syncthreads();
+    for (int c = blockIdx.y * nw + warp; c < ncols; c += gridDim.y * nw) {
+      float sh[NR], sl[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) sh[j] = sl[j] = 0.f;
+      for (int r = lane; r < rw; r += 32) {
+        if (m == n && r0 + r <= c) continue;  // strictly lower part only
+        const long long e = tb + (r0 + r) + (long long)c * NB;
+        const float ah = __ldg(Ah + e), al = __ldg(Al + e);
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+          if (j < nrhs) df_fma(sh[j], sl[j], ah, al, xh[j * 512 + r], xl[j * 512 + r]);
+      }
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        if (j >= nrhs) break;
+        double a = (double)sh[j] + (double)sl[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) atomicAdd(Y + (long long)j * N + (long long)n * NB + c, alpha * a);
+      }
+    }
+  }
+}
+template <int NR>
+__global__ void symm_rows_df_batched(const RMat* mats, const int* list, const float* Ah, const float* Al,
+                                     const double* X, double* Y, int NB, int nrhs, double alpha) {
+  extern __shared__ float xsp_f[];  // [2][nrhs][512]
+  GBX_MAT_OF_BLOCK();
+  const long long o = mt.slot0 * NB * NB;
+  symm_rows_df_body<NR>(Ah + o, Al + o, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xsp_f);
+}
+template <int NR>
+__global__ void symm_cols_df_batched(const RMat* mats, const int* list, const float* Ah, const float* Al,
+                                     const double* X, double* Y, int NB, int nrhs, double alpha) {
+  extern __shared__ float xsp_f[];
+  GBX_MAT_OF_BLOCK();
+  const long long o = mt.slot0 * NB * NB;
+  symm_cols_df_body<NR>(Ah + o, Al + o, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xsp_f);
+}
+// launches the instantiation with the smallest NR >= nrhs
+template <int NR>
+int set_df_attrs(int big) {
+  if (cudaFuncSetAttribute(symm_rows_df_batched<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(symm_cols_df_batched<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  return GBX_OK;
+}
+template <int NR>
+void launch_symm_df(dim3 gr, dim3 gc, size_t vs, cudaStream_t s, const RMat* mats, const int* list, const float* Ah,
+                    const float* Al, const double* x, double* y, int NB, int nrhs, double alpha) {
+  symm_rows_df_batched<NR><<<gr, 128, vs, s>>>(mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+  symm_cols_df_batched<NR><<<gc, 256, vs, s>>>(mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+}
+void symm_df(dim3 gr, dim3 gc, size_t vs, cudaStream_t s, const RMat* mats, const int* list, const float* Ah,
+             const float* Al, const double* x, double* y, int NB, int nrhs, double alpha) {
+  if (nrhs <= 1) launch_symm_df<1>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+  else if (nrhs <= 2) launch_symm_df<2>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+  else if (nrhs <= 4) launch_symm_df<4>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+  else if (nrhs <= 8) launch_symm_df<8>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+  else launch_symm_df<16>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+}
 
 __global__ void scale_kernel(double* Y, long long n, double beta) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -268,15 +523,10 @@ __global__ void scale_kernel(double* Y, long long n, double beta) {
 }
 
 // row sums of |A| (for ||A||_inf)
-__global__ void absrow_kernel(const double* A, double* rs, int N, int NB, int NT) {
+__device__ void absrow_body(const double* A, double* rs, int N, int NB, int NT) {
   const int slot = blockIdx.x;
-  int n = 0;
-  long long first = 0;
-  while (first + (NT - n) <= slot) {
-    first += NT - n;
-    ++n;
-  }
-  const int m = n + (int)(slot - first);
+  int m, n;
+  if (!slot_tile(slot, NT, m, n)) return;
   const int mrows = tdim(m, N, NB, NT), ncols = tdim(n, N, NB, NT);
   const double* T = A + (long long)slot * NB * NB;
   for (int i = threadIdx.x; i < mrows; i += blockDim.x) {
@@ -292,9 +542,15 @@ __global__ void absrow_kernel(const double* A, double* rs, int N, int NB, int NT
     atomicAdd(rs + (long long)n * NB + c, s);
   }
 }
+__global__ void absrow_kernel(const double* A, double* rs, int N, int NB, int NT) { absrow_body(A, rs, N, NB, NT); }
+// row sums for every matrix of the list; rs holds one N-vector per matrix at offset vec0 / nrhs
+__global__ void absrow_batched(const RMat* mats, const int* list, const double* A, double* rs, int NB, int nrhs) {
+  GBX_MAT_OF_BLOCK();
+  absrow_body(A + mt.slot0 * NB * NB, rs + mt.vec0 / nrhs, mt.N, NB, mt.NT);
+}
 
-// per right-hand side j: out[j*k + q] = reduction q of the columns (0: dot(a,b), 1: max|a|, 2: max|b|)
-__global__ void colstats_kernel(const double* a, const double* b, int N, int nrhs, double* out) {
+// per right-hand side j: out[j*3 + q] = reduction q of the columns (0: dot(a,b), 1: max|a|, 2: max|b|)
+__device__ void colstats_body(const double* a, const double* b, int N, double* out) {
   const int j = blockIdx.x;
   __shared__ double s_dot[256], s_ma[256], s_mb[256];
   double dot = 0, ma = 0, mb = 0;
@@ -322,16 +578,47 @@ __global__ void colstats_kernel(const double* a, const double* b, int N, int nrh
     out[j * 3 + 2] = s_mb[0];
   }
 }
+__global__ void colstats_kernel(const double* a, const double* b, int N, int nrhs, double* out) {
+  colstats_body(a, b, N, out);
+}
+// out: [matrix id][kMaxRhs][3]; `ncols` columns per matrix (nrhs, or 1 for the row-sum vector,
+// whose vectors are at vec0 / nrhs)
+__global__ void colstats_batched(const RMat* mats, const int* list, const double* a, const double* b, int nrhs,
+                                 int ncols, double* out) {
+  const int id = list[blockIdx.z];
+  const RMat& mt = mats[id];
+  const long long off = ncols == nrhs ? mt.vec0 : mt.vec0 / nrhs;
+  colstats_body(a + off, b ? b + off : nullptr, mt.N, out + (long long)id * kMaxRhs * 3);
+}
 
 // y_j := y_j + coef_j * x_j  (coef from device memory)
-__global__ void axpy_cols_kernel(double* y, const double* x, const double* coef, double sign, int N, int nrhs,
-                                 int xscale_mode) {
+__device__ void axpy_cols_body(double* y, const double* x, const double* coef, double sign, int N, int nrhs,
+                               int xscale_mode) {
   const long long n = (long long)N * nrhs;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int j = (int)(i / N);
     if (xscale_mode == 0) y[i] += sign * coef[j] * x[i];  // y += s*c*x
-    else y[i] = x[i] + coef[j] * y[i];                    // y = x + c*y
+    else if (xscale_mode == 1) y[i] = x[i] + coef[j] * y[i];  // y = x + c*y
+    else y[i] = 0.0;                                          // y = 0
   }
+}
+__global__ void axpy_cols_kernel(double* y, const double* x, const double* coef, double sign, int N, int nrhs,
+                                 int xscale_mode) {
+  axpy_cols_body(y, x, coef, sign, N, nrhs, xscale_mode);
+}
+// coef: [matrix id][kMaxRhs]
+__global__ void axpy_cols_batched(const RMat* mats, const int* list, double* y, const double* x, const double* coef,
+                                  double sign, int nrhs, int xscale_mode) {
+  const int id = list[blockIdx.z];
+  const RMat& mt = mats[id];
+  axpy_cols_body(y + mt.vec0, x + mt.vec0, coef + (long long)id * kMaxRhs, sign, mt.N, nrhs, xscale_mode);
+}
+// y := x (the matrix's vectors)
+__global__ void copy_vec_batched(const RMat* mats, const int* list, double* y, const double* x, int nrhs) {
+  const RMat& mt = mats[list[blockIdx.z]];
+  const long long n = (long long)mt.N * nrhs;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[mt.vec0 + i] = x[mt.vec0 + i];
 }
 
 }  // namespace refine
@@ -352,7 +639,16 @@ int set_attrs() {
       cudaFuncSetAttribute(bwd_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(symm_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(symm_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess)
+      cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(diag_inverse_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(fwd_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(fwd_update_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(bwd_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(bwd_update_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(symm_rows_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      cudaFuncSetAttribute(symm_cols_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
+      set_df_attrs<1>(big) || set_df_attrs<2>(big) || set_df_attrs<4>(big) || set_df_attrs<8>(big) ||
+      set_df_attrs<16>(big))
     return GBX_ERR_CUDA;
   done = 1;
   return GBX_OK;
@@ -417,146 +713,339 @@ extern "C" int gbx_dsymm_tiled(int N, int NB, const double* A, int nrhs, double 
   return launch_ok();
 }
 
-extern "C" int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes) {
-  if (N <= 0 || NB <= 0 || nrhs <= 0 || nrhs > kMaxRhs || !bytes) return GBX_ERR_ARG;
-  size_t f = 0;
-  if (int e = gbx_potrf_mixed_bufferSize(N, NB, &f)) return e;
-  const int NT = (N + NB - 1) / NB;
-  const size_t vec = (size_t)N * nrhs * sizeof(double);
-  *bytes = f + (size_t)NT * NB * NB * sizeof(float) + 4 * vec + 2 * (size_t)N * nrhs * sizeof(float) + N * sizeof(double) +
-           64 * kMaxRhs * sizeof(double) + 4096;
+namespace {
+// workspace of the batched refinement (the factor's workspace first)
+struct BLayout {
+  size_t fwork_bytes, inv, R, Z, P, Q, tmp, rowsum, stats, coef, mats, list, ahi, alo, total;
+};
+BLayout blayout(int batch, const int* n, int NB, int nrhs) {
+  BLayout b;
+  b.fwork_bytes = 0;
+  gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &b.fwork_bytes);
+  long long sumNT = 0, sumN = 0, slots = 0;
+  for (int k = 0; k < batch; ++k) {
+    const long long nt = (n[k] + NB - 1) / NB;
+    sumNT += nt;
+    sumN += n[k];
+    slots += nt * (nt + 1) / 2;
+  }
+  auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+  const size_t vec = (size_t)sumN * nrhs;
+  size_t o = up(b.fwork_bytes);
+  b.inv = o;
+  o += up((size_t)sumNT * NB * NB * sizeof(float));
+  b.R = o;
+  o += up(vec * 8);
+  b.Z = o;
+  o += up(vec * 8);
+  b.P = o;
+  o += up(vec * 8);
+  b.Q = o;
+  o += up(vec * 8);
+  b.tmp = o;
+  o += up(2 * vec * 4);
+  b.rowsum = o;
+  o += up((size_t)sumN * 8);
+  b.stats = o;  // two [batch][kMaxRhs][3] blocks
+  o += up((size_t)2 * batch * kMaxRhs * 3 * 8);
+  b.coef = o;  // alpha, beta: [2][batch][kMaxRhs]
+  o += up((size_t)2 * batch * kMaxRhs * 8);
+  b.mats = o;
+  o += up((size_t)batch * sizeof(RMat));
+  b.list = o;
+  o += up((size_t)batch * sizeof(int));
+  b.ahi = o;  // A split into FP32 pairs for the double-float residuals
+  o += up((size_t)slots * NB * NB * sizeof(float));
+  b.alo = o;
+  o += up((size_t)slots * NB * NB * sizeof(float));
+  b.total = o + 4096;
+  return b;
+}
+}  // namespace
+
+extern "C" int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes) {
+  if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > 1024 || nrhs <= 0 || nrhs > kMaxRhs || !bytes) return GBX_ERR_ARG;
+  for (int k = 0; k < batch; ++k)
+    if (n[k] <= 0) return GBX_ERR_ARG;
+  *bytes = blayout(batch, n, NB, nrhs).total;
   return GBX_OK;
 }
 
+extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
+                                       double* X, int prec, double tol, int maxiter, float* W, void* work,
+                                       size_t work_bytes, gbx_refine_info* info, void* stream) {
+  size_t need = 0;
+  if (int e = gbx_dposv_mixed_batched_bufferSize(batch, n, NB, nrhs, &need)) return e;
+  if (!A || !B || !X || !W || !work || maxiter < 0 || (prec != 0 && prec != 1)) return GBX_ERR_ARG;
+  if (work_bytes < need) return GBX_ERR_WORKSPACE;
+  if (int e = set_attrs()) return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  const BLayout L = blayout(batch, n, NB, nrhs);
+  char* base = (char*)work;
+  void* fwork = base;
+  float* Inv = (float*)(base + L.inv);
+  double* R = (double*)(base + L.R);
+  double* Z = (double*)(base + L.Z);
+  double* P = (double*)(base + L.P);
+  double* Q = (double*)(base + L.Q);
+  float* tmp = (float*)(base + L.tmp);
+  double* rowsum = (double*)(base + L.rowsum);
+  double* stats = (double*)(base + L.stats);
+  double* stats_x = stats + (size_t)batch * kMaxRhs * 3;
+  double* coef = (double*)(base + L.coef);
+  double* coef_b = coef + (size_t)batch * kMaxRhs;
+  RMat* dmats = (RMat*)(base + L.mats);
+  int* dlist = (int*)(base + L.list);
+  float* Ahi = (float*)(base + L.ahi);
+  float* Alo = (float*)(base + L.alo);
+
+  // matrix table (batch order) and the list of matrices by decreasing tile count
+  std::vector<RMat> mats(batch);
+  long long slot = 0, invt = 0, vecn = 0;
+  int maxNT = 0, maxN = 0;
+  for (int k = 0; k < batch; ++k) {
+    const int nt = (n[k] + NB - 1) / NB;
+    mats[k] = RMat{slot, invt, vecn, n[k], nt};
+    slot += (long long)nt * (nt + 1) / 2;
+    invt += nt;
+    vecn += (long long)n[k] * nrhs;
+    maxNT = std::max(maxNT, nt);
+    maxN = std::max(maxN, n[k]);
+  }
+  const long long nvec = vecn;
+  auto by_nt = [&](std::vector<int>& l) {
+    std::stable_sort(l.begin(), l.end(), [&](int a, int b) { return mats[a].NT > mats[b].NT; });
+  };
+  std::vector<int> all(batch);
+  for (int k = 0; k < batch; ++k) all[k] = k;
+  by_nt(all);
+  std::vector<gbx_refine_info> inf(batch);
+  std::memset(inf.data(), 0, batch * sizeof(gbx_refine_info));
+
+  // 1. low-precision factorisation of every matrix; the ones that break down are factorised again,
+  //    alone, with a growing diagonal shift
+  std::vector<unsigned char> sel(batch, 1);
+  std::vector<int> finfo(batch, 0);
+  std::vector<float> cond(batch, 0.f), cnow(batch);
+  double shift = 0.0;
+  int first_bad = 0;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    if (int e = gbx_potrf_mixed_batched(batch, n, NB, A, W, prec, shift, sel.data(), fwork, L.fwork_bytes, stream))
+      return e;
+    if (int e = gbx_potrf_mixed_batched_info(fwork, batch, n, NB, finfo.data(), cnow.data(), stream)) return e;
+    bool any = false;
+    first_bad = 0;
+    for (int k = 0; k < batch; ++k) {
+      if (!sel[k]) continue;
+      cond[k] = cnow[k];
+      inf[k].shift = shift;
+      if (finfo[k] != 0) {
+        any = true;
+        if (!first_bad) first_bad = finfo[k];
+        ++inf[k].factor_retries;
+      } else {
+        sel[k] = 0;
+      }
+    }
+    if (!any) break;
+    shift = shift == 0.0 ? (prec == 1 ? 1.0 / 2048 : 1.0 / 256) : shift * 4;
+  }
+  for (int k = 0; k < batch; ++k) inf[k].cond_estimate = cond[k];
+  bool factored = true;
+  for (int k = 0; k < batch; ++k)
+    if (sel[k]) {  // still broken after every shift
+      factored = false;
+      inf[k].backward_error = INFINITY;
+    }
+  if (!factored && batch == 1) {
+    if (info) info[0] = inf[0];
+    return first_bad;
+  }
+  std::vector<int> live;  // matrices with a factor
+  for (int k : all)
+    if (!sel[k]) live.push_back(k);
+
+  auto upload_list = [&](const std::vector<int>& l) {
+    return cudaMemcpyAsync(dlist, l.data(), l.size() * sizeof(int), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  };
+  auto count_nt_above = [&](const std::vector<int>& l, int K) {  // prefix of l with NT > K
+    int c = 0;
+    while (c < (int)l.size() && mats[l[c]].NT > K) ++c;
+    return c;
+  };
+  const unsigned gx_vec = (unsigned)std::min<long long>(64, ((long long)maxN * nrhs + 255) / 256);
+  // z := M^{-1} r for the matrices of l (FP32 sweeps; vectors in FP64)
+  auto precond = [&](const std::vector<int>& l, const double* r, double* z) {
+    float* xf = tmp;
+    float* yf = tmp + nvec;
+    const size_t vs = (size_t)nrhs * NB * sizeof(float);
+    d2s_kernel<<<512, 256, 0, s>>>(r, xf, nvec);
+    for (int K = 0; K < maxNT; ++K) {
+      const int c = count_nt_above(l, K);
+      if (!c) break;
+      fwd_diag_batched<<<dim3((NB + 7) / 8, 1, c), 256, vs, s>>>(dmats, dlist, Inv, xf, yf, NB, K, nrhs);
+      int below = 0;
+      for (int q = 0; q < c; ++q) below = std::max(below, mats[l[q]].N - (K + 1) * NB);
+      if (below > 0) fwd_update_batched<<<dim3((below + 127) / 128, 1, c), 128, vs, s>>>(dmats, dlist, W, yf, xf, NB, K, nrhs);
+    }
+    for (int K = maxNT - 1; K >= 0; --K) {
+      const int c = count_nt_above(l, K);
+      if (!c) continue;
+      bwd_diag_batched<<<dim3((NB + 31) / 32, 1, c), 256, vs + (size_t)8 * nrhs * 32 * sizeof(float), s>>>(
+          dmats, dlist, Inv, yf, xf, NB, K, nrhs);
+      if (K > 0)
+        bwd_update_batched<<<dim3((unsigned)std::min<long long>(((long long)K * NB + 7) / 8, 4096), 1, c), 256, vs, s>>>(
+            dmats, dlist, W, xf, yf, NB, K, nrhs);
+    }
+    s2d_kernel<<<512, 256, 0, s>>>(xf, z, nvec);
+  };
+  // y := y + alpha A x for the matrices of l (double-float arithmetic on the split A)
+  auto symm = [&](const std::vector<int>& l, double alpha, const double* x, double* y) {
+    const int c = (int)l.size();
+    int slots = 0;
+    for (int k : l) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
+    const size_t vs = (size_t)2 * nrhs * 512 * sizeof(float);
+    symm_df(dim3(slots, (NB + 127) / 128, c), dim3(slots, std::max(1, NB / 64), c), vs, s, dmats, dlist, Ahi, Alo, x,
+            y, NB, nrhs, alpha);
+  };
+  auto stats_of = [&](const std::vector<int>& l, const double* a, const double* b, double* out) {
+    colstats_batched<<<dim3(nrhs, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, a, b, nrhs, nrhs, out);
+  };
+  std::vector<double> hs((size_t)2 * batch * kMaxRhs * 3), hc((size_t)2 * batch * kMaxRhs, 0.0);
+  auto fetch_stats = [&]() {
+    if (cudaMemcpyAsync(hs.data(), stats, hs.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
+    return cudaStreamSynchronize(s) == cudaSuccess;
+  };
+  auto st_at = [&](const double* h, int k, int j, int q) { return h[((size_t)k * kMaxRhs + j) * 3 + q]; };
+  const double* hsx = hs.data() + (size_t)batch * kMaxRhs * 3;
+
+  if (live.empty()) {
+    if (info)
+      for (int k = 0; k < batch; ++k) info[k] = inf[k];
+    return GBX_ERR_NOCONV;
+  }
+  if (cudaMemcpyAsync(dmats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      !upload_list(live))
+    return GBX_ERR_CUDA;
+  split_kernel<<<1024, 256, 0, s>>>(A, Ahi, Alo, slot * (long long)NB * NB);
+  diag_inverse_batched<<<dim3(maxNT, (NB + kBlk - 1) / kBlk, (unsigned)live.size()), kThreads,
+                         op_trsm_smem_elems<float>() * sizeof(float), s>>>(dmats, dlist, W, Inv, NB);
+  // ||A||_inf and ||b_j||_inf per matrix
+  cudaMemsetAsync(rowsum, 0, (size_t)(nvec / nrhs) * 8, s);
+  {
+    int slots = 0;
+    for (int k : live) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
+    absrow_batched<<<dim3(slots, 1, (unsigned)live.size()), 256, 0, s>>>(dmats, dlist, A, rowsum, NB, nrhs);
+  }
+  colstats_batched<<<dim3(1, 1, (unsigned)live.size()), 256, 0, s>>>(dmats, dlist, rowsum, nullptr, nrhs, 1, stats);
+  stats_of(live, B, nullptr, stats_x);
+  if (!fetch_stats()) return GBX_ERR_CUDA;
+  std::vector<double> anorm(batch, 0.0), bnorm((size_t)batch * kMaxRhs, 0.0), rz((size_t)batch * kMaxRhs, 0.0),
+      be(batch, INFINITY);
+  for (int k : live) {
+    anorm[k] = st_at(hs.data(), k, 0, 1);
+    for (int j = 0; j < nrhs; ++j) bnorm[(size_t)k * kMaxRhs + j] = st_at(hsx, k, j, 1);
+  }
+  auto backward = [&](int k) {  // from the residual stats (hs) and the solution stats (hsx)
+    double b = 0.0;
+    for (int j = 0; j < nrhs; ++j) {
+      const double den = anorm[k] * st_at(hsx, k, j, 1) + bnorm[(size_t)k * kMaxRhs + j];
+      b = std::max(b, den > 0 ? st_at(hs.data(), k, j, 1) / den : 0.0);
+    }
+    return b;
+  };
+  auto copy_vecs = [&](const std::vector<int>& l, double* y, const double* x) {
+    copy_vec_batched<<<dim3(gx_vec, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, y, x, nrhs);
+  };
+  auto zero_vecs = [&](const std::vector<int>& l, double* y) {
+    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, y, y, coef, -1.0, nrhs, 2);
+  };
+
+  // 2. x0 = M^{-1} b ; r = b - A x0 ; z = M^{-1} r ; p = z
+  precond(live, B, X);
+  copy_vecs(live, R, B);
+  symm(live, -1.0, X, R);
+  precond(live, R, Z);
+  copy_vecs(live, P, Z);
+  stats_of(live, R, Z, stats);
+  stats_of(live, X, nullptr, stats_x);
+  if (!fetch_stats()) return GBX_ERR_CUDA;
+  for (int k : live) {
+    for (int j = 0; j < nrhs; ++j) rz[(size_t)k * kMaxRhs + j] = st_at(hs.data(), k, j, 0);
+    be[k] = backward(k);
+  }
+  // 3. preconditioned CG in FP64, each matrix until its own backward error meets the tolerance
+  // the loop's own estimate comes from the updated residual; it aims at half the tolerance so that
+  // the final check on the true residual meets the tolerance itself
+  const double target = 0.5 * tol;
+  std::vector<int> act;
+  for (int it = 0; it < maxiter; ++it) {
+    act.clear();
+    for (int k : live)
+      if (be[k] > target) act.push_back(k);
+    if (act.empty()) break;
+    if (!upload_list(act)) return GBX_ERR_CUDA;
+    zero_vecs(act, Q);
+    symm(act, 1.0, P, Q);  // q = A p
+    stats_of(act, P, Q, stats);
+    if (!fetch_stats()) return GBX_ERR_CUDA;
+    for (int k : act)
+      for (int j = 0; j < nrhs; ++j) {
+        const double pq = st_at(hs.data(), k, j, 0);
+        hc[(size_t)k * kMaxRhs + j] = pq != 0.0 ? rz[(size_t)k * kMaxRhs + j] / pq : 0.0;  // alpha
+      }
+    cudaMemcpyAsync(coef, hc.data(), (size_t)batch * kMaxRhs * 8, cudaMemcpyHostToDevice, s);
+    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)act.size()), 256, 0, s>>>(dmats, dlist, X, P, coef, 1.0, nrhs, 0);
+    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)act.size()), 256, 0, s>>>(dmats, dlist, R, Q, coef, -1.0, nrhs, 0);
+    if ((it + 1) % 8 == 0) {  // replace the recursive residual by the true one against drift
+      copy_vecs(act, R, B);
+      symm(act, -1.0, X, R);
+    }
+    precond(act, R, Z);
+    stats_of(act, R, Z, stats);
+    stats_of(act, X, nullptr, stats_x);
+    if (!fetch_stats()) return GBX_ERR_CUDA;
+    for (int k : act) {
+      ++inf[k].iterations;
+      be[k] = backward(k);
+      for (int j = 0; j < nrhs; ++j) {
+        const double rz_new = st_at(hs.data(), k, j, 0);
+        const double old = rz[(size_t)k * kMaxRhs + j];
+        hc[(size_t)(batch + k) * kMaxRhs + j] = old != 0.0 ? rz_new / old : 0.0;  // beta
+        rz[(size_t)k * kMaxRhs + j] = rz_new;
+      }
+    }
+    cudaMemcpyAsync(coef_b, hc.data() + (size_t)batch * kMaxRhs, (size_t)batch * kMaxRhs * 8, cudaMemcpyHostToDevice, s);
+    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)act.size()), 256, 0, s>>>(dmats, dlist, P, Z, coef_b, 1.0, nrhs, 1);
+  }
+  // 4. final check on the true residual of every factorised matrix
+  if (!upload_list(live)) return GBX_ERR_CUDA;
+  copy_vecs(live, R, B);
+  symm(live, -1.0, X, R);
+  stats_of(live, R, nullptr, stats);
+  stats_of(live, X, nullptr, stats_x);
+  if (!fetch_stats()) return GBX_ERR_CUDA;
+  bool ok = factored;
+  for (int k : live) {
+    inf[k].backward_error = backward(k);
+    inf[k].anorm = anorm[k];
+    if (!(inf[k].backward_error <= tol)) ok = false;
+  }
+  if (cudaGetLastError() != cudaSuccess) return GBX_ERR_CUDA;
+  if (info)
+    for (int k = 0; k < batch; ++k) info[k] = inf[k];
+  return ok ? GBX_OK : GBX_ERR_NOCONV;
+}
+
+extern "C" int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes) {
+  if (N <= 0) return GBX_ERR_ARG;
+  return gbx_dposv_mixed_batched_bufferSize(1, &N, NB, nrhs, bytes);
+}
+
+// one matrix: the batch of one
 extern "C" int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec,
                                double tol, int maxiter, float* W, void* work, size_t work_bytes, gbx_refine_info* info,
                                void* stream) {
-  if (N <= 0 || NB <= 0 || nrhs <= 0 || nrhs > kMaxRhs || !A || !B || !X || !W || !work || maxiter < 0)
-    return GBX_ERR_ARG;
-  size_t need = 0;
-  if (int e = gbx_dposv_mixed_bufferSize(N, NB, nrhs, &need)) return e;
-  if (work_bytes < need) return GBX_ERR_WORKSPACE;
-  cudaStream_t s = (cudaStream_t)stream;
-  size_t fbytes = 0;
-  gbx_potrf_mixed_bufferSize(N, NB, &fbytes);
-  const int NT = (N + NB - 1) / NB;
-  char* p = (char*)work;
-  void* fwork = p;
-  p += (fbytes + 255) / 256 * 256;
-  float* Inv = (float*)p;
-  p += ((size_t)NT * NB * NB * sizeof(float) + 255) / 256 * 256;
-  const size_t vec = (size_t)N * nrhs;
-  double* R = (double*)p;
-  p += (vec * 8 + 255) / 256 * 256;
-  double* Z = (double*)p;
-  p += (vec * 8 + 255) / 256 * 256;
-  double* P = (double*)p;
-  p += (vec * 8 + 255) / 256 * 256;
-  double* Q = (double*)p;
-  p += (vec * 8 + 255) / 256 * 256;
-  float* tmp = (float*)p;
-  p += (2 * vec * 4 + 255) / 256 * 256;
-  double* rowsum = (double*)p;
-  p += ((size_t)N * 8 + 255) / 256 * 256;
-  double* stats = (double*)p;  // [kMaxRhs*3] x2 + coefficients
-  double* coef = stats + 6 * kMaxRhs;
-
-  gbx_refine_info inf;
-  std::memset(&inf, 0, sizeof inf);
-  // 1. low-precision factorisation (shifted and retried if it breaks down)
-  double shift = 0.0;
-  int st = 0;
-  for (int attempt = 0; attempt < 8; ++attempt) {
-    if (int e = gbx_potrf_mixed(N, NB, A, W, prec, shift, fwork, fbytes, stream)) return e;
-    float cond = 0.f;
-    st = gbx_potrf_mixed_info(fwork, N, NB, &cond, stream);
-    inf.cond_estimate = cond;
-    if (st == 0) break;
-    if (st < 0) return st;
-    shift = shift == 0.0 ? (prec == 1 ? 1.0 / 2048 : 1.0 / 256) : shift * 4;
-    ++inf.factor_retries;
-  }
-  if (st != 0) return st;
-  inf.shift = shift;
-  if (int e = gbx_spotri_diag(N, NB, W, Inv, stream)) return e;
-  // ||A||_inf
-  cudaMemsetAsync(rowsum, 0, (size_t)N * 8, s);
-  absrow_kernel<<<NT * (NT + 1) / 2, 256, 0, s>>>(A, rowsum, N, NB, NT);
-  colstats_kernel<<<1, 256, 0, s>>>(rowsum, nullptr, N, 1, stats);
-  double hs[6 * kMaxRhs];
-  cudaMemcpyAsync(hs, stats, 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-  const double anorm = hs[1];
-  std::vector<double> bnorm(nrhs), rz(nrhs), hcoef(2 * kMaxRhs);
-  colstats_kernel<<<nrhs, 256, 0, s>>>(B, nullptr, N, nrhs, stats);
-  cudaMemcpyAsync(hs, stats, 3 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-  for (int j = 0; j < nrhs; ++j) bnorm[j] = hs[3 * j + 1];
-
-  // 2. x0 = M^{-1} b ; r = b - A x0
-  if (int e = gbx_sprecond(N, NB, W, Inv, nrhs, B, X, tmp, stream)) return e;
-  cudaMemcpyAsync(R, B, vec * 8, cudaMemcpyDeviceToDevice, s);
-  if (int e = gbx_dsymm_tiled(N, NB, A, nrhs, -1.0, X, 1.0, R, stream)) return e;
-  // z = M^{-1} r ; p = z
-  if (int e = gbx_sprecond(N, NB, W, Inv, nrhs, R, Z, tmp, stream)) return e;
-  cudaMemcpyAsync(P, Z, vec * 8, cudaMemcpyDeviceToDevice, s);
-  colstats_kernel<<<nrhs, 256, 0, s>>>(R, Z, N, nrhs, stats);
-  cudaMemcpyAsync(hs, stats, 3 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-  for (int j = 0; j < nrhs; ++j) rz[j] = hs[3 * j];
-  // backward error of x0
-  auto backward = [&](const double* stat_r, const double* stat_x) {
-    double be = 0.0;
-    for (int j = 0; j < nrhs; ++j) {
-      const double den = anorm * stat_x[3 * j + 1] + bnorm[j];
-      be = std::max(be, den > 0 ? stat_r[3 * j + 1] / den : 0.0);
-    }
-    return be;
-  };
-  double hx[3 * kMaxRhs];
-  colstats_kernel<<<nrhs, 256, 0, s>>>(X, nullptr, N, nrhs, stats + 3 * kMaxRhs);
-  cudaMemcpyAsync(hx, stats + 3 * kMaxRhs, 3 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-  double be = backward(hs, hx);
-  int it = 0;
-  // 3. preconditioned CG in FP64
-  for (; it < maxiter && be > tol; ++it) {
-    if (int e = gbx_dsymm_tiled(N, NB, A, nrhs, 1.0, P, 0.0, Q, stream)) return e;  // q = A p
-    colstats_kernel<<<nrhs, 256, 0, s>>>(P, Q, N, nrhs, stats);
-    cudaMemcpyAsync(hs, stats, 3 * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-    for (int j = 0; j < nrhs; ++j) hcoef[j] = hs[3 * j] != 0.0 ? rz[j] / hs[3 * j] : 0.0;  // alpha_j
-    cudaMemcpyAsync(coef, hcoef.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s);
-    axpy_cols_kernel<<<512, 256, 0, s>>>(X, P, coef, 1.0, N, nrhs, 0);   // x += alpha p
-    axpy_cols_kernel<<<512, 256, 0, s>>>(R, Q, coef, -1.0, N, nrhs, 0);  // r -= alpha q
-    if ((it + 1) % 8 == 0) {  // replace the recursive residual by the true one against drift
-      cudaMemcpyAsync(R, B, vec * 8, cudaMemcpyDeviceToDevice, s);
-      if (int e = gbx_dsymm_tiled(N, NB, A, nrhs, -1.0, X, 1.0, R, stream)) return e;
-    }
-    if (int e = gbx_sprecond(N, NB, W, Inv, nrhs, R, Z, tmp, stream)) return e;  // z = M^{-1} r
-    colstats_kernel<<<nrhs, 256, 0, s>>>(R, Z, N, nrhs, stats);
-    colstats_kernel<<<nrhs, 256, 0, s>>>(X, nullptr, N, nrhs, stats + 3 * kMaxRhs);
-    cudaMemcpyAsync(hs, stats, 6 * kMaxRhs * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-    be = backward(hs, hs + 3 * kMaxRhs);
-    for (int j = 0; j < nrhs; ++j) {
-      const double rz_new = hs[3 * j];
-      hcoef[kMaxRhs + j] = rz[j] != 0.0 ? rz_new / rz[j] : 0.0;  // beta_j
-      rz[j] = rz_new;
-    }
-    cudaMemcpyAsync(coef + kMaxRhs, hcoef.data() + kMaxRhs, nrhs * sizeof(double), cudaMemcpyHostToDevice, s);
-    axpy_cols_kernel<<<512, 256, 0, s>>>(P, Z, coef + kMaxRhs, 1.0, N, nrhs, 1);  // p = z + beta p
-  }
-  // 4. final check on the true residual
-  cudaMemcpyAsync(R, B, vec * 8, cudaMemcpyDeviceToDevice, s);
-  if (int e = gbx_dsymm_tiled(N, NB, A, nrhs, -1.0, X, 1.0, R, stream)) return e;
-  colstats_kernel<<<nrhs, 256, 0, s>>>(R, nullptr, N, nrhs, stats);
-  colstats_kernel<<<nrhs, 256, 0, s>>>(X, nullptr, N, nrhs, stats + 3 * kMaxRhs);
-  cudaMemcpyAsync(hs, stats, 6 * kMaxRhs * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
-  inf.backward_error = backward(hs, hs + 3 * kMaxRhs);
-  inf.iterations = it;
-  inf.anorm = anorm;
-  if (info) *info = inf;
-  return inf.backward_error <= tol ? GBX_OK : GBX_ERR_NOCONV;
+  if (N <= 0) return GBX_ERR_ARG;
+  return gbx_dposv_mixed_batched(1, &N, NB, A, nrhs, B, X, prec, tol, maxiter, W, work, work_bytes, info, stream);
 }

@@ -7,6 +7,8 @@
   1 down to 1/kappa, so that the condition number is kappa. H is passed to the device in
   compact-WY form H = I - U V^T (U = V T, LAPACK's dlarft recurrence for T), with G = V^T diag(lam) V.
 * rhs: right-hand sides ~ N(0, 1) from numpy default_rng(seed + 1).
+* householder batch: matrix k of a batch is the householder workload of order n_k with seed
+  seed + k, right-hand sides rhs(n_k, nrhs, seed + k).
 """
 import numpy as np
 
@@ -52,3 +54,29 @@ def householder_tiles(N, NB, r, kappa, seed, device):
     to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
     gbx.gen_lowrank(t, N, NB, to(lam), to(U), to(V), to(G))
     return t
+
+
+def batch_sizes(count, lo, hi, step, seed=42):
+    """`count` orders drawn uniformly from step * {lo..hi} (numpy default_rng(seed))."""
+    return step * np.random.default_rng(seed).integers(lo, hi + 1, size=count)
+
+
+def householder_batch(sizes, NB, r, kappa, seed, device, nrhs=0):
+    """Concatenated tile-major lower tiles of a batch of Householder matrices (matrix k with seed
+    seed + k), generated on `device`; with nrhs > 0 also the concatenated column-major right-hand
+    sides (CUDA float64). Returns (tiles, rhs or None)."""
+    import torch
+
+    import ttg_gb300 as gbx
+    offs, total = gbx.batched_tile_offsets(sizes, NB)
+    t = torch.empty(total, dtype=torch.float64, device=device)
+    to = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+    for k, n in enumerate(sizes):
+        n = int(n)
+        lam, U, V, G = householder_factors(n, r, kappa, seed + k)
+        view = t[int(offs[k]):]
+        gbx.gen_lowrank(view, n, NB, to(lam), to(U), to(V), to(G))
+    if nrhs <= 0:
+        return t, None
+    b = np.concatenate([rhs(int(n), nrhs, seed + k).ravel() for k, n in enumerate(sizes)])
+    return t, to(b)
