@@ -517,6 +517,317 @@ void symm_df(dim3 gr, dim3 gc, size_t vs, cudaStream_t s, const RMat* mats, cons
   else launch_symm_df<16>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
 }
 
+// ---- preconditioner sweeps as persistent launches ---------------------------------------------
+// z := (L L^T)^{-1} r in two launches (forward L y = x, backward L^T z = y), each over an in-order
+// list of tile tasks of every listed matrix:
+//   forward  DIAG(K):   wait until the K updates of tile row K are in; y_K = L_KK^{-1} x_K; flag K
+//            UPD(M, K): wait for flag K; x_M -= L_MK y_K (FP32 atomics); count one for row M
+//   backward DIAG(K):   wait until the NT-1-K updates of row K are in; z_K = L_KK^{-T} y_K; flag K
+//            UPD(M, K): wait for flag M; y_K -= L_MK^T z_M; count one for row K
+// Every task waits only on tasks earlier in its list, so CTAs taking tasks in list order cannot
+// deadlock; waits are bounded (the run state's status becomes GBX_ERR_TIMEOUT). x and y are the
+// FP32 vectors at vec0 of each matrix (column j of a matrix at j * N); vectors written by other
+// CTAs' atomics are read through L2.
+struct SweepTask {
+  int q;            // matrix (table index)
+  short kind, sub;  // 0 diagonal / 1 off-diagonal tile; sub-task index
+  int M, K;         // tile (M, K)
+};
+constexpr int kDiagSubs = 8;  // sub-tasks of a diagonal task: 64 output entries each
+constexpr int kUpdSubs = 8;   // sub-tasks of an off-diagonal task: 64 rows (forward) / columns (backward)
+
+// 16-byte load of rows r..r+3 of column c of a tile; rows at or past `lim` read as zero (the tile slot
+// holds NB rows, so a load that starts before `lim` stays inside it)
+__device__ __forceinline__ float4 ld4_rows(const float* T, int r, long long c, int NB, int lim) {
+  float4 v = r < lim ? __ldg((const float4*)(T + r + c * NB)) : make_float4(0, 0, 0, 0);
+  if (r + 1 >= lim) v.y = 0.f;
+  if (r + 2 >= lim) v.z = 0.f;
+  if (r + 3 >= lim) v.w = 0.f;
+  return v;
+}
+
+// vectors of tile row r0 (n entries, nrhs columns) into shared memory, zero past n
+// (one pass of independent loads per thread: scalar, since column j starts at j * N, which need not be
+// 16-byte aligned)
+__device__ __forceinline__ void load_vec(const float* V, int N, long long r0, int n, int nrhs, float* vs) {
+  float v[8];
+  for (int base = 0; base < 512 * nrhs; base += 8 * 256) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * 256 + threadIdx.x, r = idx & 511, j = idx >> 9;
+      v[u] = (idx < 512 * nrhs && r < n) ? __ldcg(V + (long long)j * N + r0 + r) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * 256 + threadIdx.x;
+      if (idx < 512 * nrhs) vs[idx] = v[u];
+    }
+  }
+  __syncthreads();
+}
+
+// warp-reduces acc[j] and, in lane 0, hands the sums to `put(j, sum)`
+template <int NR, typename F>
+__device__ __forceinline__ void warp_sums(float (&acc)[NR], int nrhs, F put) {
+#pragma unroll
+  for (int j = 0; j < NR; ++j) {
+    float a = acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0 && j < nrhs) put(j, a);
+  }
+}
+
+// forward diagonal, sub-task s: y_c = sum_{r <= c} L^{-1}(c, r) x_r for c in [64 s, 64 s + 64), with
+// L^{-1}(c, r) = out(r, c); a warp owns 8 columns, lanes four rows at a time
+template <int NR>
+__device__ void sweep_fwd_diag(const float* out, const float* X, float* Y, int N, int NB, int n, long long r0, int nrhs,
+                               int sub, float* xs) {
+  load_vec(X, N, r0, n, nrhs, xs);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int cc = 0; cc < 8; cc += 2) {
+    const int c0 = 64 * sub + 8 * warp + cc;
+    if (c0 >= n) break;
+    float acc0[NR], acc1[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc0[j] = acc1[j] = 0.f;
+    float4 v0[4], v1[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {  // out(r, c) for r <= c only
+      const int r = 4 * lane + 128 * t;
+      v0[t] = ld4_rows(out, r, c0, NB, min(n, c0 + 1));
+      v1[t] = c0 + 1 < n ? ld4_rows(out, r, c0 + 1, NB, min(n, c0 + 2)) : make_float4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int r = 4 * lane + 128 * t;
+#pragma unroll
+      for (int j = 0; j < NR; ++j)
+        if (j < nrhs) {
+          const float* x = xs + j * 512 + r;
+          acc0[j] = fmaf(v0[t].x, x[0], fmaf(v0[t].y, x[1], fmaf(v0[t].z, x[2], fmaf(v0[t].w, x[3], acc0[j]))));
+          acc1[j] = fmaf(v1[t].x, x[0], fmaf(v1[t].y, x[1], fmaf(v1[t].z, x[2], fmaf(v1[t].w, x[3], acc1[j]))));
+        }
+    }
+    warp_sums<NR>(acc0, nrhs, [&](int j, float a) { Y[(long long)j * N + r0 + c0] = a; });
+    if (c0 + 1 < n) warp_sums<NR>(acc1, nrhs, [&](int j, float a) { Y[(long long)j * N + r0 + c0 + 1] = a; });
+  }
+}
+
+// forward update, sub-task s: x_M -= L_MK y_K on rows [64 s, 64 s + 64); a thread owns four
+// consecutive rows and one sixteenth of the columns; the partial sums meet in shared memory
+template <int NR>
+__device__ void sweep_fwd_upd(const float* L, const float* Y, float* X, int N, int NB, int mrows, int kn, long long ry,
+                              long long rx, int nrhs, int sub, float* ys) {
+  load_vec(Y, N, ry, kn, nrhs, ys);
+  const int rq = threadIdx.x & 15, g = threadIdx.x >> 4;
+  const int i0 = 64 * sub + 4 * rq;
+  float acc[4][NR];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[i][j] = 0.f;
+  if (i0 < mrows) {
+    const int span = (kn + 15) / 16, cb = g * span, ce = min(kn, cb + span);
+    for (int c = cb; c < ce; c += 8) {
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = c + u < ce ? ld4_rows(L, i0, c + u, NB, mrows) : make_float4(0, 0, 0, 0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+          if (j < nrhs) {
+            const float y = c + u < ce ? ys[j * 512 + c + u] : 0.f;
+            acc[0][j] = fmaf(v[u].x, y, acc[0][j]);
+            acc[1][j] = fmaf(v[u].y, y, acc[1][j]);
+            acc[2][j] = fmaf(v[u].z, y, acc[2][j]);
+            acc[3][j] = fmaf(v[u].w, y, acc[3][j]);
+          }
+    }
+  }
+  float* part = ys + NR * 512;  // [16 groups][NR][64 rows]
+#pragma unroll
+  for (int j = 0; j < NR; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) part[(g * NR + j) * 64 + 4 * rq + i] = acc[i][j];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 64 * nrhs; idx += blockDim.x) {
+    const int r = idx & 63, j = idx >> 6;
+    if (64 * sub + r >= mrows) continue;
+    float sum = 0.f;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) sum += part[(q * NR + j) * 64 + r];
+    atomicAdd(X + (long long)j * N + rx + 64 * sub + r, -sum);
+  }
+}
+
+// backward diagonal, sub-task s: z_i = sum_{c >= i} out(i, c) y_c for i in [64 s, 64 s + 64); a
+// thread owns four consecutive rows and one sixteenth of the columns
+template <int NR>
+__device__ void sweep_bwd_diag(const float* out, const float* Y, float* X, int N, int NB, int n, long long r0, int nrhs,
+                               int sub, float* ys) {
+  load_vec(Y, N, r0, n, nrhs, ys);
+  const int rq = threadIdx.x & 15, g = threadIdx.x >> 4;
+  const int i0 = 64 * sub + 4 * rq;
+  float acc[4][NR];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[i][j] = 0.f;
+  if (i0 < n) {
+    for (int c = i0 + g; c < n; c += 16 * 4) {  // columns c, c+16, c+32, c+48 of this group, from the diagonal on
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int cu = c + 16 * u;
+        v[u] = cu < n ? ld4_rows(out, i0, cu, NB, min(n, cu + 1)) : make_float4(0, 0, 0, 0);  // rows <= cu only
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < NR; ++j)
+          if (j < nrhs) {
+            const float y = ys[j * 512 + min(c + 16 * u, 511)];
+            acc[0][j] = fmaf(v[u].x, y, acc[0][j]);
+            acc[1][j] = fmaf(v[u].y, y, acc[1][j]);
+            acc[2][j] = fmaf(v[u].z, y, acc[2][j]);
+            acc[3][j] = fmaf(v[u].w, y, acc[3][j]);
+          }
+    }
+  }
+  float* part = ys + NR * 512;  // [16 groups][NR][64 rows]
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NR; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) part[(g * NR + j) * 64 + 4 * rq + i] = acc[i][j];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 64 * nrhs; idx += blockDim.x) {
+    const int r = idx & 63, j = idx >> 6;
+    if (64 * sub + r >= n) continue;
+    float sum = 0.f;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) sum += part[(q * NR + j) * 64 + r];
+    X[(long long)j * N + r0 + 64 * sub + r] = sum;
+  }
+}
+
+// backward update, sub-task s: y_K -= L_MK^T z_M on columns [64 s, 64 s + 64): a warp owns 8
+// columns, lanes four rows at a time
+template <int NR>
+__device__ void sweep_bwd_upd(const float* L, const float* X, float* Y, int N, int NB, int mrows, int kn, long long rz,
+                              long long ry, int nrhs, int sub, float* zs) {
+  load_vec(X, N, rz, mrows, nrhs, zs);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int cc = 0; cc < 8; cc += 2) {
+    const int c0 = 64 * sub + 8 * warp + cc;
+    if (c0 >= kn) break;
+    float acc0[NR], acc1[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc0[j] = acc1[j] = 0.f;
+    float4 v0[4], v1[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int r = 4 * lane + 128 * t;
+      v0[t] = ld4_rows(L, r, c0, NB, mrows);
+      v1[t] = c0 + 1 < kn ? ld4_rows(L, r, c0 + 1, NB, mrows) : make_float4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int r = 4 * lane + 128 * t;
+#pragma unroll
+      for (int j = 0; j < NR; ++j)
+        if (j < nrhs) {
+          const float* z = zs + j * 512 + r;
+          acc0[j] = fmaf(v0[t].x, z[0], fmaf(v0[t].y, z[1], fmaf(v0[t].z, z[2], fmaf(v0[t].w, z[3], acc0[j]))));
+          acc1[j] = fmaf(v1[t].x, z[0], fmaf(v1[t].y, z[1], fmaf(v1[t].z, z[2], fmaf(v1[t].w, z[3], acc1[j]))));
+        }
+    }
+    warp_sums<NR>(acc0, nrhs, [&](int j, float a) { atomicAdd(Y + (long long)j * N + ry + c0, -a); });
+    if (c0 + 1 < kn) warp_sums<NR>(acc1, nrhs, [&](int j, float a) { atomicAdd(Y + (long long)j * N + ry + c0 + 1, -a); });
+  }
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256) sweep_kernel(int dir, const RMat* mats, const SweepTask* tasks, int ntasks,
+                                                    const float* W, const float* Inv, float* Xf, float* Yf, int NB,
+                                                    int nrhs, int* cnt, int* flag, DagState* st, uint64_t timeout_ns) {
+  extern __shared__ __align__(16) float vs_f[];  // [NR][512] vector, then [16][NR][64] partial sums
+  __shared__ int s_t, s_ok;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long t = -1;
+      if (!ld_volatile(&st->abort)) t = (long long)atomicAdd(&st->head, 1ULL);
+      s_t = (t >= 0 && t < ntasks) ? (int)t : -1;
+    }
+    __syncthreads();
+    if (s_t < 0) break;
+    const SweepTask tk = tasks[s_t];
+    const RMat& mt = mats[tk.q];
+    const int N = mt.N, NT = mt.NT;
+    int* c = cnt + mt.inv0;
+    int* f = flag + mt.inv0;
+    if (threadIdx.x == 0) {
+      bool ok;
+      if (dir == 0)
+        ok = tk.kind == 0 ? wait_geq(c + tk.K, kUpdSubs * tk.K, st, timeout_ns)
+                          : wait_geq(f + tk.K, kDiagSubs, st, timeout_ns);
+      else
+        ok = tk.kind == 0 ? wait_geq(c + tk.K, kUpdSubs * (NT - 1 - tk.K), st, timeout_ns)
+                          : wait_geq(f + tk.M, kDiagSubs, st, timeout_ns);
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) break;
+    float* X = Xf + mt.vec0;
+    float* Y = Yf + mt.vec0;
+    const int kn = tdim(tk.K, N, NB, NT);
+    if (tk.kind == 0) {
+      const float* out = Inv + (mt.inv0 + tk.K) * (long long)NB * NB;
+      if (dir == 0) sweep_fwd_diag<NR>(out, X, Y, N, NB, kn, (long long)tk.K * NB, nrhs, tk.sub, vs_f);
+      else sweep_bwd_diag<NR>(out, Y, X, N, NB, kn, (long long)tk.K * NB, nrhs, tk.sub, vs_f);
+    } else {
+      const float* L = W + (mt.slot0 + slot_of(tk.M, tk.K, NT)) * (long long)NB * NB;
+      const int mrows = tdim(tk.M, N, NB, NT);
+      if (dir == 0)
+        sweep_fwd_upd<NR>(L, Y, X, N, NB, mrows, kn, (long long)tk.K * NB, (long long)tk.M * NB, nrhs, tk.sub, vs_f);
+      else
+        sweep_bwd_upd<NR>(L, X, Y, N, NB, mrows, kn, (long long)tk.M * NB, (long long)tk.K * NB, nrhs, tk.sub, vs_f);
+    }
+    __threadfence();  // this thread's results are visible before the completion is
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (tk.kind == 0) signal_done(f + tk.K);
+      else signal_done(c + (dir == 0 ? tk.M : tk.K));
+    }
+  }
+}
+
+template <int NR>
+int set_sweep_attrs(int big) {
+  return cudaFuncSetAttribute(sweep_kernel<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) == cudaSuccess
+             ? GBX_OK
+             : GBX_ERR_CUDA;
+}
+// shared memory of a sweep CTA: the vector, then the partial sums
+inline size_t sweep_smem(int NR) { return (size_t)NR * 512 * sizeof(float) + (size_t)16 * NR * 64 * sizeof(float); }
+void launch_sweep(int dir, int grid, cudaStream_t s, const RMat* mats, const SweepTask* tasks, int ntasks,
+                  const float* W, const float* Inv, float* Xf, float* Yf, int NB, int nrhs, int* cnt, int* flag,
+                  DagState* st, uint64_t timeout_ns) {
+  const int NRb = nrhs <= 1 ? 1 : nrhs <= 2 ? 2 : nrhs <= 4 ? 4 : nrhs <= 8 ? 8 : 16;
+  const size_t vs = sweep_smem(NRb);
+#define GBX_SWEEP(NR)                                                                                              \
+  sweep_kernel<NR><<<grid, 256, vs, s>>>(dir, mats, tasks, ntasks, W, Inv, Xf, Yf, NB, nrhs, cnt, flag, st, timeout_ns)
+  if (nrhs <= 1) GBX_SWEEP(1);
+  else if (nrhs <= 2) GBX_SWEEP(2);
+  else if (nrhs <= 4) GBX_SWEEP(4);
+  else if (nrhs <= 8) GBX_SWEEP(8);
+  else GBX_SWEEP(16);
+#undef GBX_SWEEP
+}
+
 __global__ void scale_kernel(double* Y, long long n, double beta) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     Y[i] = beta == 0.0 ? 0.0 : Y[i] * beta;
@@ -648,7 +959,8 @@ int set_attrs() {
       cudaFuncSetAttribute(symm_rows_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(symm_cols_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       set_df_attrs<1>(big) || set_df_attrs<2>(big) || set_df_attrs<4>(big) || set_df_attrs<8>(big) ||
-      set_df_attrs<16>(big))
+      set_df_attrs<16>(big) || set_sweep_attrs<1>(big) || set_sweep_attrs<2>(big) || set_sweep_attrs<4>(big) ||
+      set_sweep_attrs<8>(big) || set_sweep_attrs<16>(big))
     return GBX_ERR_CUDA;
   done = 1;
   return GBX_OK;
@@ -716,7 +1028,7 @@ extern "C" int gbx_dsymm_tiled(int N, int NB, const double* A, int nrhs, double 
 namespace {
 // workspace of the batched refinement (the factor's workspace first)
 struct BLayout {
-  size_t fwork_bytes, inv, R, Z, P, Q, tmp, rowsum, stats, coef, mats, list, ahi, alo, total;
+  size_t fwork_bytes, inv, R, Z, P, Q, tmp, rowsum, stats, coef, mats, list, ahi, alo, sweep, tasks, total;
 };
 BLayout blayout(int batch, const int* n, int NB, int nrhs) {
   BLayout b;
@@ -758,6 +1070,10 @@ BLayout blayout(int batch, const int* n, int NB, int nrhs) {
   o += up((size_t)slots * NB * NB * sizeof(float));
   b.alo = o;
   o += up((size_t)slots * NB * NB * sizeof(float));
+  b.sweep = o;  // two run states, then forward / backward row counters and flags
+  o += up(2 * sizeof(DagState) + (size_t)4 * sumNT * sizeof(int));
+  b.tasks = o;  // forward then backward task lists (sub-tasks of every tile)
+  o += up((size_t)2 * slots * std::max(kDiagSubs, kUpdSubs) * sizeof(SweepTask));
   b.total = o + 4096;
   return b;
 }
@@ -868,35 +1184,63 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
   auto upload_list = [&](const std::vector<int>& l) {
     return cudaMemcpyAsync(dlist, l.data(), l.size() * sizeof(int), cudaMemcpyHostToDevice, s) == cudaSuccess;
   };
-  auto count_nt_above = [&](const std::vector<int>& l, int K) {  // prefix of l with NT > K
-    int c = 0;
-    while (c < (int)l.size() && mats[l[c]].NT > K) ++c;
-    return c;
-  };
   const unsigned gx_vec = (unsigned)std::min<long long>(64, ((long long)maxN * nrhs + 255) / 256);
-  // z := M^{-1} r for the matrices of l (FP32 sweeps; vectors in FP64)
+  // z := M^{-1} r for the matrices of l (FP32 sweeps; vectors in FP64): two persistent launches
+  // over task lists that interleave the listed matrices step by step
+  DagState* sw_st = (DagState*)(base + L.sweep);
+  int* sw_cnt = (int*)(base + L.sweep + 2 * sizeof(DagState));
+  SweepTask* d_tasks = (SweepTask*)(base + L.tasks);
+  if (cudaMemsetAsync(sw_st, 0, 2 * sizeof(DagState), s) != cudaSuccess) return GBX_ERR_CUDA;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
+  std::vector<int> swept;  // matrices of the uploaded task lists
+  int nf = 0, nb = 0;
+  const uint64_t tmo = gbx_get_wait_timeout_ns();
   auto precond = [&](const std::vector<int>& l, const double* r, double* z) {
     float* xf = tmp;
     float* yf = tmp + nvec;
-    const size_t vs = (size_t)nrhs * NB * sizeof(float);
     d2s_kernel<<<512, 256, 0, s>>>(r, xf, nvec);
-    for (int K = 0; K < maxNT; ++K) {
-      const int c = count_nt_above(l, K);
-      if (!c) break;
-      fwd_diag_batched<<<dim3((NB + 7) / 8, 1, c), 256, vs, s>>>(dmats, dlist, Inv, xf, yf, NB, K, nrhs);
-      int below = 0;
-      for (int q = 0; q < c; ++q) below = std::max(below, mats[l[q]].N - (K + 1) * NB);
-      if (below > 0) fwd_update_batched<<<dim3((below + 127) / 128, 1, c), 128, vs, s>>>(dmats, dlist, W, yf, xf, NB, K, nrhs);
+    if (l != swept) {
+      std::vector<SweepTask> tf, tb;
+      auto push = [](std::vector<SweepTask>& v, int q, int kind, int M, int K) {
+        const int subs = kind == 0 ? kDiagSubs : kUpdSubs;
+        for (int u = 0; u < subs; ++u) v.push_back(SweepTask{q, (short)kind, (short)u, M, K});
+      };
+      for (int K = 0; K < maxNT; ++K) {
+        for (int q : l)
+          if (mats[q].NT > K) push(tf, q, 0, K, K);
+        for (int q : l)  // the next step's own row first: it is on the critical path
+          if (K + 1 < mats[q].NT) push(tf, q, 1, K + 1, K);
+        for (int q : l)
+          for (int M = K + 2; M < mats[q].NT; ++M) push(tf, q, 1, M, K);
+      }
+      for (int st = 0; st < maxNT; ++st) {  // steps counted from each matrix's last tile row
+        for (int q : l)
+          if (mats[q].NT > st) push(tb, q, 0, mats[q].NT - 1 - st, mats[q].NT - 1 - st);
+        for (int q : l) {
+          const int K = mats[q].NT - 1 - st;
+          if (K >= 1) push(tb, q, 1, K, K - 1);
+        }
+        for (int q : l) {
+          const int K = mats[q].NT - 1 - st;
+          for (int J = 0; J + 1 < K; ++J) push(tb, q, 1, K, J);
+        }
+      }
+      nf = (int)tf.size();
+      nb = (int)tb.size();
+      tf.insert(tf.end(), tb.begin(), tb.end());
+      cudaMemcpyAsync(d_tasks, tf.data(), tf.size() * sizeof(SweepTask), cudaMemcpyHostToDevice, s);
+      swept = l;
     }
-    for (int K = maxNT - 1; K >= 0; --K) {
-      const int c = count_nt_above(l, K);
-      if (!c) continue;
-      bwd_diag_batched<<<dim3((NB + 31) / 32, 1, c), 256, vs + (size_t)8 * nrhs * 32 * sizeof(float), s>>>(
-          dmats, dlist, Inv, yf, xf, NB, K, nrhs);
-      if (K > 0)
-        bwd_update_batched<<<dim3((unsigned)std::min<long long>(((long long)K * NB + 7) / 8, 4096), 1, c), 256, vs, s>>>(
-            dmats, dlist, W, xf, yf, NB, K, nrhs);
-    }
+    // fresh queue heads and counters; status and abort stay, so a wait that ran out is reported
+    cudaMemsetAsync(&sw_st[0].head, 0, sizeof(unsigned long long), s);
+    cudaMemsetAsync(&sw_st[1].head, 0, sizeof(unsigned long long), s);
+    cudaMemsetAsync(sw_cnt, 0, (size_t)4 * invt * sizeof(int), s);
+    const int gf = std::max(1, std::min(2 * sms, nf)), gb = std::max(1, std::min(2 * sms, nb));
+    launch_sweep(0, gf, s, dmats, d_tasks, nf, W, Inv, xf, yf, NB, nrhs, sw_cnt, sw_cnt + invt, sw_st, tmo);
+    launch_sweep(1, gb, s, dmats, d_tasks + nf, nb, W, Inv, xf, yf, NB, nrhs, sw_cnt + 2 * invt, sw_cnt + 3 * invt,
+                 sw_st + 1, tmo);
     s2d_kernel<<<512, 256, 0, s>>>(xf, z, nvec);
   };
   // y := y + alpha A x for the matrices of l (double-float arithmetic on the split A)
@@ -1025,6 +1369,9 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
   stats_of(live, R, nullptr, stats);
   stats_of(live, X, nullptr, stats_x);
   if (!fetch_stats()) return GBX_ERR_CUDA;
+  int sw_status[2 * sizeof(DagState) / sizeof(int)];
+  if (cudaMemcpy(sw_status, sw_st, 2 * sizeof(DagState), cudaMemcpyDeviceToHost) != cudaSuccess) return GBX_ERR_CUDA;
+  if (sw_status[0] || sw_status[sizeof(DagState) / sizeof(int)]) return GBX_ERR_TIMEOUT;  // a sweep's wait ran out
   bool ok = factored;
   for (int k : live) {
     inf[k].backward_error = backward(k);
