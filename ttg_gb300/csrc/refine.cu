@@ -389,21 +389,37 @@ __device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al,
   sl = __fadd_rn(sl, __fadd_rn(err, c));
 }
 
-// x (FP64) of one tile row/column range into split smem arrays [nrhs][512] hi and lo
-__device__ __forceinline__ void load_split(const double* X, int N, long long off, int w, int nrhs, float* xh, float* xl) {
+// x split once per product into FP32 pairs (same layout as x), then staged per tile
+__global__ void split_vec_kernel(const double* X, float* xh, float* xl, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = X[i];
+    const float h = __double2float_rn(v);
+    xh[i] = h;
+    xl[i] = __double2float_rn(v - (double)h);
+  }
+}
+__device__ __forceinline__ void load_pair(const float* Xh, const float* Xl, int N, long long off, int w, int nrhs,
+                                          float* xh, float* xl) {
   for (int idx = threadIdx.x; idx < w * nrhs; idx += blockDim.x) {
     const int c = idx % w, j = idx / w;
-    const double v = X[(long long)j * N + off + c];
-    const float h = __double2float_rn(v);
-    xh[j * 512 + c] = h;
-    xl[j * 512 + c] = __double2float_rn(v - (double)h);
+    xh[j * 512 + c] = Xh[(long long)j * N + off + c];
+    xl[j * 512 + c] = Xl[(long long)j * N + off + c];
   }
 }
 
-// NR: compile-time bound on nrhs, so that the accumulators live in registers
+// (sh, sl) += (th, tl) for double-float pairs (TwoSum on the high parts)
+__device__ __forceinline__ void df_add(float& sh, float& sl, float th, float tl) {
+  const float t = __fadd_rn(sh, th);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(th, bp));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, tl));
+}
+
+// rows: thread per row; Y_m += A_mn X_n (diagonal tiles: columns <= row)
 template <int NR>
-__device__ void symm_rows_df_body(const float* Ah, const float* Al, const double* X, double* Y, int N, int NB, int NT,
-                                  int nrhs, double alpha, float* sm) {
+__device__ void symm_rows_df_body(const float* Ah, const float* Al, const float* Xh, const float* Xl, double* Y, int N,
+                                  int NB, int NT, int nrhs, double alpha, float* sm) {
   const int slot = blockIdx.x, rb = blockIdx.y;
   int m, n;
   if (!slot_tile(slot, NT, m, n)) return;
@@ -419,11 +435,26 @@ __device__ void symm_rows_df_body(const float* Ah, const float* Al, const double
   for (int c0 = 0; c0 < ncols; c0 += 512) {
     const int cw = min(512, ncols - c0);
     __syncthreads();
-    load_split(X, N, (long long)n * NB + c0, cw, nrhs, xh, xl);
+    load_pair(Xh, Xl, N, (long long)n * NB + c0, cw, nrhs, xh, xl);
     __syncthreads();
     if (i < mrows) {
       const int cend = (m == n) ? min(cw, i - c0 + 1) : cw;
-      for (int c = 0; c < cend; ++c) {
+      int c = 0;
+      for (; c + 4 <= cend; c += 4) {  // four independent load pairs in flight
+        float ah[4], al[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const long long e = tb + i + (long long)(c0 + c + u) * NB;
+          ah[u] = __ldg(Ah + e);
+          al[u] = __ldg(Al + e);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int j = 0; j < NR; ++j)
+            if (j < nrhs) df_fma(sh[j], sl[j], ah[u], al[u], xh[j * 512 + c + u], xl[j * 512 + c + u]);
+      }
+      for (; c < cend; ++c) {
         const long long e = tb + i + (long long)(c0 + c) * NB;
         const float ah = __ldg(Ah + e), al = __ldg(Al + e);
 #pragma unroll
@@ -438,9 +469,12 @@ __device__ void symm_rows_df_body(const float* Ah, const float* Al, const double
       if (j < nrhs) atomicAdd(Y + (long long)j * N + (long long)m * NB + i, alpha * ((double)sh[j] + (double)sl[j]));
 }
 
+// columns: warp per column over the strictly lower part; Y_n += A_mn^T X_m. The lane sums meet in
+// double-float shuffles; each warp converts its columns' sums to FP64 together, once per 8 columns,
+// so that the FP64 pipe (slow on this GPU) sees a handful of instructions per column.
 template <int NR>
-__device__ void symm_cols_df_body(const float* Ah, const float* Al, const double* X, double* Y, int N, int NB, int NT,
-                                  int nrhs, double alpha, float* sm) {
+__device__ void symm_cols_df_body(const float* Ah, const float* Al, const float* Xh, const float* Xl, double* Y, int N,
+                                  int NB, int NT, int nrhs, double alpha, float* sm) {
   const int slot = blockIdx.x;
   int m, n;
   if (!slot_tile(slot, NT, m, n)) return;
@@ -449,13 +483,16 @@ __device__ void symm_cols_df_body(const float* Ah, const float* Al, const double
   if ((int)blockIdx.y * nw >= ncols) return;
   float* xh = sm;
   float* xl = sm + nrhs * 512;
+  float* res = sm + 2 * nrhs * 512 + warp * (8 * NR * 2);  // [8 columns][NR][hi, lo] per warp
   const long long tb = (long long)slot * NB * NB;
   for (int r0 = 0; r0 < mrows; r0 += 512) {
     const int rw = min(512, mrows - r0);
     __syncthreads();
-    load_split(X, N, (long long)m * NB + r0, rw, nrhs, xh, xl);
+    load_pair(Xh, Xl, N, (long long)m * NB + r0, rw, nrhs, xh, xl);
     __syncthreads();
+    int q = 0, cfirst = -1;
     for (int c = blockIdx.y * nw + warp; c < ncols; c += gridDim.y * nw) {
+      if (cfirst < 0) cfirst = c;
       float sh[NR], sl[NR];
 #pragma unroll
       for (int j = 0; j < NR; ++j) sh[j] = sl[j] = 0.f;
@@ -469,30 +506,51 @@ __device__ void symm_cols_df_body(const float* Ah, const float* Al, const double
       }
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
-        if (j >= nrhs) break;
-        double a = (double)sh[j] + (double)sl[j];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) atomicAdd(Y + (long long)j * N + (long long)n * NB + c, alpha * a);
+        for (int o = 16; o > 0; o >>= 1) {
+          const float th = __shfl_xor_sync(0xffffffffu, sh[j], o), tl = __shfl_xor_sync(0xffffffffu, sl[j], o);
+          df_add(sh[j], sl[j], th, tl);
+        }
+      }
+      if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+          res[(q * NR + j) * 2] = sh[j];
+          res[(q * NR + j) * 2 + 1] = sl[j];
+        }
+      ++q;
+      const int cnext = c + gridDim.y * nw;
+      if (q == 8 || cnext >= ncols) {  // flush: every lane converts and adds a few of the results
+        __syncwarp();
+        const int stride = gridDim.y * nw;
+        for (int e = lane; e < q * nrhs; e += 32) {
+          const int qq = e / nrhs, j = e % nrhs;
+          const double v = (double)res[(qq * NR + j) * 2] + (double)res[(qq * NR + j) * 2 + 1];
+          atomicAdd(Y + (long long)j * N + (long long)n * NB + cfirst + qq * stride, alpha * v);
+        }
+        __syncwarp();
+        q = 0;
+        cfirst = -1;
       }
     }
   }
 }
+
 template <int NR>
 __global__ void symm_rows_df_batched(const RMat* mats, const int* list, const float* Ah, const float* Al,
-                                     const double* X, double* Y, int NB, int nrhs, double alpha) {
+                                     const float* Xh, const float* Xl, double* Y, int NB, int nrhs, double alpha) {
   extern __shared__ float xsp_f[];  // [2][nrhs][512]
   GBX_MAT_OF_BLOCK();
   const long long o = mt.slot0 * NB * NB;
-  symm_rows_df_body<NR>(Ah + o, Al + o, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xsp_f);
+  symm_rows_df_body<NR>(Ah + o, Al + o, Xh + mt.vec0, Xl + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xsp_f);
 }
 template <int NR>
 __global__ void symm_cols_df_batched(const RMat* mats, const int* list, const float* Ah, const float* Al,
-                                     const double* X, double* Y, int NB, int nrhs, double alpha) {
-  extern __shared__ float xsp_f[];
+                                     const float* Xh, const float* Xl, double* Y, int NB, int nrhs, double alpha) {
+  extern __shared__ float xsp_f[];  // [2][nrhs][512], then [8 warps][8 columns][NR][2] results
   GBX_MAT_OF_BLOCK();
   const long long o = mt.slot0 * NB * NB;
-  symm_cols_df_body<NR>(Ah + o, Al + o, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xsp_f);
+  symm_cols_df_body<NR>(Ah + o, Al + o, Xh + mt.vec0, Xl + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xsp_f);
 }
 // launches the instantiation with the smallest NR >= nrhs
 template <int NR>
@@ -504,17 +562,19 @@ int set_df_attrs(int big) {
 }
 template <int NR>
 void launch_symm_df(dim3 gr, dim3 gc, size_t vs, cudaStream_t s, const RMat* mats, const int* list, const float* Ah,
-                    const float* Al, const double* x, double* y, int NB, int nrhs, double alpha) {
-  symm_rows_df_batched<NR><<<gr, 128, vs, s>>>(mats, list, Ah, Al, x, y, NB, nrhs, alpha);
-  symm_cols_df_batched<NR><<<gc, 256, vs, s>>>(mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+                    const float* Al, const float* xh, const float* xl, double* y, int NB, int nrhs, double alpha) {
+  symm_rows_df_batched<NR><<<gr, 128, vs, s>>>(mats, list, Ah, Al, xh, xl, y, NB, nrhs, alpha);
+  symm_cols_df_batched<NR><<<gc, 256, vs + (size_t)8 * 8 * NR * 2 * sizeof(float), s>>>(mats, list, Ah, Al, xh, xl, y,
+                                                                                        NB, nrhs, alpha);
 }
+// y += alpha A x with x split into FP32 pairs xh, xl beforehand
 void symm_df(dim3 gr, dim3 gc, size_t vs, cudaStream_t s, const RMat* mats, const int* list, const float* Ah,
-             const float* Al, const double* x, double* y, int NB, int nrhs, double alpha) {
-  if (nrhs <= 1) launch_symm_df<1>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
-  else if (nrhs <= 2) launch_symm_df<2>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
-  else if (nrhs <= 4) launch_symm_df<4>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
-  else if (nrhs <= 8) launch_symm_df<8>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
-  else launch_symm_df<16>(gr, gc, vs, s, mats, list, Ah, Al, x, y, NB, nrhs, alpha);
+             const float* Al, const float* xh, const float* xl, double* y, int NB, int nrhs, double alpha) {
+  if (nrhs <= 1) launch_symm_df<1>(gr, gc, vs, s, mats, list, Ah, Al, xh, xl, y, NB, nrhs, alpha);
+  else if (nrhs <= 2) launch_symm_df<2>(gr, gc, vs, s, mats, list, Ah, Al, xh, xl, y, NB, nrhs, alpha);
+  else if (nrhs <= 4) launch_symm_df<4>(gr, gc, vs, s, mats, list, Ah, Al, xh, xl, y, NB, nrhs, alpha);
+  else if (nrhs <= 8) launch_symm_df<8>(gr, gc, vs, s, mats, list, Ah, Al, xh, xl, y, NB, nrhs, alpha);
+  else launch_symm_df<16>(gr, gc, vs, s, mats, list, Ah, Al, xh, xl, y, NB, nrhs, alpha);
 }
 
 // ---- preconditioner sweeps as persistent launches ---------------------------------------------
@@ -1249,8 +1309,11 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
     int slots = 0;
     for (int k : l) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
     const size_t vs = (size_t)2 * nrhs * 512 * sizeof(float);
-    symm_df(dim3(slots, (NB + 127) / 128, c), dim3(slots, std::max(1, NB / 64), c), vs, s, dmats, dlist, Ahi, Alo, x,
-            y, NB, nrhs, alpha);
+    float* xh = tmp;  // the preconditioner's FP32 buffers are free between its calls
+    float* xl = tmp + nvec;
+    split_vec_kernel<<<512, 256, 0, s>>>(x, xh, xl, nvec);
+    symm_df(dim3(slots, (NB + 127) / 128, c), dim3(slots, std::max(1, NB / 64), c), vs, s, dmats, dlist, Ahi, Alo, xh,
+            xl, y, NB, nrhs, alpha);
   };
   auto stats_of = [&](const std::vector<int>& l, const double* a, const double* b, double* out) {
     colstats_batched<<<dim3(nrhs, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, a, b, nrhs, nrhs, out);
