@@ -241,6 +241,17 @@ int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, in
                             int prec, double tol, int maxiter, float* W, void* work, size_t work_bytes,
                             gbx_refine_info* info, void* stream);
 
+/* Factorisation and solve from host buffers (pinned for overlap): A_host and L_host hold the
+ * tile-major lower storage (tiled_numel doubles), B_host / X_host are column-major N x nrhs; tiles
+ * and X are device buffers of the same sizes. Tile columns are copied in while the executor runs,
+ * each column of L is copied back as soon as it is final, then X = (L L^T)^{-1} B comes back.
+ * Asynchronous on `stream`; gbx_dpotrf_tiled_status(work) gives the factorisation status. No
+ * counterpart in the reference, whose tiles reach the device through PaRSEC's stage-in
+ * (parsec/ttg.h:1434-1672) and come back on wait() (parsec/devicefunc.h:232-256). */
+int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes);
+int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, int nrhs, const double* B_host,
+                         double* X_host, double* tiles, double* X, void* work, size_t work_bytes, void* stream);
+
 /* ============================================================================================
  * Batched solves of many independent SPD matrices of uneven sizes in one persistent launch
  * (capturable in a CUDA graph: no host synchronisation, no allocation). No counterpart in the

@@ -312,3 +312,58 @@ def test_task_timeline_trace(gbx, cuda, tmp_path):
     assert all(t["start_ns"] >= pot[t["b"]]["end_ns"] for t in trsm)  # dependency order is visible
     gbx.trace_to_chrome(recs, str(tmp_path / "t.json"))
     assert len(json.load(open(tmp_path / "t.json"))["traceEvents"]) == len(recs)
+
+
+def _wait_stream(torch, seconds=60.0):
+    """Polls the current stream with a deadline instead of blocking forever."""
+    import time
+    ev = torch.cuda.Event()
+    ev.record()
+    t0 = time.time()
+    while not ev.query():
+        assert time.time() - t0 < seconds, "stream did not finish"
+        time.sleep(0.001)
+
+
+@pytest.mark.parametrize("N,NB,nrhs", [(3000, 512, 2), (1000, 128, 1)])
+def test_dposv_tiled_host_overlap(gbx, cuda, N, NB, nrhs):
+    """Host buffers in, host buffers out, copies overlapped with the executor: the factor and the
+    solution equal the device-resident path's bit for bit (both are deterministic)."""
+    import torch
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=11)
+    B = torch.randn(nrhs, N, dtype=torch.float64, device=cuda)
+    T = A.clone()
+    gbx.potrf_tiled(T, N, NB)
+    Xd = gbx.potrs_tiled(T, N, NB, B.clone())
+    A_host = torch.empty(A.numel(), dtype=torch.float64, pin_memory=True)
+    A_host.copy_(A)
+    B_host = torch.empty(B.shape, dtype=torch.float64, pin_memory=True)
+    B_host.copy_(B)
+    L_host, X_host, _ = gbx.dposv_tiled_host(A_host, N, NB, B_host, check=False)
+    _wait_stream(torch)
+    assert torch.equal(L_host, T.cpu())
+    assert torch.equal(X_host, Xd.cpu())
+
+
+def test_dposv_tiled_host_non_spd_completes(gbx, cuda):
+    """A breakdown stops the executor early; the copy-out stream is released and the call ends with
+    the pivot status."""
+    import ctypes
+    import torch
+    N, NB = 2048, 512
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=3)
+    A_host = torch.empty(A.numel(), dtype=torch.float64, pin_memory=True)
+    A_host.copy_(A)
+    slot = 2 * 4 - 2 * 1 // 2  # tile (2, 2) of NT = 4
+    A_host[slot * NB * NB + 5 + 5 * NB] = -1e6  # row 1029 of the matrix
+    B_host = torch.ones(1, N, dtype=torch.float64).pin_memory()
+    need = ctypes.c_size_t(0)
+    gbx.call("gbx_dposv_tiled_host_bufferSize", N, NB, ctypes.byref(need))
+    work = torch.empty(need.value, dtype=torch.uint8, device=cuda)
+    L_host, X_host, _ = gbx.dposv_tiled_host(A_host, N, NB, B_host, work=work, check=False)
+    _wait_stream(torch)
+    st = gbx.call("gbx_dpotrf_tiled_status", ctypes.c_void_p(work.data_ptr()),
+                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 2 * NB + 5 + 1

@@ -72,6 +72,8 @@ SIGNATURES = {
     "gbx_dposv_batched": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
     "gbx_dposv_batched_ex": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _sz, _vp]),
     "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
+    "gbx_dposv_tiled_host_bufferSize": (_i, [_i, _i, _szp]),
+    "gbx_dposv_tiled_host": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gbx_potrf_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _szp]),
     "gbx_potrf_mixed_batched": (_i, [_i, _vp, _i, _vp, _vp, _i, _d, _vp, _vp, _sz, _vp]),
     "gbx_potrf_mixed_batched_info": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
@@ -232,6 +234,29 @@ def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=N
     if st < 0 and st != GBX_ERR_NOCONV:
         raise GbxError("gbx_dposv_mixed", st)
     return X, info.as_dict(), st
+
+
+def dposv_tiled_host(A_host, N, NB, B_host, tiles=None, X=None, work=None, L_host=None, X_host=None, stream=None,
+                     check=True):
+    """Factor + solve from host buffers with the copies overlapped (gbx_dposv_tiled_host).
+    A_host: tile-major lower FP64 (pinned CPU tensor); B_host: (nrhs, N) pinned CPU tensor.
+    Returns (L_host, X_host, status); with check=True the stream is synchronised first."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nrhs = 1 if B_host.dim() == 1 else B_host.shape[0]
+    need = _sz(0)
+    call("gbx_dposv_tiled_host_bufferSize", N, NB, ctypes.byref(need))
+    if work is None or work.numel() < need.value:
+        work = torch.empty(need.value, dtype=torch.uint8, device=dev)
+    tiles = torch.empty(A_host.numel(), dtype=torch.float64, device=dev) if tiles is None else tiles
+    X = torch.empty(B_host.shape, dtype=torch.float64, device=dev) if X is None else X
+    L_host = torch.empty(A_host.shape, dtype=torch.float64, pin_memory=True) if L_host is None else L_host
+    X_host = torch.empty(B_host.shape, dtype=torch.float64, pin_memory=True) if X_host is None else X_host
+    s = _stream(stream)
+    call("gbx_dposv_tiled_host", N, NB, _ptr(A_host), _ptr(L_host), nrhs, _ptr(B_host), _ptr(X_host), _ptr(tiles),
+         _ptr(X), _ptr(work), need.value, s)
+    st = call("gbx_dpotrf_tiled_status", _ptr(work), s) if check else None
+    return L_host, X_host, st
 
 
 def batched_tile_offsets(sizes, NB):

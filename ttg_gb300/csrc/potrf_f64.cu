@@ -5,6 +5,7 @@
 // pipe busy (enough independent FMAs per warp, operands staged in shared memory, L2-only loads)
 // and the executor is organised to keep every SM busy (device-side ready queue, lookahead order,
 // fine-grained 128 x 128 blocks, no host round trip per task).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -84,7 +85,18 @@ struct DagParams {
   DagState* st;
   int* cnt;            // packed lower per-block completion counters
   uint64_t timeout_ns;
+  // host-overlapped runs (gbx_dposv_tiled_host), else null: arrived[k] != 0 once tile column k is
+  // in HBM; col_done[k] counts finished POTRF/TRSM blocks of tile column k; tile_r blocks per tile
+  const int* arrived;
+  int* col_done;
+  int tile_r, tile_cols;
 };
+
+// stream waits on col_done must end on every exit: a launch that stops early sets every count high
+__device__ __forceinline__ void release_columns(const DagParams& P) {
+  if (P.col_done && ld_volatile(&P.st->abort))
+    for (int k = 0; k < P.tile_cols; ++k) atomicExch(P.col_done + k, 1 << 30);
+}
 
 // Persistent executor: one CTA per SM takes tasks from the ready queue in order.
 // Counter protocol (writers of block (M,N) in order: GEMM(M,N,0..N-1), then TRSM(M,N); of (M,M):
@@ -112,7 +124,14 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     int* target;
     if (threadIdx.x == 0) {
       bool ok = true;
-      switch (tk.type) {
+      if (P.arrived) {  // the tile columns the task touches must be in HBM
+        const int* arr = P.arrived;
+        const int r = P.tile_r;
+        const int c1 = tk.type == T_POTRF ? tk.a : tk.type == T_TRSM ? tk.b : tk.type == T_SYRK ? tk.a : tk.c;
+        const int c2 = tk.type == T_SYRK ? tk.b : tk.type == T_GEMM ? tk.b : c1;
+        ok = wait_geq(arr + c1 / r, 1, P.st, P.timeout_ns) && wait_geq(arr + c2 / r, 1, P.st, P.timeout_ns);
+      }
+      if (ok) switch (tk.type) {
         case T_POTRF:
           ok = wait_geq(P.cnt + tri_index(tk.a, tk.a, NTb), tk.a, P.st, P.timeout_ns);
           break;
@@ -143,6 +162,7 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
           if (threadIdx.x == 0) {
             atomicCAS(&P.st->status, 0, K * V.b + info);
             atomicExch(&P.st->abort, 1);
+            release_columns(P);
           }
           __syncthreads();
           return;
@@ -174,9 +194,12 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     __syncthreads();
     if (threadIdx.x == 0) {
       signal_done(target);
+      if (P.col_done && (tk.type == T_POTRF || tk.type == T_TRSM))  // block (a, b) of L is final
+        atomicAdd(P.col_done + (tk.type == T_POTRF ? tk.a : tk.b) / P.tile_r, 1);
       trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);
     }
   }
+  if (threadIdx.x == 0) release_columns(P);
 }
 
 // ---- single-purpose grids for the tile-level entry points ------------------------------------
@@ -446,7 +469,7 @@ size_t dag_workspace_bytes(int NTb) {
 }
 
 int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaStream_t s, long long first_task,
-               uint64_t timeout_ns) {
+               uint64_t timeout_ns, const int* arrived = nullptr, int* col_done = nullptr) {
   const size_t need = dag_workspace_bytes(NTb);
   if (work == nullptr || work_bytes < need) return GBX_ERR_WORKSPACE;
   DevInfo di;
@@ -462,6 +485,10 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   P.cnt = (int*)((char*)work + sizeof(DagState));
   P.timeout_ns = timeout_ns;
   P.trace = current_trace();
+  P.arrived = arrived;
+  P.col_done = col_done;
+  P.tile_r = V.r;
+  P.tile_cols = V.NT;
   long long grid = (long long)di.sms * di.dag_blocks_per_sm;
   grid = std::max(1LL, std::min(grid, P.ntasks));
   potrf_dag_f64_kernel<<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(P);
@@ -625,6 +652,120 @@ int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, in
     if (K > 0) trsv_update_kernel<<<K, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 1);
   }
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+// ---- factorisation and solve from host buffers with the copies overlapped --------------------
+// Tile column n of the input goes to HBM on a copy stream, followed by a stream memory write of
+// arrived[n]; the executor's tasks wait (bounded) for the columns they touch. Each finished
+// POTRF/TRSM block adds to col_done of its tile column, and a second copy stream waits on that
+// count (stream memory wait) before it copies the column back. The executor sets every count high
+// on any early exit, so the copy stream never waits forever. Stream memory operations come from
+// the driver entry points; the copy streams and events are per device, created on first use.
+namespace {
+typedef CUresult (*PFN_streamValue32)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+struct HostOverlap {
+  PFN_streamValue32 write = nullptr, wait = nullptr;
+  cudaStream_t in = nullptr, out = nullptr;
+  cudaEvent_t ev0 = nullptr, ev_in = nullptr, ev_out = nullptr;
+  bool ready = false;
+};
+std::mutex g_host_mtx;
+HostOverlap g_host[32];
+
+int host_overlap(HostOverlap*& ho) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 32) return GBX_ERR_CUDA;
+  HostOverlap& h = g_host[dev];
+  ho = &h;
+  if (h.ready) return GBX_OK;
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p)
+    return GBX_ERR_CUDA;
+  h.write = (PFN_streamValue32)p;
+  p = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuStreamWaitValue32", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p)
+    return GBX_ERR_CUDA;
+  h.wait = (PFN_streamValue32)p;
+  if (cudaStreamCreateWithFlags(&h.in, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h.out, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h.ev0, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h.ev_in, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h.ev_out, cudaEventDisableTiming) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  h.ready = true;
+  return GBX_OK;
+}
+size_t host_dag_bytes(int N, int NB) {
+  size_t b = 0;
+  gbx_dpotrf_tiled_bufferSize(N, NB, &b);
+  return (b + 255) / 256 * 256;
+}
+}  // namespace
+
+int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes) {
+  if (N <= 0 || NB <= 0 || block_edge(NB) == 0 || !bytes) return GBX_ERR_ARG;
+  const int NT = (N + NB - 1) / NB;
+  *bytes = host_dag_bytes(N, NB) + (size_t)2 * NT * sizeof(int);
+  return GBX_OK;
+}
+
+int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, int nrhs, const double* B_host,
+                         double* X_host, double* tiles, double* X, void* work, size_t work_bytes, void* stream) {
+  size_t need = 0;
+  if (int e = gbx_dposv_tiled_host_bufferSize(N, NB, &need)) return e;
+  if (nrhs < 0 || !A_host || !L_host || !tiles || (nrhs > 0 && (!B_host || !X_host || !X))) return GBX_ERR_ARG;
+  if (!work || work_bytes < need) return GBX_ERR_WORKSPACE;
+  std::lock_guard<std::mutex> lk(g_host_mtx);  // one caller at a time on the shared copy streams
+  HostOverlap* h = nullptr;
+  if (int e = host_overlap(h)) return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  const BlockView V = tiled_view(N, NB, tiles);
+  const int NTb = (N + V.b - 1) / V.b, NT = V.NT, r = V.r;
+  const size_t dag = host_dag_bytes(N, NB);
+  int* arrived = (int*)((char*)work + dag);
+  int* col_done = arrived + NT;
+  const long long tile = (long long)NB * NB;
+  auto col_off = [&](int n) { return ((long long)n * NT - (long long)n * (n - 1) / 2) * tile; };
+  if (cudaMemsetAsync(arrived, 0, (size_t)2 * NT * sizeof(int), s) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaEventRecord(h->ev0, s) != cudaSuccess || cudaStreamWaitEvent(h->in, h->ev0, 0) != cudaSuccess ||
+      cudaStreamWaitEvent(h->out, h->ev0, 0) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  for (int n = 0; n < NT; ++n) {  // copy-in, one tile column at a time
+    const long long off = col_off(n), cnt = (long long)(NT - n) * tile;
+    if (cudaMemcpyAsync(tiles + off, A_host + off, (size_t)cnt * sizeof(double), cudaMemcpyHostToDevice, h->in) !=
+            cudaSuccess ||
+        h->write((CUstream)h->in, (CUdeviceptr)(arrived + n), 1, 0) != CUDA_SUCCESS)
+      return GBX_ERR_CUDA;
+  }
+  if (nrhs > 0 && cudaMemcpyAsync(X, B_host, (size_t)N * nrhs * sizeof(double), cudaMemcpyHostToDevice, h->in) !=
+                      cudaSuccess)
+    return GBX_ERR_CUDA;
+  if (cudaEventRecord(h->ev_in, h->in) != cudaSuccess) return GBX_ERR_CUDA;
+  if (int e = launch_dag(V, NTb, work, dag, s, 0, gbx_get_wait_timeout_ns(), arrived, col_done)) {
+    cudaMemsetAsync(col_done, 0x7f, (size_t)NT * sizeof(int), s);  // nothing will count: release the copy stream
+    return e;
+  }
+  for (int k = 0; k < NT; ++k) {  // copy-out, each column as soon as its blocks are final
+    unsigned target = 0;
+    for (int J = k * r; J < std::min((k + 1) * r, NTb); ++J) target += (unsigned)(NTb - J);
+    const long long off = col_off(k), cnt = (long long)(NT - k) * tile;
+    if (h->wait((CUstream)h->out, (CUdeviceptr)(col_done + k), target, 0 /* CU_STREAM_WAIT_VALUE_GEQ */) !=
+            CUDA_SUCCESS ||
+        cudaMemcpyAsync(L_host + off, tiles + off, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, h->out) !=
+            cudaSuccess)
+      return GBX_ERR_CUDA;
+  }
+  if (cudaEventRecord(h->ev_out, h->out) != cudaSuccess || cudaStreamWaitEvent(s, h->ev_in, 0) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  if (nrhs > 0) {
+    if (int e = gbx_dpotrs_tiled(N, NB, tiles, nrhs, X, N, stream)) return e;
+    if (cudaMemcpyAsync(X_host, X, (size_t)N * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return GBX_ERR_CUDA;
+  }
+  return cudaStreamWaitEvent(s, h->ev_out, 0) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
 static int gen_tiles(int N, int NB, int kind, double v, unsigned long long seed, double* tiles, void* stream) {
