@@ -243,9 +243,11 @@ int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, in
 
 /* Factorisation and solve from host buffers (pinned for overlap): A_host and L_host hold the
  * tile-major lower storage (tiled_numel doubles), B_host / X_host are column-major N x nrhs; tiles
- * and X are device buffers of the same sizes. Tile columns are copied in while the executor runs,
- * each column of L is copied back as soon as it is final, then X = (L L^T)^{-1} B comes back.
- * Asynchronous on `stream`; gbx_dpotrf_tiled_status(work) gives the factorisation status. No
+ * and X are device buffers of the same sizes. A and B are copied in, the executor runs, each tile
+ * column of L is copied back as soon as it is final (while the factorisation goes on), then
+ * X = (L L^T)^{-1} B comes back. Returns once the factorisation has finished on the device (the
+ * calling thread issues the copy-out as the columns complete); the solve and the last copies are
+ * still queued on `stream`. gbx_dpotrf_tiled_status(work) gives the factorisation status. No
  * counterpart in the reference, whose tiles reach the device through PaRSEC's stage-in
  * (parsec/ttg.h:1434-1672) and come back on wait() (parsec/devicefunc.h:232-256). */
 int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes);

@@ -5,12 +5,13 @@
 // pipe busy (enough independent FMAs per warp, operands staged in shared memory, L2-only loads)
 // and the executor is organised to keep every SM busy (device-side ready queue, lookahead order,
 // fine-grained 128 x 128 blocks, no host round trip per task).
-#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "block_ops.cuh"
@@ -85,17 +86,26 @@ struct DagParams {
   DagState* st;
   int* cnt;            // packed lower per-block completion counters
   uint64_t timeout_ns;
-  // host-overlapped runs (gbx_dposv_tiled_host), else null: arrived[k] != 0 once tile column k is
-  // in HBM; col_done[k] counts finished POTRF/TRSM blocks of tile column k; tile_r blocks per tile
-  const int* arrived;
+  // host-buffer runs (gbx_dposv_tiled_host), else null: col_done[g] counts finished POTRF/TRSM
+  // blocks of the g-th group of group_blocks consecutive block columns; the block that completes a
+  // group raises host_flag[g] (mapped pinned host memory) to 1
   int* col_done;
-  int tile_r, tile_cols;
+  volatile int* host_flag;
+  int group_blocks, groups;
 };
 
-// stream waits on col_done must end on every exit: a launch that stops early sets every count high
+// finished POTRF/TRSM blocks a group needs: block columns J of the group hold NTb - J blocks each
+__device__ __forceinline__ int group_target(const DagParams& P, int g) {
+  const int a = g * P.group_blocks, b = min(P.NTb, a + P.group_blocks);
+  return (b - a) * P.NTb - (a + b - 1) * (b - a) / 2;
+}
+
+// the host waits on host_flag: a launch that stops early raises every flag to 2
 __device__ __forceinline__ void release_columns(const DagParams& P) {
-  if (P.col_done && ld_volatile(&P.st->abort))
-    for (int k = 0; k < P.tile_cols; ++k) atomicExch(P.col_done + k, 1 << 30);
+  if (P.host_flag && ld_volatile(&P.st->abort)) {
+    __threadfence_system();
+    for (int k = 0; k < P.groups; ++k) P.host_flag[k] = 2;
+  }
 }
 
 // Persistent executor: one CTA per SM takes tasks from the ready queue in order.
@@ -124,14 +134,7 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     int* target;
     if (threadIdx.x == 0) {
       bool ok = true;
-      if (P.arrived) {  // the tile columns the task touches must be in HBM
-        const int* arr = P.arrived;
-        const int r = P.tile_r;
-        const int c1 = tk.type == T_POTRF ? tk.a : tk.type == T_TRSM ? tk.b : tk.type == T_SYRK ? tk.a : tk.c;
-        const int c2 = tk.type == T_SYRK ? tk.b : tk.type == T_GEMM ? tk.b : c1;
-        ok = wait_geq(arr + c1 / r, 1, P.st, P.timeout_ns) && wait_geq(arr + c2 / r, 1, P.st, P.timeout_ns);
-      }
-      if (ok) switch (tk.type) {
+      switch (tk.type) {
         case T_POTRF:
           ok = wait_geq(P.cnt + tri_index(tk.a, tk.a, NTb), tk.a, P.st, P.timeout_ns);
           break;
@@ -194,8 +197,13 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     __syncthreads();
     if (threadIdx.x == 0) {
       signal_done(target);
-      if (P.col_done && (tk.type == T_POTRF || tk.type == T_TRSM))  // block (a, b) of L is final
-        atomicAdd(P.col_done + (tk.type == T_POTRF ? tk.a : tk.b) / P.tile_r, 1);
+      if (P.col_done && (tk.type == T_POTRF || tk.type == T_TRSM)) {  // block (a, b) of L is final
+        const int g = (tk.type == T_POTRF ? tk.a : tk.b) / P.group_blocks;
+        if (atomicAdd(P.col_done + g, 1) + 1 == group_target(P, g)) {
+          __threadfence_system();  // every block of the group (each CTA fenced before counting) first
+          P.host_flag[g] = 1;
+        }
+      }
       trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);
     }
   }
@@ -469,7 +477,8 @@ size_t dag_workspace_bytes(int NTb) {
 }
 
 int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaStream_t s, long long first_task,
-               uint64_t timeout_ns, const int* arrived = nullptr, int* col_done = nullptr) {
+               uint64_t timeout_ns, int* col_done = nullptr, volatile int* host_flag = nullptr,
+               int group_blocks = 1) {
   const size_t need = dag_workspace_bytes(NTb);
   if (work == nullptr || work_bytes < need) return GBX_ERR_WORKSPACE;
   DevInfo di;
@@ -485,10 +494,10 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   P.cnt = (int*)((char*)work + sizeof(DagState));
   P.timeout_ns = timeout_ns;
   P.trace = current_trace();
-  P.arrived = arrived;
   P.col_done = col_done;
-  P.tile_r = V.r;
-  P.tile_cols = V.NT;
+  P.host_flag = host_flag;
+  P.group_blocks = group_blocks;
+  P.groups = (NTb + group_blocks - 1) / group_blocks;
   long long grid = (long long)di.sms * di.dag_blocks_per_sm;
   grid = std::max(1LL, std::min(grid, P.ntasks));
   potrf_dag_f64_kernel<<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(P);
@@ -654,21 +663,29 @@ int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, in
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
-// ---- factorisation and solve from host buffers with the copies overlapped --------------------
-// Tile column n of the input goes to HBM on a copy stream, followed by a stream memory write of
-// arrived[n]; the executor's tasks wait (bounded) for the columns they touch. Each finished
-// POTRF/TRSM block adds to col_done of its tile column, and a second copy stream waits on that
-// count (stream memory wait) before it copies the column back. The executor sets every count high
-// on any early exit, so the copy stream never waits forever. Stream memory operations come from
-// the driver entry points; the copy streams and events are per device, created on first use.
+// ---- factorisation and solve from host buffers, the copies overlapped ---------------------------
+//   copy-in:  tile columns go to HBM one by one on a copy stream, each followed by a 4-byte copy
+//             that raises its arrival flag in device memory; executor tasks check (bounded) the
+//             flags of the columns they touch until the flag "every column is in" is up, after
+//             which they stop checking;
+//   copy-out: each finished POTRF/TRSM block adds to the count of its group of tile columns
+//             (about eight groups); the block that completes a group raises the group's flag in
+//             mapped pinned host memory, and the calling thread, which polls those flags, issues
+//             that group's copy back (its tiles are contiguous) on a second copy stream, so L
+//             streams out while the factorisation runs.
+// Stream memory operations were measured to signal a quarter of a second late on this platform,
+// hence plain copies and a polling thread. The executor raises every group flag on any early
+// exit, and the thread also stops when the launch has finished, so no side waits on a flag that
+// cannot come.
 namespace {
-typedef CUresult (*PFN_streamValue32)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
 struct HostOverlap {
-  PFN_streamValue32 write = nullptr, wait = nullptr;
-  cudaStream_t in = nullptr, out = nullptr;
-  cudaEvent_t ev0 = nullptr, ev_in = nullptr, ev_out = nullptr;
+  cudaStream_t out = nullptr;
+  cudaEvent_t ev0 = nullptr, ev_kernel = nullptr, ev_out = nullptr;
+  int* flags = nullptr;        // pinned mapped host memory: kMaxGroups copy-out flags
+  int* flags_dev = nullptr;    // its device address
   bool ready = false;
 };
+constexpr int kMaxGroups = 64;
 std::mutex g_host_mtx;
 HostOverlap g_host[32];
 
@@ -678,22 +695,12 @@ int host_overlap(HostOverlap*& ho) {
   HostOverlap& h = g_host[dev];
   ho = &h;
   if (h.ready) return GBX_OK;
-  void* p = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-      q != cudaDriverEntryPointSuccess || !p)
-    return GBX_ERR_CUDA;
-  h.write = (PFN_streamValue32)p;
-  p = nullptr;
-  if (cudaGetDriverEntryPointByVersion("cuStreamWaitValue32", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-      q != cudaDriverEntryPointSuccess || !p)
-    return GBX_ERR_CUDA;
-  h.wait = (PFN_streamValue32)p;
-  if (cudaStreamCreateWithFlags(&h.in, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h.out, cudaStreamNonBlocking) != cudaSuccess ||
+  if (cudaStreamCreateWithFlags(&h.out, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&h.ev0, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h.ev_in, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h.ev_out, cudaEventDisableTiming) != cudaSuccess)
+      cudaEventCreateWithFlags(&h.ev_kernel, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h.ev_out, cudaEventDisableTiming) != cudaSuccess ||
+      cudaHostAlloc((void**)&h.flags, kMaxGroups * sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&h.flags_dev, h.flags, 0) != cudaSuccess)
     return GBX_ERR_CUDA;
   h.ready = true;
   return GBX_OK;
@@ -707,8 +714,7 @@ size_t host_dag_bytes(int N, int NB) {
 
 int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes) {
   if (N <= 0 || NB <= 0 || block_edge(NB) == 0 || !bytes) return GBX_ERR_ARG;
-  const int NT = (N + NB - 1) / NB;
-  *bytes = host_dag_bytes(N, NB) + (size_t)2 * NT * sizeof(int);
+  *bytes = host_dag_bytes(N, NB) + (size_t)kMaxGroups * sizeof(int);
   return GBX_OK;
 }
 
@@ -718,48 +724,53 @@ int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, in
   if (int e = gbx_dposv_tiled_host_bufferSize(N, NB, &need)) return e;
   if (nrhs < 0 || !A_host || !L_host || !tiles || (nrhs > 0 && (!B_host || !X_host || !X))) return GBX_ERR_ARG;
   if (!work || work_bytes < need) return GBX_ERR_WORKSPACE;
-  std::lock_guard<std::mutex> lk(g_host_mtx);  // one caller at a time on the shared copy streams
+  std::lock_guard<std::mutex> lk(g_host_mtx);  // one caller at a time on the shared flags and copy streams
   HostOverlap* h = nullptr;
   if (int e = host_overlap(h)) return e;
   cudaStream_t s = (cudaStream_t)stream;
   const BlockView V = tiled_view(N, NB, tiles);
   const int NTb = (N + V.b - 1) / V.b, NT = V.NT, r = V.r;
   const size_t dag = host_dag_bytes(N, NB);
-  int* arrived = (int*)((char*)work + dag);
-  int* col_done = arrived + NT;
+  int* col_done = (int*)((char*)work + dag);  // kMaxGroups counts
   const long long tile = (long long)NB * NB;
   auto col_off = [&](int n) { return ((long long)n * NT - (long long)n * (n - 1) / 2) * tile; };
-  if (cudaMemsetAsync(arrived, 0, (size_t)2 * NT * sizeof(int), s) != cudaSuccess) return GBX_ERR_CUDA;
-  if (cudaEventRecord(h->ev0, s) != cudaSuccess || cudaStreamWaitEvent(h->in, h->ev0, 0) != cudaSuccess ||
-      cudaStreamWaitEvent(h->out, h->ev0, 0) != cudaSuccess)
+  const int G = (NT + 7) / 8, ngroups = (NT + G - 1) / G;  // tile columns per copy-out group (<= 8 groups)
+  // the previous call's launch may still be leaving (an aborted launch raises flags from every CTA)
+  if (cudaEventSynchronize(h->ev_kernel) != cudaSuccess) return GBX_ERR_CUDA;
+  volatile int* out_flag = h->flags;
+  for (int g = 0; g < ngroups; ++g) out_flag[g] = 0;
+  // copy-in: one copy of the whole tile array (copies interleaved with other stream operations ran
+  // many times slower here), then the right-hand sides
+  if (cudaMemcpyAsync(tiles, A_host, (size_t)col_off(NT) * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return GBX_ERR_CUDA;
-  for (int n = 0; n < NT; ++n) {  // copy-in, one tile column at a time
-    const long long off = col_off(n), cnt = (long long)(NT - n) * tile;
-    if (cudaMemcpyAsync(tiles + off, A_host + off, (size_t)cnt * sizeof(double), cudaMemcpyHostToDevice, h->in) !=
-            cudaSuccess ||
-        h->write((CUstream)h->in, (CUdeviceptr)(arrived + n), 1, 0) != CUDA_SUCCESS)
-      return GBX_ERR_CUDA;
-  }
-  if (nrhs > 0 && cudaMemcpyAsync(X, B_host, (size_t)N * nrhs * sizeof(double), cudaMemcpyHostToDevice, h->in) !=
-                      cudaSuccess)
+  if (nrhs > 0 &&
+      cudaMemcpyAsync(X, B_host, (size_t)N * nrhs * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return GBX_ERR_CUDA;
-  if (cudaEventRecord(h->ev_in, h->in) != cudaSuccess) return GBX_ERR_CUDA;
-  if (int e = launch_dag(V, NTb, work, dag, s, 0, gbx_get_wait_timeout_ns(), arrived, col_done)) {
-    cudaMemsetAsync(col_done, 0x7f, (size_t)NT * sizeof(int), s);  // nothing will count: release the copy stream
-    return e;
-  }
-  for (int k = 0; k < NT; ++k) {  // copy-out, each column as soon as its blocks are final
-    unsigned target = 0;
-    for (int J = k * r; J < std::min((k + 1) * r, NTb); ++J) target += (unsigned)(NTb - J);
-    const long long off = col_off(k), cnt = (long long)(NT - k) * tile;
-    if (h->wait((CUstream)h->out, (CUdeviceptr)(col_done + k), target, 0 /* CU_STREAM_WAIT_VALUE_GEQ */) !=
-            CUDA_SUCCESS ||
-        cudaMemcpyAsync(L_host + off, tiles + off, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, h->out) !=
-            cudaSuccess)
-      return GBX_ERR_CUDA;
-  }
-  if (cudaEventRecord(h->ev_out, h->out) != cudaSuccess || cudaStreamWaitEvent(s, h->ev_in, 0) != cudaSuccess)
+  if (cudaMemsetAsync(col_done, 0, (size_t)kMaxGroups * sizeof(int), s) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaEventRecord(h->ev0, s) != cudaSuccess || cudaStreamWaitEvent(h->out, h->ev0, 0) != cudaSuccess)
     return GBX_ERR_CUDA;
+  if (int e = launch_dag(V, NTb, work, dag, s, 0, gbx_get_wait_timeout_ns(), col_done, h->flags_dev, G * r)) return e;
+  if (cudaEventRecord(h->ev_kernel, s) != cudaSuccess) return GBX_ERR_CUDA;
+  // copy-out: each group as soon as the executor raises its flag
+  for (int g = 0; g < ngroups;) {
+    if (out_flag[g] != 0) {
+      const int k0 = g * G, k1 = std::min(NT, k0 + G);
+      const long long off = col_off(k0), cnt = col_off(k1) - off;
+      if (cudaMemcpyAsync(L_host + off, tiles + off, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, h->out) !=
+          cudaSuccess)
+        return GBX_ERR_CUDA;
+      ++g;
+      continue;
+    }
+    const cudaError_t q = cudaEventQuery(h->ev_kernel);
+    if (q == cudaSuccess) {  // the launch is over: its flags are all visible by now
+      if (out_flag[g] != 0) continue;
+      return GBX_ERR_CUDA;  // finished without completing the group and without an abort: a failure
+    }
+    if (q != cudaErrorNotReady) return GBX_ERR_CUDA;
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  if (cudaEventRecord(h->ev_out, h->out) != cudaSuccess) return GBX_ERR_CUDA;
   if (nrhs > 0) {
     if (int e = gbx_dpotrs_tiled(N, NB, tiles, nrhs, X, N, stream)) return e;
     if (cudaMemcpyAsync(X_host, X, (size_t)N * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)
