@@ -314,6 +314,7 @@ def run_ours(args, ws, rank, local):
         torch.cuda.empty_cache()
         line["batched_mixed"] = run_batched_mixed(gbx, dev, cpu=rank == 0 and not args.no_cpu)
     line["config_small"] = run_config1(gbx, dev, cpu=rank == 0 and not args.no_cpu)
+    line["potri"] = run_potri(gbx, dev, cpu=rank == 0 and not args.no_cpu)
 
     if rank == 0 and not args.no_cpu:
         times, blas = cpu_run(args.cpu_N, NB, 2)
@@ -562,6 +563,66 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
         out["cpu_baseline"] = {"value": sflops / sec / 1e12, "unit": "TFLOP/s", "cores": cpu_cores(), "kind": "port",
                                "sample": "first %d matrices of the batch, FP64 dpotrf+dpotrs per matrix (%s), one "
                                          "matrix per thread" % (cpu_sample, "OpenBLAS" if blas else "plain loops")}
+    return out
+
+
+def _dense_from_tiles(t, N, NB):
+    """Full symmetric matrix on the device from lower tiles (torch slicing, one tile at a time)."""
+    import torch
+    NT = (N + NB - 1) // NB
+    D = torch.zeros(N, N, dtype=torch.float64, device=t.device)
+    tl = NB * NB
+    for n in range(NT):
+        for m in range(n, NT):
+            slot = n * NT - n * (n - 1) // 2 + (m - n)
+            mb, nb = min(NB, N - m * NB), min(NB, N - n * NB)
+            blk = t[slot * tl:(slot + 1) * tl].view(NB, NB).T[:mb, :nb]  # column-major tile
+            if m == n:
+                blk = torch.tril(blk)
+            D[m * NB:m * NB + mb, n * NB:n * NB + nb] = blk
+    return D + torch.tril(D, -1).T
+
+
+def run_potri(gbx, dev, N=8192, NB=512, reps=3, cpu=True):
+    """Inverse from the factor (the reference's POTRI chain, TRTRI + LAUUM), FP64, N=8192 NB=512:
+    device time of gbx_dpotri_tiled and the residual ||A X v - v|| / ||v|| for a random v."""
+    import numpy as np
+    import torch
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
+    gbx.gen_uniform_sym(A, N, NB, seed=42)
+    L = A.clone()
+    gbx.potrf_tiled(L, N, NB)
+    T = torch.empty_like(L)
+    times = []
+    for i in range(reps + 1):
+        T.copy_(L)
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        gbx.potri_tiled(T, N, NB)
+        e1.record()
+        e1.synchronize()
+        if i:
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    flops = N * ((2.0 / 3) + N * ((1.0 / 3) * N + 1)) + N * ((1.0 / 6) + N * ((1.0 / 3) * N - 0.5))  # FLOPS_DPOTRI
+    Ad, Xd = _dense_from_tiles(A, N, NB), _dense_from_tiles(T, N, NB)
+    v = torch.randn(N, dtype=torch.float64, device=dev)
+    res = ((Ad @ (Xd @ v) - v).norm() / v.norm()).item()
+    out = {"config": {"workload": "potri FP64 N=%d NB=%d from the factor of (M+M^T)/2 + N*I seed 42" % (N, NB),
+                      "N": N, "NB": NB, "flops": flops},
+           "gpu": {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "residual_AXv_minus_v": res}}
+    if cpu:
+        import oracle
+        n_s = 1024  # bounded CPU sample: the restated tile algorithm in plain loops, one thread
+        t = oracle.uniform_sym_tiles(n_s, 128, 42)
+        oracle.potrf_tiled(t, n_s, 128, nthreads=0, use_blas=oracle.load_openblas())
+        t0 = time.perf_counter()
+        oracle.potri_tiled(t, n_s, 128)
+        sec = time.perf_counter() - t0
+        fs = n_s * ((2.0 / 3) + n_s * ((1.0 / 3) * n_s + 1)) + n_s * ((1.0 / 6) + n_s * ((1.0 / 3) * n_s - 0.5))
+        out["cpu_baseline"] = {"value": fs / sec / 1e12, "unit": "TFLOP/s", "cores": 1, "kind": "port",
+                               "sample": "N=%d NB=128, the oracle's plain-loop tile TRTRI + LAUUM, one thread" % n_s}
     return out
 
 

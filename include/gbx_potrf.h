@@ -241,6 +241,14 @@ int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, in
                             int prec, double tol, int maxiter, float* W, void* work, size_t work_bytes,
                             gbx_refine_info* info, void* stream);
 
+/* Inverse of the SPD matrix from its factor, in place (replaces the reference's host-only POTRI
+ * chain, examples/potrf/potri.h:18-29: TRTRI of the lower factor, trtri_L.h, then LAUUM,
+ * lauum.h): on entry the lower tiles hold L from gbx_dpotrf_tiled, on exit the lower triangle of
+ * A^{-1} (strict upper parts of diagonal tiles and padding past N: unspecified). FP64, NB a
+ * multiple of 128; asynchronous on `stream`. */
+int gbx_dpotri_tiled_bufferSize(int N, int NB, size_t* bytes);
+int gbx_dpotri_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream);
+
 /* Factorisation and solve from host buffers (pinned for overlap): A_host and L_host hold the
  * tile-major lower storage (tiled_numel doubles), B_host / X_host are column-major N x nrhs; tiles
  * and X are device buffers of the same sizes. A and B are copied in, the executor runs, each tile

@@ -56,6 +56,8 @@ def lib():
         L.orc_dposv_batched.argtypes = [ctypes.c_int, _ip, _i64p, _i64p, _dp, _dp, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, _ip]
         L.orc_gen_uniform_sym_batched.argtypes = [ctypes.c_int, _ip, _i64p, ctypes.c_uint64, _dp]
+        L.orc_potri_tiled.restype = ctypes.c_int
+        L.orc_potri_tiled.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
         _lib = L
     return _lib
 
@@ -196,3 +198,8 @@ def dposv_batched(sizes, A, B, nrhs=1, nthreads=0, use_blas=False):
     lib().orc_dposv_batched(len(n), n.ctypes.data_as(_ip), offA.ctypes.data_as(_i64p), offB.ctypes.data_as(_i64p),
                             _p(A), _p(B), nrhs, nthreads, 1 if use_blas else 0, info.ctypes.data_as(_ip))
     return info
+
+
+def potri_tiled(tiles, N, NB):
+    """In place: the lower tiles of L become the lower triangle of A^{-1} (restated TRTRI + LAUUM)."""
+    return lib().orc_potri_tiled(N, NB, _p(tiles))

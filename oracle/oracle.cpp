@@ -587,3 +587,89 @@ extern "C" void orc_gen_uniform_sym_batched(int batch, const int* n, const int64
   for (int k = 0; k < batch; ++k)
     orc_gen_uniform_sym_colmajor(n[k], seed + (uint64_t)k * 0x9e3779b97f4a7c15ULL, (double)n[k], A + offA[k], n[k]);
 }
+
+// ------------------------------------------------------------------------------------------------
+// inverse from the factor: TRTRI (examples/potrf/trtri_L.h: TRSMR, GEMM, TRSML, TRTRI tasks) then
+// LAUUM (examples/potrf/lauum.h: SYRK/GEMM, TRMM, LAUUM tasks), restated step by step on tiles
+// ------------------------------------------------------------------------------------------------
+namespace {
+struct TileMat {
+  int N, NB, NT;
+  double* t;
+  double* at(int m, int n) { return t + orc_tile_slot(m, n, NT) * (int64_t)NB * NB; }
+  int dim(int k) const { return tile_dim(k, NT, N, NB); }
+};
+// inverse of a lower triangular n x n block (column-major, ld), written as a dense lower matrix
+void tri_inverse_lower(int n, const double* L, int ld, std::vector<double>& X) {
+  X.assign((size_t)n * n, 0.0);
+  for (int j = 0; j < n; ++j) {  // column j of L^{-1}: forward substitution of e_j
+    X[j + (size_t)j * n] = 1.0 / L[j + (int64_t)j * ld];
+    for (int i = j + 1; i < n; ++i) {
+      double s = 0.0;
+      for (int p = j; p < i; ++p) s += L[i + (int64_t)p * ld] * X[p + (size_t)j * n];
+      X[i + (size_t)j * n] = -s / L[i + (int64_t)i * ld];
+    }
+  }
+}
+// C (m x n, ld NB) := beta C + alpha op(A) op(B) with op(X) = X or X^T, contraction length kd;
+// lowA / lowB: only the stored lower triangle of the operand counts
+void tile_gemm(int m, int n, int kd, bool ta, bool tb, bool lowA, bool lowB, const double* A, int lda, const double* B,
+               int ldb, double* C, int ldc, double alpha, double beta) {
+  std::vector<double> out((size_t)m * n, 0.0);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) {
+      double s = 0.0;
+      for (int p = 0; p < kd; ++p) {
+        const int ar = ta ? p : i, ac = ta ? i : p, br = tb ? j : p, bc = tb ? p : j;
+        if ((lowA && ar < ac) || (lowB && br < bc)) continue;
+        s += A[ar + (int64_t)ac * lda] * B[br + (int64_t)bc * ldb];
+      }
+      out[i + (size_t)j * m] = s;
+    }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) {
+      double& c = C[i + (int64_t)j * ldc];
+      c = (beta == 0.0 ? 0.0 : beta * c) + alpha * out[i + (size_t)j * m];
+    }
+}
+}  // namespace
+
+extern "C" int orc_potri_tiled(int N, int NB, double* tiles) {
+  TileMat A{N, NB, (N + NB - 1) / NB, tiles};
+  const int NT = A.NT;
+  std::vector<double> Linv, tmp;
+  for (int k = 0; k < NT; ++k) {  // TRTRI
+    const int kk = A.dim(k);
+    tri_inverse_lower(kk, A.at(k, k), NB, Linv);
+    for (int m = k + 1; m < NT; ++m) {  // A_mk := -A_mk L_kk^{-1}
+      const int mm = A.dim(m);
+      tmp.assign(A.at(m, k), A.at(m, k) + (size_t)NB * NB);
+      tile_gemm(mm, kk, kk, false, false, false, false, tmp.data(), NB, Linv.data(), kk, A.at(m, k), NB, -1.0, 0.0);
+    }
+    for (int m = k + 1; m < NT; ++m)  // A_mn += A_mk A_kn
+      for (int n = 0; n < k; ++n)
+        tile_gemm(A.dim(m), NB, kk, false, false, false, false, A.at(m, k), NB, A.at(k, n), NB, A.at(m, n), NB, 1.0, 1.0);
+    for (int n = 0; n < k; ++n) {  // A_kn := L_kk^{-1} A_kn
+      tmp.assign(A.at(k, n), A.at(k, n) + (size_t)NB * NB);
+      tile_gemm(kk, NB, kk, false, false, false, false, Linv.data(), kk, tmp.data(), NB, A.at(k, n), NB, 1.0, 0.0);
+    }
+    for (int j = 0; j < kk; ++j)
+      for (int i = j; i < kk; ++i) A.at(k, k)[i + (int64_t)j * NB] = Linv[i + (size_t)j * kk];
+  }
+  for (int k = 0; k < NT; ++k) {  // LAUUM
+    const int kk = A.dim(k);
+    for (int m = 0; m < k; ++m)  // A_mn += A_km^T A_kn
+      for (int n = 0; n <= m; ++n)
+        tile_gemm(NB, NB, kk, true, false, false, false, A.at(k, m), NB, A.at(k, n), NB, A.at(m, n), NB, 1.0, 1.0);
+    for (int n = 0; n < k; ++n) {  // A_kn := A_kk^T A_kn (A_kk lower)
+      tmp.assign(A.at(k, n), A.at(k, n) + (size_t)NB * NB);
+      tile_gemm(kk, NB, kk, true, false, true, false, A.at(k, k), NB, tmp.data(), NB, A.at(k, n), NB, 1.0, 0.0);
+    }
+    tmp.assign(A.at(k, k), A.at(k, k) + (size_t)NB * NB);  // A_kk := A_kk^T A_kk (lower)
+    std::vector<double> d((size_t)NB * NB, 0.0);
+    tile_gemm(kk, kk, kk, true, false, true, true, tmp.data(), NB, tmp.data(), NB, d.data(), NB, 1.0, 0.0);
+    for (int j = 0; j < kk; ++j)
+      for (int i = j; i < kk; ++i) A.at(k, k)[i + (int64_t)j * NB] = d[i + (size_t)j * NB];
+  }
+  return 0;
+}

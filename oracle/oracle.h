@@ -80,6 +80,11 @@ double orc_check_dpotrf(int N, const double* L, const double* A0);
 /* ||A0 - L L^T||_F / (N ||A0||_F), A0 full symmetric col-major, L lower col-major */
 double orc_frob_residual(int N, const double* L, const double* A0);
 
+/* ---- inverse from the factor (the reference's POTRI chain, examples/potrf/potri.h, trtri_L.h,
+ * lauum.h): the PLASMA tile algorithms TRTRI (lower, non-unit) then LAUUM, plain loops, in place
+ * on the lower tiles of the factor; returns 0 ---- */
+int orc_potri_tiled(int N, int NB, double* tiles);
+
 /* ---- batched solves (the per-matrix LAPACK loop a CPU user runs for many small systems) ---- */
 /* matrix k: n[k] x n[k] column-major at A + offA[k] (lower triangle read, factor written in place),
  * right-hand sides n[k] x nrhs at B + offB[k] (overwritten by the solution). Matrices are taken

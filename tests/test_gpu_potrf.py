@@ -367,3 +367,21 @@ def test_dposv_tiled_host_non_spd_completes(gbx, cuda):
     st = gbx.call("gbx_dpotrf_tiled_status", ctypes.c_void_p(work.data_ptr()),
                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert st == 2 * NB + 5 + 1
+
+
+@pytest.mark.parametrize("N,NB", [(1000, 128), (1800, 512), (512, 512)])
+def test_potri_matches_oracle_and_inverse(gbx, cuda, N, NB):
+    """Device TRTRI + LAUUM against the oracle's restatement (same factor) and numpy's inverse."""
+    import torch
+    A = oracle.uniform_sym_full(N, 33)
+    t0 = oracle.tiles_from_full(A, NB)
+    ref = t0.copy()
+    assert oracle.potrf_tiled(ref, N, NB, nthreads=0)[0] == 0
+    T = to_dev(ref, cuda)  # the same factor on both sides
+    gbx.potri_tiled(T, N, NB)
+    got = np.tril(oracle.tiles_to_lower(T.cpu().numpy(), N, NB))
+    assert oracle.potri_tiled(ref, N, NB) == 0
+    want = np.tril(oracle.tiles_to_lower(ref, N, NB))
+    scale = np.abs(want).max()
+    assert np.abs(got - want).max() <= 1e-13 * scale
+    assert np.abs(got - np.tril(np.linalg.inv(A))).max() <= 1e-12 * scale

@@ -160,3 +160,15 @@ def test_batched_oracle_reports_bad_matrix():
     B = np.ones(10)
     info = oracle.dposv_batched(sizes, A, B)
     assert info[0] == 0 and info[1] == 3
+
+
+@pytest.mark.parametrize("N,NB", [(700, 128), (300, 64), (128, 128)])
+def test_potri_oracle_inverse(N, NB):
+    """The restated TRTRI + LAUUM tile algorithm gives A^{-1} from the factor."""
+    A = oracle.uniform_sym_full(N, 21)
+    t = oracle.tiles_from_full(A, NB)
+    assert oracle.potrf_tiled(t, N, NB, nthreads=2)[0] == 0
+    assert oracle.potri_tiled(t, N, NB) == 0
+    Ainv = np.tril(oracle.tiles_to_lower(t, N, NB))
+    ref = np.tril(np.linalg.inv(A))
+    assert np.abs(Ainv - ref).max() <= 1e-13 * np.abs(ref).max()

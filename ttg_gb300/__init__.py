@@ -72,6 +72,8 @@ SIGNATURES = {
     "gbx_dposv_batched": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
     "gbx_dposv_batched_ex": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _sz, _vp]),
     "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
+    "gbx_dpotri_tiled_bufferSize": (_i, [_i, _i, _szp]),
+    "gbx_dpotri_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
     "gbx_dposv_tiled_host_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dposv_tiled_host": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gbx_potrf_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _szp]),
@@ -234,6 +236,17 @@ def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=N
     if st < 0 and st != GBX_ERR_NOCONV:
         raise GbxError("gbx_dposv_mixed", st)
     return X, info.as_dict(), st
+
+
+def potri_tiled(tiles, N, NB, workspace=None, stream=None):
+    """In place: the lower tiles of the factor L (from potrf_tiled) become the lower triangle of A^{-1}."""
+    import torch
+    need = _sz(0)
+    call("gbx_dpotri_tiled_bufferSize", N, NB, ctypes.byref(need))
+    if workspace is None or workspace.numel() < need.value:
+        workspace = torch.empty(need.value, dtype=torch.uint8, device=tiles.device)
+    call("gbx_dpotri_tiled", N, NB, _ptr(tiles), _ptr(workspace), need.value, _stream(stream))
+    return tiles
 
 
 def dposv_tiled_host(A_host, N, NB, B_host, tiles=None, X=None, work=None, L_host=None, X_host=None, stream=None,
