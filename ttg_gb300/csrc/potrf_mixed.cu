@@ -94,15 +94,17 @@ __host__ __device__ inline TileKey decode(long long t, int NT) {
 struct MixMat {
   long long slot0;
   int N, NT, cnt0, id;  // id: index into the per-matrix info / condition arrays
+  int dcnt0, pad;       // first counter of the diagonal tiles' 128-block counters (NT * nb * nb)
 };
-// a run of consecutive queue positions [start, next segment's start) holding the sub-task slots
-// local0.. of one matrix's own task order. Segments are ordered by phase (phase p of a matrix: its
+// a run of consecutive queue positions [start, next segment's start) holding, `mult` slots each,
+// the tile tasks task0.. of one matrix's own task order. Segments are ordered by phase (phase p of a matrix: its
 // tasks from POTRF(p) up to POTRF(p+1)), then by matrix, so the matrices of a batch advance side by
 // side; every matrix still sees its own tasks in its own order, which keeps in-order grabbing free
 // of deadlock.
 struct MixSeg {
-  long long start, local0;
-  int mat, pad;
+  long long start, task0;  // first queue position, first tile task (in the matrix's own order)
+  int mat, mult;           // matrix; queue slots per tile task in this segment
+  int sub0, pad;           // sub-task of the first slot (one-slot segments of POTRF mini-tasks)
 };
 
 struct Params {
@@ -114,7 +116,9 @@ struct Params {
   int f16;     // 1: fp16 operands, 0: bf16
   int sub_g;   // GEMM sub-tasks per tile = (NB/128)*(NB/256)
   int sub_t;   // TRSM sub-tasks per tile = NB/64
-  int slots;   // queue slots per tile task = max of the sub-task counts
+  int nb;      // 128-blocks per tile edge (the diagonal tile's POTRF is a mini flowgraph of them)
+  int npot;    // mini-tasks of a POTRF: per panel p, the block POTRF, nb-1-p TRSMs, their updates
+  int* dcnt;   // completion counters of the diagonal tiles' 128-blocks
   int sub_s;   // SYRK sub-tasks per tile (lower 128 x 256 sub-tiles)
   long long ntasks;  // sub-task slots of all matrices
   const MixMat* mats;
@@ -161,47 +165,57 @@ __device__ __forceinline__ float pow2f(int e) {
 }
 
 // ---- FP32 SIMT tasks ---------------------------------------------------------------------------
-__device__ int task_potrf(const Params& P, const Cur& cm, int K, float* sm) {
+// POTRF(K) as a right-looking flowgraph of 128-blocks inside the diagonal tile, one queue slot per
+// mini-task, in an order in which every mini-task waits only on earlier ones:
+//   for each panel p:  PF(p): block (p,p) := chol(block (p,p))
+//                      PT(p,i), i > p: block (i,p) := block (i,p) L_pp^{-T}
+//                      PU(p,i,j), i >= j > p: block (i,j) -= block (i,p) block (j,p)^T
+// Block counter (i,j) counts its finished writers (PU of panels < j, then PT/PF of panel j).
+struct Mini {
+  int kind, p, i, j;  // kind 0 PF, 1 PT, 2 PU
+};
+__host__ __device__ inline int panel_minis(int nb, int p) { return 1 + (nb - 1 - p) + (nb - 1 - p) * (nb - p) / 2; }
+__device__ inline Mini mini_decode(int sub, int nb) {
+  int p = 0;
+  while (sub >= panel_minis(nb, p)) sub -= panel_minis(nb, p++);
+  if (sub == 0) return Mini{0, p, p, p};
+  if (sub - 1 < nb - 1 - p) return Mini{1, p, p + sub, p};
+  int u = sub - 1 - (nb - 1 - p), j = p + 1;  // pairs i >= j > p, column by column
+  while (u >= nb - j) u -= nb - j++;
+  return Mini{2, p, j + u, j};
+}
+
+// returns 0 or the 1-based pivot index within the block (PF only)
+__device__ int task_potrf_mini(const Params& P, const Cur& cm, int K, const Mini& mk, float* sm) {
   const int NB = P.NB, n = tdim(K, cm, NB);
   float* A = P.W + (cm.slot0 + slot_of(K, K, cm.NT)) * (long long)NB * NB;
-  uint64_t ph[3] = {0, 0, 0};  // time in the three phases (tracing only)
-  for (int p0 = 0; p0 < n; p0 += kBlk) {
-    const int pb = min(kBlk, n - p0);
-    uint64_t t = P.trace.buf ? globaltimer_ns() : 0;
-    if (p0 > 0)
-      for (int r0 = p0; r0 < n; r0 += kBlk)
-        op_gemm_nt<float>(A + r0, NB, A + p0, NB, A + r0 + (long long)p0 * NB, NB, min(kBlk, n - r0), pb, p0,
-                          r0 == p0, sm);
-    if (P.trace.buf) {
-      const uint64_t u = globaltimer_ns();
-      ph[0] += u - t;
-      t = u;
+  auto blk = [&](int i, int j) { return A + kBlk * i + (long long)kBlk * j * NB; };
+  auto bdim = [&](int i) { return min(kBlk, n - kBlk * i); };  // <= 0: past the ragged edge
+  const int dp = bdim(mk.p);
+  if (mk.kind == 0) {
+    if (dp <= 0) return 0;
+    const int info = op_potrf<float>(blk(mk.p, mk.p), NB, dp, sm);
+    if (info == 0 && threadIdx.x == 0) {  // condition estimate of the block from its factor's diagonal
+      float mn = 3.0e38f, mx = 0.f;
+      for (int i = 0; i < dp; ++i) {
+        const float d = __ldcg(blk(mk.p, mk.p) + i + (long long)i * NB);
+        mn = fminf(mn, d);
+        mx = fmaxf(mx, d);
+      }
+      const float est = (mx / mn) * (mx / mn);
+      atomicMax((int*)(P.cond_est + cm.id), __float_as_int(est));  // positive floats order like their bits
     }
-    const int info = op_potrf<float>(A + p0 + (long long)p0 * NB, NB, pb, sm);
-    if (info) return p0 + info;
-    if (P.trace.buf) {
-      const uint64_t u = globaltimer_ns();
-      ph[1] += u - t;
-      t = u;
-    }
-    for (int r0 = p0 + kBlk; r0 < n; r0 += kBlk)
-      op_trsm<float>(A + p0 + (long long)p0 * NB, NB, A + r0 + (long long)p0 * NB, NB, min(kBlk, n - r0), pb, sm);
-    if (P.trace.buf) ph[2] += globaltimer_ns() - t;
+    __syncthreads();
+    return info;
   }
-  if (P.trace.buf && threadIdx.x == 0)
-    for (int q = 0; q < 3; ++q) trace_record(P.trace, globaltimer_ns() - ph[q], 4 + q, K, 0, 0, 0);
-  // condition estimate of the diagonal tile from its factor's diagonal
-  if (threadIdx.x == 0) {
-    float mn = 3.0e38f, mx = 0.f;
-    for (int i = 0; i < n; ++i) {
-      const float d = __ldcg(A + i + (long long)i * NB);
-      mn = fminf(mn, d);
-      mx = fmaxf(mx, d);
-    }
-    const float est = (mx / mn) * (mx / mn);
-    atomicMax((int*)(P.cond_est + cm.id), __float_as_int(est));  // positive floats order like their bits
+  if (mk.kind == 1) {
+    const int di = bdim(mk.i);
+    if (di > 0 && dp > 0) op_trsm<float>(blk(mk.p, mk.p), NB, blk(mk.i, mk.p), NB, di, dp, sm);
+    return 0;
   }
-  __syncthreads();
+  const int di = bdim(mk.i), dj = bdim(mk.j);
+  if (di > 0 && dj > 0 && dp > 0)
+    op_gemm_nt<float>(blk(mk.i, mk.p), NB, blk(mk.j, mk.p), NB, blk(mk.i, mk.j), NB, di, dj, dp, mk.i == mk.j, sm);
   return 0;
 }
 
@@ -369,7 +383,7 @@ __global__ void __launch_bounds__(kThr, 1)
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ long long s_task, s_slot0;
-  __shared__ int s_go, s_info, s_N, s_NT, s_cnt0, s_id;
+  __shared__ int s_go, s_info, s_N, s_NT, s_cnt0, s_id, s_dcnt0, s_sub;
   __shared__ float s_colscale[kSubN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -403,7 +417,9 @@ __global__ void __launch_bounds__(kThr, 1)
         }
         const MixSeg sg = P.segs[lo];
         const MixMat mm = P.mats[sg.mat];
-        s_task = sg.local0 + (t - sg.start);
+        s_task = sg.task0 + (t - sg.start) / sg.mult;
+        s_sub = sg.sub0 + (int)((t - sg.start) % sg.mult);
+        s_dcnt0 = mm.dcnt0;
         s_slot0 = mm.slot0;
         s_N = mm.N;
         s_NT = mm.NT;
@@ -423,19 +439,38 @@ __global__ void __launch_bounds__(kThr, 1)
     cm.id = s_id;
     cm.cnt = P.cnt + s_cnt0;
     const int NT = cm.NT;
-    const TileKey tk = decode(t / P.slots, NT);
-    const int sub = (int)(t % P.slots);
-    const int nsub = tk.type == T_POTRF ? 1 : tk.type == T_TRSM ? P.sub_t : tk.type == T_SYRK ? P.sub_s : P.sub_g;
+    const TileKey tk = decode(t, NT);
+    const int sub = s_sub;
+    const int nsub =
+        tk.type == T_POTRF ? P.npot : tk.type == T_TRSM ? P.sub_t : tk.type == T_SYRK ? P.sub_s : P.sub_g;
     if (sub >= nsub) continue;  // unused slot of a task with fewer sub-tasks (uniform across the CTA)
+    Mini mk{0, 0, 0, 0};
+    int* dc = nullptr;  // the diagonal tile's block counters (POTRF mini-tasks)
+    if (tk.type == T_POTRF) {
+      mk = mini_decode(sub, P.nb);
+      dc = P.dcnt + s_dcnt0 + (long long)tk.a * P.nb * P.nb;
+    }
     int* target = nullptr;
+    int* target2 = nullptr;  // the tile counter, moved by the last mini-task of a POTRF
     if (threadIdx.x == 0) {
       bool ok = true;
       const int Sg = P.sub_g, St = P.sub_t, Ss = P.sub_s;
       int* cnt = cm.cnt;
       switch (tk.type) {
-        case T_POTRF:
+        case T_POTRF: {
+          const int nb = P.nb;
           ok = wait_geq(cnt + tri_index(tk.a, tk.a, NT), Ss * tk.a, P.st, P.timeout_ns);
+          if (mk.kind == 0)
+            ok = ok && wait_geq(dc + mk.p * nb + mk.p, mk.p, P.st, P.timeout_ns);
+          else if (mk.kind == 1)
+            ok = ok && wait_geq(dc + mk.p * nb + mk.p, mk.p + 1, P.st, P.timeout_ns) &&
+                 wait_geq(dc + mk.i * nb + mk.p, mk.p, P.st, P.timeout_ns);
+          else
+            ok = ok && wait_geq(dc + mk.i * nb + mk.p, mk.p + 1, P.st, P.timeout_ns) &&
+                 wait_geq(dc + mk.j * nb + mk.p, mk.p + 1, P.st, P.timeout_ns) &&
+                 wait_geq(dc + mk.i * nb + mk.j, mk.p, P.st, P.timeout_ns);
           break;
+        }
         case T_TRSM:
           ok = wait_geq(cnt + tri_index(tk.b, tk.b, NT), Ss * tk.b + 1, P.st, P.timeout_ns) &&
                wait_geq(cnt + tri_index(tk.a, tk.b, NT), Sg * tk.b, P.st, P.timeout_ns);
@@ -458,8 +493,10 @@ __global__ void __launch_bounds__(kThr, 1)
       __syncthreads();
       if (threadIdx.x == 0) {
         int* c = cm.cnt;
-        if (tk.type == T_POTRF) signal_done(c + tri_index(tk.a, tk.a, NT));
-        else if (tk.type == T_TRSM) signal_done(c + tri_index(tk.a, tk.b, NT));
+        if (tk.type == T_POTRF) {
+          signal_done(dc + mk.i * P.nb + mk.j);
+          if (mk.kind == 0 && mk.p == P.nb - 1) signal_done(c + tri_index(tk.a, tk.a, NT));
+        } else if (tk.type == T_TRSM) signal_done(c + tri_index(tk.a, tk.b, NT));
         else if (tk.type == T_SYRK) signal_done(c + tri_index(tk.b, tk.b, NT));
         else signal_done(c + tri_index(tk.a, tk.b, NT));
       }
@@ -468,21 +505,23 @@ __global__ void __launch_bounds__(kThr, 1)
     const uint64_t t_start = P.trace.buf ? globaltimer_ns() : 0;
 
     if (tk.type == T_POTRF) {
-      const int info = task_potrf(P, cm, tk.a, (float*)smem);
+      const int info = task_potrf_mini(P, cm, tk.a, mk, (float*)smem);
       if (threadIdx.x == 0) s_info = info;
       __syncthreads();
       if (s_info) {
+        const int piv = tk.a * NB + kBlk * mk.p + s_info;  // 1-based row of the matrix
         if (P.nmats == 1) {  // one matrix: stop the whole launch
           if (threadIdx.x == 0) {
-            atomicCAS(P.minfo + cm.id, 0, tk.a * NB + s_info);
-            atomicCAS(&P.st->status, 0, tk.a * NB + s_info);
+            atomicCAS(P.minfo + cm.id, 0, piv);
+            atomicCAS(&P.st->status, 0, piv);
             atomicExch(&P.st->abort, 1);
           }
           break;
         }
-        if (threadIdx.x == 0) atomicCAS(P.minfo + cm.id, 0, tk.a * NB + s_info);  // others go on
+        if (threadIdx.x == 0) atomicCAS(P.minfo + cm.id, 0, piv);  // others go on
       }
-      target = cm.cnt + tri_index(tk.a, tk.a, NT);
+      target = dc + mk.i * P.nb + mk.j;
+      if (mk.kind == 0 && mk.p == P.nb - 1) target2 = cm.cnt + tri_index(tk.a, tk.a, NT);
     } else if (tk.type == T_TRSM) {
       task_trsm(P, cm, tk.a, tk.b, sub, (float*)smem);
       target = cm.cnt + tri_index(tk.a, tk.b, NT);
@@ -585,6 +624,7 @@ __global__ void __launch_bounds__(kThr, 1)
     __syncthreads();
     if (threadIdx.x == 0 && target) {
       signal_done(target);
+      if (target2) signal_done(target2);
       trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, sub);
     }
   }
@@ -613,24 +653,34 @@ __global__ void shift_diag_kernel(float* W, int N, int NB, int NT, float shift) 
 // workspace layout for a batch (one matrix is the batch of one): run state, completion counters,
 // per-matrix condition estimates and info, the matrix table, row exponents, low-precision copies
 struct Ws {
-  size_t state, cnt, cond, minfo, mats, segs, rowexp, lb, total;
-  long long slots, cnts, nsegs;
+  size_t state, cnt, dcnt, cond, minfo, mats, segs, rowexp, lb, total;
+  long long slots, cnts, nsegs, dcnts;
 };
 inline size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+int npot_of(int NB) {  // mini-tasks of one POTRF
+  const int nb = NB / kBlk;
+  int c = 0;
+  for (int p = 0; p < nb; ++p) c += panel_minis(nb, p);
+  return c;
+}
 inline Ws layout_batch(int batch, const int* n, int NB) {
-  long long slots = 0, nsegs = 0;
+  long long slots = 0, nsegs = 0, dcnts = 0;
+  const long long nb = NB / kBlk;
   for (int k = 0; k < batch; ++k) {
     const long long nt = (n[k] + NB - 1) / NB;
     slots += nt * (nt + 1) / 2;
-    nsegs += 4 * nt;  // queue segments: at most four task groups per phase, nt phases
+    nsegs += (4 + npot_of(NB)) * nt;  // queue segments: per phase, three groups + POTRF mini-tasks
+    dcnts += nt * nb * nb;
   }
   Ws w;
   w.nsegs = nsegs;
   w.slots = slots;
   w.cnts = slots;  // one counter per tile
+  w.dcnts = dcnts;
   w.state = 0;
   w.cnt = sizeof(DagState);
-  w.cond = up(w.cnt + (size_t)w.cnts * sizeof(int), 256);
+  w.dcnt = up(w.cnt + (size_t)w.cnts * sizeof(int), 256);
+  w.cond = up(w.dcnt + (size_t)w.dcnts * sizeof(int), 256);
   w.minfo = up(w.cond + (size_t)batch * sizeof(float), 256);
   w.mats = up(w.minfo + (size_t)batch * sizeof(int), 256);
   w.segs = up(w.mats + (size_t)batch * sizeof(MixMat), 256);
@@ -683,13 +733,18 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
   const int sub_g = (NB / kSubM) * (NB / kSubN);
   const int sub_t = NB / kTrsmRows;
   const int nslot = std::max(std::max(sub_g, sub_t), sub_syrk(NB));
+  const int nb = NB / kBlk;
+  int npot = 0;  // mini-tasks of one POTRF
+  for (int p = 0; p < nb; ++p) npot += panel_minis(nb, p);
   // matrix table: slot / counter offsets in batch order, queue order largest first
-  std::vector<long long> slot0(batch);
-  long long acc = 0;
+  std::vector<long long> slot0(batch), dcnt0(batch);
+  long long acc = 0, dacc = 0;
   for (int k = 0; k < batch; ++k) {
     slot0[k] = acc;
+    dcnt0[k] = dacc;
     const long long nt = (n[k] + NB - 1) / NB;
     acc += nt * (nt + 1) / 2;
+    dacc += nt * nb * nb;
   }
   std::vector<int> order;
   for (int k = 0; k < batch; ++k)
@@ -705,12 +760,15 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
     mats[q].NT = nt;
     mats[q].cnt0 = (int)slot0[k];
     mats[q].id = k;
+    mats[q].dcnt0 = (int)dcnt0[k];
+    mats[q].pad = 0;
     maxNT = std::max(maxNT, nt);
   }
   // queue: phase by phase; within a phase, group by group (1: the updates of the next panel's
   // column, 2: its POTRF, 3: its TRSMs, 4: the trailing updates), within a group the matrices
-  // largest first. The CTAs then find whole groups of independent tasks of many matrices instead
-  // of one matrix's dependent chain.
+  // largest first; the POTRF group goes mini-task by mini-task across the matrices. The CTAs then
+  // find whole groups of independent tasks of many matrices instead of one matrix's dependent
+  // chain.
   std::vector<MixSeg> segs;
   long long task0 = 0;
   auto group_range = [&](int nt, int p, int g, long long& first, long long& last) {
@@ -726,16 +784,27 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
     last = base + hi[g];
   };
   for (int p = 0; p < maxNT; ++p)
-    for (int g = 1; g <= 4; ++g)
+    for (int g = 1; g <= 4; ++g) {
+      if (g == 2)  // the single POTRF of this phase, one slot per mini-task
+        for (int u = 0; u < npot; ++u)
+          for (size_t q = 0; q < mats.size(); ++q) {
+            if (mats[q].NT <= p) continue;
+            long long first, last;
+            group_range(mats[q].NT, p, 2, first, last);
+            segs.push_back(MixSeg{task0, first, (int)q, 1, u, 0});
+            task0 += 1;
+          }
       for (size_t q = 0; q < mats.size(); ++q) {
         const int nt = mats[q].NT;
         if (nt <= p) continue;
         long long first, last;
         group_range(nt, p, g, first, last);
         if (last <= first) continue;
-        segs.push_back(MixSeg{task0, first * nslot, (int)q, 0});
+        if (g == 2) continue;  // (queued above, mini-task by mini-task)
+        segs.push_back(MixSeg{task0, first, (int)q, nslot, 0, 0});
         task0 += (last - first) * nslot;
       }
+    }
   if ((long long)segs.size() > w.nsegs) return GBX_ERR_WORKSPACE;  // the table must fit its reserved space
   char* base = (char*)work;
   // state, counters, condition estimates and info are cleared for every matrix; the copies and
@@ -770,7 +839,9 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
   P.f16 = prec == 1;
   P.sub_g = sub_g;
   P.sub_t = sub_t;
-  P.slots = nslot;
+  P.nb = nb;
+  P.npot = npot;
+  P.dcnt = (int*)(base + w.dcnt);
   P.sub_s = sub_syrk(NB);
   P.ntasks = task0;
   P.mats = (const MixMat*)(base + w.mats);
