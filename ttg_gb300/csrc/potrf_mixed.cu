@@ -570,17 +570,25 @@ __global__ void __launch_bounds__(kThr, 1)
         }
         umma_commit(smem_u32(&done_bar));
       } else if (warp >= 4) {
-        const int q = warp & 3;
-        const int r = r0 + q * 32 + lane;  // row of C handled by this thread
-        const int mrows = tdim(M, cm, NB), ncols = tdim(Nn, cm, NB);
-        float* C = P.W + sC * (long long)NB * NB;
         // while the MMAs run: column scales of this sub-tile into shared memory, C lines into L2
+        const int ncols = tdim(Nn, cm, NB), mrows = tdim(M, cm, NB);
+        const float* C = P.W + sC * (long long)NB * NB;
+        const int q = warp & 3;
         for (int c = (warp - 4) * 32 + lane; c < kSubN; c += 128)
           s_colscale[c] = (c0 + c < ncols) ? pow2f(__ldcg(P.rowexp + sB * NB + c0 + c)) : 0.f;
         if (r0 + q * 32 < mrows)
           for (int c = lane; c < kSubN && c0 + c < ncols; c += 32)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(C + (r0 + q * 32) + (long long)(c0 + c) * NB));
-        asm volatile("bar.sync 1, 128;" ::: "memory");  // the four epilogue warps
+      }
+      __syncwarp();
+      __syncthreads();  // column scales ready; warps 0 and 1 have issued their last TMA / MMA
+      {
+        // epilogue on all eight warps: warp w reads TMEM lanes 32 (w % 4) .. (its rows) for one half
+        // of the 256 columns; C := C - (A B^T) scaled by the rows' and columns' powers of two
+        const int q = warp & 3, h = warp >> 2;
+        const int r = r0 + q * 32 + lane;  // row of C handled by this thread
+        const int mrows = tdim(M, cm, NB), ncols = tdim(Nn, cm, NB);
+        float* C = P.W + sC * (long long)NB * NB;
         const float rscale = (r < mrows) ? pow2f(__ldcg(P.rowexp + sA * NB + r)) : 0.f;
         const bool row_ok = r < mrows;
         const bool syrk = tk.type == T_SYRK;
@@ -594,11 +602,12 @@ __global__ void __launch_bounds__(kThr, 1)
               dst[j] = (row_ok && col < ncols) ? __ldcg(C + r + (long long)col * NB) : 0.f;
             }
           };
-          load16(cur, 0);
-          for (int c = 0; c < kSubN; c += 16) {
+          const int cb = h * (kSubN / 2), ce = cb + kSubN / 2;
+          load16(cur, cb);
+          for (int c = cb; c < ce; c += 16) {
             uint32_t v[16];
             tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
-            if (c + 16 < kSubN) load16(nxt, c + 16);  // next chunk's loads are in flight during this chunk
+            if (c + 16 < ce) load16(nxt, c + 16);  // next chunk's loads are in flight during this chunk
             tmem_ld_wait();
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
@@ -610,8 +619,6 @@ __global__ void __launch_bounds__(kThr, 1)
             for (int j = 0; j < 16; ++j) cur[j] = nxt[j];
           }
         }
-      } else {
-        // warps 2 and 3 (and the idle lanes of warps 0 and 1) skip the tensor part
       }
       if (warp == 0 && lane != 0) prod_it += nkb;
       if (warp != 0) prod_it += nkb;
