@@ -382,8 +382,8 @@ class Batch:
         return out
 
 
-TASK_NAMES = ["POTRF", "TRSM", "SYRK", "GEMM", "potrf:gemm-updates", "potrf:block-potrf", "potrf:block-trsm",
-              "?", "?", "?", "?", "?", "?", "?", "?", "?"]
+TASK_NAMES = ["POTRF", "TRSM", "SYRK", "GEMM"] + ["?"] * 12  # record type = key >> 60
+# (the mixed executor's POTRF records are its 128-block mini-tasks: sub-task = mini-task index)
 
 
 def trace_records(buf):
