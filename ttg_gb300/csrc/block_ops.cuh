@@ -390,6 +390,7 @@ __device__ void fwd_solve(const T* L, int n, int ld, T* xs) {  // L y = x
     __syncthreads();
     for (int i = p0 + pw + tid; i < n; i += blockDim.x) {
       T s = T(0);
+#pragma unroll 8
       for (int c = 0; c < pw; ++c) s += L[i + (long long)(p0 + c) * ld] * xs[p0 + c];
       xs[i] -= s;
     }

@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     }
     __syncthreads();
     if (threadIdx.x == 0) {
+      trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);  // end stamp before any waiter can start
       signal_done(target);
       if (P.col_done && (tk.type == T_POTRF || tk.type == T_TRSM)) {  // block (a, b) of L is final
         const int g = (tk.type == T_POTRF ? tk.a : tk.b) / P.group_blocks;
@@ -204,7 +205,6 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
           P.host_flag[g] = 1;
         }
       }
-      trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);
     }
   }
   if (threadIdx.x == 0) release_columns(P);
@@ -248,67 +248,120 @@ __global__ void set_head_kernel(DagState* st, unsigned long long head) {
 }
 
 // ---- tiled solve: forward (L y = b) and backward (L^T x = y) sweeps over b x b blocks ---------
-// diag solve of one block for all nrhs columns, panel-blocked (fwd_solve / bwd_solve)
-__global__ void __launch_bounds__(kThreads) trsv_diag_kernel(BlockView V, int K, double* X, int ldx, int nrhs,
-                                                             int trans) {
-  __shared__ double xs[kBlk];
-  const int kb = V.dim(K);
-  const double* L = V.ptr(K, K);
-  for (int r = 0; r < nrhs; ++r) {
-    double* x = X + (long long)r * ldx + (long long)K * V.b;
-    for (int i = threadIdx.x; i < kb; i += blockDim.x) xs[i] = x[i];
-    __syncthreads();
-    if (!trans) fwd_solve<double>(L, kb, V.ld, xs);
-    else bwd_solve<double>(L, kb, V.ld, xs);
-    for (int i = threadIdx.x; i < kb; i += blockDim.x) x[i] = xs[i];
-    __syncthreads();
+// Each sweep is one persistent launch over an in-order task sequence, step s holding NTb - s tasks:
+//   forward,  K = s:          DIAG(K): wait until the K updates of block row K are in, then
+//                             y_K = L_KK^{-1} x_K by substitution; flag K
+//                             UPD(K+j, K): wait for flag K; x_{K+j} -= L_{K+j,K} y_K (FP64 atomics);
+//                             count one for row K+j
+//   backward, K = NTb-1-s:    DIAG(K): wait until the NTb-1-K updates of row K are in, then
+//                             z_K = L_KK^{-T} y_K; flag K
+//                             UPD(K, K-j): wait for flag K; y_{K-j} -= L_{K,K-j}^T z_K; count row K-j
+// Every task waits only on earlier tasks, so CTAs taking tasks in order cannot deadlock; waits are
+// bounded (status GBX_ERR_TIMEOUT). Vectors other CTAs update atomically are read through L2.
+__device__ __forceinline__ void solve_decode(long long t, int NTb, int& s, int& j) {
+  int lo = 0, hi = NTb - 1;  // largest s with start(s) = s NTb - s (s - 1) / 2 <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((long long)mid * NTb - (long long)mid * (mid - 1) / 2 <= t) lo = mid;
+    else hi = mid - 1;
   }
+  s = lo;
+  j = (int)(t - ((long long)lo * NTb - (long long)lo * (lo - 1) / 2));
 }
 
-// forward update: x_M -= L_MK x_K for every M > K (one CTA per block row M)
-// backward update: x_J -= L_KJ^T x_K for every J < K (one CTA per block column J)
-__global__ void __launch_bounds__(kThreads) trsv_update_kernel(BlockView V, int K, double* X, int ldx, int nrhs,
-                                                               int trans) {
+template <int DIR>
+__global__ void __launch_bounds__(kThreads) solve_sweep_kernel(BlockView V, int NTb, double* X, int ldx, int nrhs,
+                                                               DagState* st, int* cnt, int* flag,
+                                                               uint64_t timeout_ns) {
   __shared__ double xk[kBlk];
   __shared__ double part[kThreads];
-  const int kb = V.dim(K);
-  if (!trans) {
-    const int M = K + 1 + blockIdx.x;
-    const int mb = V.dim(M);
-    const double* L = V.ptr(M, K);
-    for (int r = 0; r < nrhs; ++r) {
-      const double* xsrc = X + (long long)r * ldx + (long long)K * V.b;
-      for (int i = threadIdx.x; i < kb; i += blockDim.x) xk[i] = xsrc[i];
-      __syncthreads();
-      // rows split over 2 halves of the CTA along k
-      const int row = threadIdx.x & (kBlk - 1), half = threadIdx.x >> 7;
-      double s = 0.0;
-      if (row < mb)
-        for (int c = half; c < kb; c += 2) s = fma(L[row + (long long)c * V.ld], xk[c], s);
-      part[threadIdx.x] = s;
-      __syncthreads();
-      if (half == 0 && row < mb) X[(long long)r * ldx + (long long)M * V.b + row] -= part[row] + part[row + kBlk];
-      __syncthreads();
+  __shared__ long long s_t;
+  __shared__ int s_ok;
+  const long long ntasks = (long long)NTb * (NTb + 1) / 2;
+  const int tid = threadIdx.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) {
+      long long t = -1;
+      if (!ld_volatile(&st->abort)) t = (long long)atomicAdd(&st->head, 1ULL);
+      s_t = (t >= 0 && t < ntasks) ? t : -1;
     }
-  } else {
-    const int J = blockIdx.x;  // J < K
-    const int jb = V.dim(J);
-    const double* L = V.ptr(K, J);  // kb x jb block, we need L^T
-    for (int r = 0; r < nrhs; ++r) {
-      const double* xsrc = X + (long long)r * ldx + (long long)K * V.b;
-      for (int i = threadIdx.x; i < kb; i += blockDim.x) xk[i] = xsrc[i];
-      __syncthreads();
-      // output index j (column of L_KJ): dot of column j with xk; 2 threads per column? use warps
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int j = warp; j < jb; j += kThreads / 32) {
-        double s = 0.0;
-        for (int i = lane; i < kb; i += 32) s = fma(L[i + (long long)j * V.ld], xk[i], s);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) X[(long long)r * ldx + (long long)J * V.b + j] -= s;
+    __syncthreads();
+    if (s_t < 0) break;
+    int sidx, j;
+    solve_decode(s_t, NTb, sidx, j);
+    const int K = DIR == 0 ? sidx : NTb - 1 - sidx;
+    const int O = DIR == 0 ? K + j : K - j;  // the other block of an update task
+    if (tid == 0) {
+      s_ok = j == 0 ? wait_geq(cnt + K, DIR == 0 ? K : NTb - 1 - K, st, timeout_ns)
+                    : wait_geq(flag + K, 1, st, timeout_ns);
+    }
+    __syncthreads();
+    if (!s_ok) break;
+    const int kb = V.dim(K);
+    if (j == 0) {  // substitution in the diagonal block, one right-hand side at a time
+      const double* L = V.ptr(K, K);
+      for (int r = 0; r < nrhs; ++r) {
+        double* x = X + (long long)r * ldx + (long long)K * V.b;
+        for (int i = tid; i < kb; i += blockDim.x) xk[i] = __ldcg(x + i);
+        __syncthreads();
+        if (DIR == 0) fwd_solve<double>(L, kb, V.ld, xk);
+        else bwd_solve<double>(L, kb, V.ld, xk);
+        for (int i = tid; i < kb; i += blockDim.x) x[i] = xk[i];
+        __syncthreads();
       }
-      __syncthreads();
+    } else if (DIR == 0) {  // x_O -= L_OK y_K: rows split over two halves of the CTA along k
+      const int ob = V.dim(O);
+      const double* L = V.ptr(O, K);
+      for (int r = 0; r < nrhs; ++r) {
+        const double* y = X + (long long)r * ldx + (long long)K * V.b;
+        for (int i = tid; i < kb; i += blockDim.x) xk[i] = __ldcg(y + i);
+        __syncthreads();
+        const int row = tid & (kBlk - 1), half = tid >> 7;
+        double a = 0.0;
+        if (row < ob) {
+          double a2 = 0.0;  // two chains, eight loads in flight per thread
+          int c = half;
+          for (; c + 14 < kb; c += 16) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = __ldcg(L + row + (long long)(c + 2 * u) * V.ld);
+#pragma unroll
+            for (int u = 0; u < 8; u += 2) {
+              a = fma(v[u], xk[c + 2 * u], a);
+              a2 = fma(v[u + 1], xk[c + 2 * u + 2], a2);
+            }
+          }
+          for (; c < kb; c += 2) a = fma(__ldcg(L + row + (long long)c * V.ld), xk[c], a);
+          a += a2;
+        }
+        part[tid] = a;
+        __syncthreads();
+        if (half == 0 && row < ob) atomicAdd(X + (long long)r * ldx + (long long)O * V.b + row, -(part[row] + part[row + kBlk]));
+        __syncthreads();
+      }
+    } else {  // y_O -= L_KO^T z_K: warp per column of L_KO
+      const int ob = V.dim(O);
+      const double* L = V.ptr(K, O);
+      const int warp = tid >> 5, lane = tid & 31;
+      for (int r = 0; r < nrhs; ++r) {
+        const double* z = X + (long long)r * ldx + (long long)K * V.b;
+        for (int i = tid; i < kb; i += blockDim.x) xk[i] = __ldcg(z + i);
+        __syncthreads();
+        for (int c = warp; c < ob; c += kThreads / 32) {
+          double a = 0.0;
+#pragma unroll 4
+          for (int i = lane; i < kb; i += 32) a = fma(__ldcg(L + i + (long long)c * V.ld), xk[i], a);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+          if (lane == 0) atomicAdd(X + (long long)r * ldx + (long long)O * V.b + c, -a);
+        }
+        __syncthreads();
+      }
     }
+    __threadfence();  // this thread's results are visible before the completion is
+    __syncthreads();
+    if (tid == 0) signal_done(j == 0 ? flag + K : cnt + O);
   }
 }
 
@@ -422,10 +475,19 @@ __global__ void plgsy_tile_kernel(double bump, int m, int n, double* A, int lda,
 
 // ---- host side --------------------------------------------------------------------------------
 struct DevInfo {
+  int dev = 0;
   int sms = 0;
   int dag_blocks_per_sm = 0;
   bool attrs_set = false;
 };
+// run state of the solve sweeps, per device (gbx_dpotrs_tiled has no workspace argument)
+struct SolveScratch {
+  void* buf = nullptr;
+  size_t bytes = 0;
+  cudaEvent_t ev = nullptr;  // recorded after each use: the next call's stream waits on it
+};
+std::mutex g_solve_mtx;
+SolveScratch g_solve[32];
 std::mutex g_mtx;
 std::vector<DevInfo> g_dev;
 TraceBuf g_trace{nullptr, 0};
@@ -441,6 +503,8 @@ int device_info(DevInfo& out) {
   std::lock_guard<std::mutex> lk(g_mtx);
   if ((int)g_dev.size() <= dev) g_dev.resize(dev + 1);
   DevInfo& d = g_dev[dev];
+  d.dev = dev;
+  if (dev >= 32) return GBX_ERR_CUDA;
   if (!d.attrs_set) {
     if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
     if (cudaFuncSetAttribute(potrf_dag_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -652,14 +716,31 @@ int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, in
   cudaStream_t s = (cudaStream_t)stream;
   const BlockView V = tiled_view(N, NB, const_cast<double*>(tiles));
   const int NTb = (N + V.b - 1) / V.b;
-  for (int K = 0; K < NTb; ++K) {
-    trsv_diag_kernel<<<1, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 0);
-    if (K + 1 < NTb) trsv_update_kernel<<<NTb - K - 1, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 0);
+  DevInfo di;
+  if (int e = device_info(di)) return e;
+  // run state and counters of the two sweeps: a per-device buffer, serialised across calls (the
+  // previous call's launches are done before this one clears it)
+  std::lock_guard<std::mutex> lk(g_solve_mtx);
+  SolveScratch& sc = g_solve[di.dev];
+  const size_t need = 2 * sizeof(DagState) + (size_t)4 * NTb * sizeof(int);
+  if (!sc.ev && cudaEventCreateWithFlags(&sc.ev, cudaEventDisableTiming) != cudaSuccess) return GBX_ERR_CUDA;
+  if (sc.bytes < need) {
+    if (sc.buf && (cudaEventSynchronize(sc.ev) != cudaSuccess || cudaFree(sc.buf) != cudaSuccess)) return GBX_ERR_CUDA;
+    sc.buf = nullptr;
+    sc.bytes = 0;
+    if (cudaMalloc(&sc.buf, need) != cudaSuccess) return GBX_ERR_CUDA;
+    sc.bytes = need;
   }
-  for (int K = NTb - 1; K >= 0; --K) {
-    trsv_diag_kernel<<<1, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 1);
-    if (K > 0) trsv_update_kernel<<<K, kThreads, 0, s>>>(V, K, B, ldb, nrhs, 1);
-  }
+  if (cudaStreamWaitEvent(s, sc.ev, 0) != cudaSuccess) return GBX_ERR_CUDA;
+  DagState* st = (DagState*)sc.buf;
+  int* c = (int*)((char*)sc.buf + 2 * sizeof(DagState));
+  if (cudaMemsetAsync(sc.buf, 0, need, s) != cudaSuccess) return GBX_ERR_CUDA;
+  const long long ntasks = (long long)NTb * (NTb + 1) / 2;
+  const int grid = (int)std::max(1LL, std::min<long long>(2LL * di.sms, ntasks));
+  const uint64_t tmo = gbx_get_wait_timeout_ns();
+  solve_sweep_kernel<0><<<grid, kThreads, 0, s>>>(V, NTb, B, ldb, nrhs, st, c, c + NTb, tmo);
+  solve_sweep_kernel<1><<<grid, kThreads, 0, s>>>(V, NTb, B, ldb, nrhs, st + 1, c + 2 * NTb, c + 3 * NTb, tmo);
+  if (cudaEventRecord(sc.ev, s) != cudaSuccess) return GBX_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 

@@ -630,9 +630,9 @@ __global__ void __launch_bounds__(kThr, 1)
     }
     __syncthreads();
     if (threadIdx.x == 0 && target) {
+      trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, sub);  // end stamp before any waiter can start
       signal_done(target);
       if (target2) signal_done(target2);
-      trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, sub);
     }
   }
   tc_fence_before();
