@@ -120,6 +120,14 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
   __syncthreads();
 }
 
+// FP32 reciprocal without a branch: the hardware approximation refined by one Newton-Raphson step,
+// r <- r + r (1 - d r) (within an ulp or so of 1/d). The IEEE division carries a slow-path branch
+// that splits an unrolled solve into many scheduling regions and keeps its loads from being hoisted.
+__device__ __forceinline__ float rcp_nr(float d) {
+  const float r = __fdividef(1.f, d);
+  return fmaf(r, fmaf(-d, r, 1.f), r);
+}
+
 // ------------------------------------------------------------------------------------------------
 // block POTRF (lower, n <= 128) in shared memory, blocked by 32 columns:
 //   1. warp 0 factors the 32 x 32 diagonal block (warp-synchronous, no CTA barrier per column)
@@ -144,6 +152,24 @@ __device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, in
       if (c & 1) s0 = fma(-x[c - 1], Lp[c + ldp * (c - 1)], s0);
       x[c] = (s0 + s1) * (T(1) / Lp[c + ldp * c]);  // the reciprocal does not depend on x: off the chain
     }
+  }
+}
+
+// The same solve column by column for a full FP32 panel: once x(c) is final it is subtracted from
+// the later entries, so column c of Lp is read with 16-byte loads that do not depend on x, and the
+// chain per column is one multiply and one FMA. Lp is 16-byte aligned and ldp a multiple of 4. The
+// warp sync every 8 columns bounds how far ahead the compiler hoists the loads (register pressure
+// inside the persistent mixed kernel). Called by whole warps.
+__device__ __forceinline__ void col_solve32(float (&x)[32], const float* Lp, int ldp) {
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    float l[32];
+#pragma unroll
+    for (int q = c / 4; q < 8; ++q) lds4(Lp + c * ldp + 4 * q, *reinterpret_cast<float(*)[4]>(&l[4 * q]));
+    x[c] *= rcp_nr(l[c]);
+#pragma unroll
+    for (int r = c + 1; r < 32; ++r) x[r] = fmaf(-l[r], x[c], x[r]);
+    if ((c + 1) % 8 == 0 && c < 31) __syncwarp();  // keeps the loads hoisted at most 8 columns ahead
   }
 }
 

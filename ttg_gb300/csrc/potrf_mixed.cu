@@ -222,8 +222,9 @@ __device__ int task_potrf_mini(const Params& P, const Cur& cm, int K, const Mini
 // TRSM(M, K) sub-task rb: rows 64 rb .. 64 rb + 63 of W(M,K) := W(M,K) L_KK^{-T}, then their scaled
 // low-precision row-major copy. The 64 x NB block stays in shared memory for the whole solve:
 // per 32-column panel, each of 64 threads solves its row in registers against the panel's
-// triangle, then all 256 threads apply the panel to the columns right of it (right-looking rank-32
-// update, 4 x 4 register micro-tiles with 16-byte shared loads).
+// triangle (column-wise substitution), then all 256 threads apply the panel to the columns right of
+// it (right-looking rank-32 update, 4 x 8 register micro-tiles with 16-byte shared loads). The next
+// panel of L is loaded into registers while the current one is solved and applied.
 // smem: block [NB][64] + L panel [32][512] = 192 KB for NB = 512
 __device__ void task_trsm(const Params& P, const Cur& cm, int M, int K, int rb, float* sm) {
   const int NB = P.NB, r0 = rb * kTrsmRows, mrows = tdim(M, cm, NB), n = tdim(K, cm, NB);
@@ -254,37 +255,43 @@ __device__ void task_trsm(const Params& P, const Cur& cm, int M, int K, int rb, 
       if (f < n * (kTrsmRows / 4)) *(float4*)(Bs + 4 * f) = v[u];
     }
   }
-  const int tr = tid & 15, tc = tid >> 4;  // update micro-tile: rows 4tr.., columns 4tc.. of a 64-column chunk
+  const int tr = tid & 15, tc = tid >> 4;  // update micro-tile: rows 4tr.., columns 8tc.. of a 128-column chunk
+  // the panel's columns of L, rows p0.. : sixteen 16-byte loads per thread, issued one panel ahead
+  // so that they are in flight during the previous panel's update (not during the solve, which
+  // needs the registers); rows past the edge stay inside the tile slot and are never read back
+  float4 pre[16];
+  auto load_panel = [&](int q0) {
+    const int qw = min(32, n - q0), qspan = n - q0;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int f = u * kThr + tid, c = f >> 7, ii = (f & 127) * 4;
+      if (c < qw && ii < qspan) pre[u] = __ldcg((const float4*)(L + (q0 + ii) + (long long)(q0 + c) * NB));
+    }
+  };
+  load_panel(0);
   for (int p0 = 0; p0 < n; p0 += 32) {
     const int pw = min(32, n - p0), span = n - p0;
     __syncthreads();  // the previous panel's update is complete
-    // the panel's columns of L, rows p0.. : 16-byte loads, eight in flight per thread (rows past
-    // the edge stay inside the tile slot and are never read back)
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      float4 v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int f = (h * 8 + u) * kThr + tid, c = f >> 7, ii = (f & 127) * 4;
-        if (c < pw && ii < span) v[u] = __ldcg((const float4*)(L + (p0 + ii) + (long long)(p0 + c) * NB));
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int f = (h * 8 + u) * kThr + tid, c = f >> 7, ii = (f & 127) * 4;
-        if (c < pw && ii < span) *(float4*)(Ls + c * kMaxNB + ii) = v[u];
-      }
+    for (int u = 0; u < 16; ++u) {
+      const int f = u * kThr + tid, c = f >> 7, ii = (f & 127) * 4;
+      if (c < pw && ii < span) *(float4*)(Ls + c * kMaxNB + ii) = pre[u];
     }
     __syncthreads();
     if (tid < kTrsmRows) {
       float x[32];
 #pragma unroll
       for (int c = 0; c < 32; ++c) x[c] = c < pw ? Bs[(p0 + c) * kTrsmRows + tid] : 0.f;
-      row_solve32<float>(x, Ls, kMaxNB, pw);
+      if (pw == 32)
+        col_solve32(x, Ls, kMaxNB);
+      else
+        row_solve32<float>(x, Ls, kMaxNB, pw);
 #pragma unroll
       for (int c = 0; c < 32; ++c)
         if (c < pw) Bs[(p0 + c) * kTrsmRows + tid] = x[c];
     }
     __syncthreads();
+    if (p0 + 32 < n) load_panel(p0 + 32);  // in flight during this panel's update
     // Bs(:, p0+jj) -= Bs(:, p0:p0+pw) * L(p0+jj, p0:p0+pw)^T for jj in [pw, span), chunks of 128
     // columns; a thread owns rows 4tr..4tr+3 x columns jj..jj+7 (three 16-byte loads per 32 FMAs)
     for (int j0 = pw; j0 < span; j0 += 128) {
