@@ -241,6 +241,11 @@ int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, in
                             int prec, double tol, int maxiter, float* W, void* work, size_t work_bytes,
                             gbx_refine_info* info, void* stream);
 
+/* hi[i] + lo[i] = a[i] for n FP64 values: hi = fl32(a), lo = fl32(a - hi), rounded to nearest even
+ * (the double-float split of the refinement's residual products, computed on the bit pattern;
+ * bitwise equal to the FP64 conversions). Asynchronous on `stream`. No counterpart in the reference. */
+int gbx_split_f64(const double* a, float* hi, float* lo, long long n, void* stream);
+
 /* Inverse of the SPD matrix from its factor, in place (replaces the reference's host-only POTRI
  * chain, examples/potrf/potri.h:18-29: TRTRI of the lower factor, trtri_L.h, then LAUUM,
  * lauum.h): on entry the lower tiles hold L from gbx_dpotrf_tiled, on exit the lower triangle of

@@ -114,7 +114,8 @@ def test_dposv_mixed_batched_uneven(gbx, cuda, prec):
     NB, nrhs = 256, 2
     sizes = np.array([700, 256, 1300, 1024, 90, 513])
     A, B = workloads.householder_batch(sizes, NB, 2, 1e4, 7, cuda, nrhs=nrhs)
-    X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300)
+    Wd = torch.empty(A.numel(), dtype=torch.float32, device=cuda)
+    X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300, W=Wd)
     assert st == 0, infos
     Xn, Bn = X.cpu().numpy(), B.cpu().numpy()
     off = 0
@@ -125,6 +126,8 @@ def test_dposv_mixed_batched_uneven(gbx, cuda, prec):
         Bk = Bn[off:off + n * nrhs].reshape(nrhs, n)
         off += n * nrhs
         assert infos[k]["backward_error"] <= 1e-14, (k, infos[k])
+        anorm = np.abs(Ad).sum(1).max()  # ||A||_inf from the single pass over A (FP32 partial sums)
+        assert abs(infos[k]["anorm"] - anorm) <= 1e-5 * anorm, (k, infos[k]["anorm"], anorm)
         for j in range(nrhs):
             r = Bk[j] - Ad @ Xk[j]
             be = np.abs(r).max() / (np.abs(Ad).sum(1).max() * np.abs(Xk[j]).max() + np.abs(Bk[j]).max())
@@ -157,6 +160,36 @@ def test_dposv_mixed_batched_uneven(gbx, cuda, prec):
         Lb = oracle.tiles_to_lower(Wk.double().cpu().numpy(), n, NB)
         L1 = oracle.tiles_to_lower(W1.double().cpu().numpy(), n, NB)
         assert np.array_equal(Lb, L1), k
+        # the solver's factor (W converted by its single pass over A) is the same factor
+        Ld = oracle.tiles_to_lower(Wd[o:o + W1.numel()].double().cpu().numpy(), n, NB)
+        assert np.array_equal(Ld, L1), k
+
+
+def test_split_f64_bitwise(gbx, cuda):
+    """The integer-arithmetic split hi + lo = a equals the FP64 conversions bit for bit:
+    hi = fl32(a), lo = fl32(a - hi), over random exponents, rounding ties and special values."""
+    import torch
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    a = rng.standard_normal(n) * np.exp2(rng.integers(-160, 160, n).astype(np.float64))
+    # halfway cases of the hi rounding (low 29 mantissa bits = 2^28, odd and even kept bit)
+    bits = a[:4096].view(np.uint64)
+    bits = (bits & ~np.uint64((1 << 29) - 1)) | np.uint64(1 << 28)
+    a[:4096] = bits.view(np.float64)
+    special = np.array([0.0, -0.0, 1.0, -1.0, 5e-324, -5e-324, 1e-310, 2.0 ** -126, 2.0 ** -149, 2.0 ** -150,
+                        3.4028234663852886e38, 3.4028235677973366e38, 1e39, -1e300, np.inf, -np.inf, np.nan,
+                        1.0 + 2.0 ** -24, 1.0 + 3 * 2.0 ** -24, 1.0 + 2.0 ** -52, 2.0 ** 127 * 1.9999999])
+    a[4096:4096 + special.size] = special
+    hi, lo = gbx.split_f64(torch.from_numpy(a).to(cuda))
+    torch.cuda.synchronize()
+    with np.errstate(over="ignore", invalid="ignore"):
+        h_ref = a.astype(np.float32)
+        l_ref = (a - h_ref.astype(np.float64)).astype(np.float32)
+    h, l = hi.cpu().numpy(), lo.cpu().numpy()
+    for got, ref in ((h, h_ref), (l, l_ref)):
+        nan = np.isnan(ref)
+        assert np.array_equal(np.isnan(got), nan)
+        assert np.array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))
 
 
 def test_dposv_mixed_batched_reports_non_spd_member(gbx, cuda):

@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
     "gbx_dpotri_tiled_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dpotri_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
+    "gbx_split_f64": (_i, [_vp, _vp, _vp, ctypes.c_longlong, _vp]),
     "gbx_dposv_tiled_host_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dposv_tiled_host": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gbx_potrf_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _szp]),
@@ -236,6 +237,16 @@ def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=N
     if st < 0 and st != GBX_ERR_NOCONV:
         raise GbxError("gbx_dposv_mixed", st)
     return X, info.as_dict(), st
+
+
+def split_f64(a, stream=None):
+    """(hi, lo) FP32 tensors with hi + lo = a for an FP64 CUDA tensor (gbx_split_f64)."""
+    import torch
+    a = a.contiguous()
+    hi = torch.empty(a.shape, dtype=torch.float32, device=a.device)
+    lo = torch.empty(a.shape, dtype=torch.float32, device=a.device)
+    call("gbx_split_f64", _ptr(a), _ptr(hi), _ptr(lo), a.numel(), _stream(stream))
+    return hi, lo
 
 
 def potri_tiled(tiles, N, NB, workspace=None, stream=None):

@@ -728,8 +728,10 @@ namespace mixed {
 // factorises the selected matrices of a batch (sel[k] != 0; all when sel is null) in one launch.
 // A, W: the matrices' tile-major lower storage concatenated in batch order (matrix k's slots follow
 // matrix k-1's). The table is ordered largest first so the longest critical paths start first.
+// w_ready: W already holds fl32(A) for every selected matrix (written by the refinement's single
+// pass over A), so the conversion launches are skipped; only valid with shift == 0.
 int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
-                 const unsigned char* sel, void* work, size_t work_bytes, cudaStream_t s) {
+                 const unsigned char* sel, void* work, size_t work_bytes, cudaStream_t s, bool w_ready) {
   const Ws w = layout_batch(batch, n, NB);
   if (work_bytes < w.total) return GBX_ERR_WORKSPACE;
   {
@@ -833,6 +835,7 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
   // rows of a ragged tile's low-precision copy past the matrix edge are never written; the tensor
   // cores read them, but they only reach rows / columns of C that the epilogue does not store
   for (const MixMat& m : mats) {
+    if (w_ready && shift == 0.0) break;
     const long long nsl = (long long)m.NT * (m.NT + 1) / 2, nel = nsl * (long long)NB * NB;
     convert_kernel<<<std::min<long long>(g_sms * 8, (nel + 255) / 256), 256, 0, s>>>(
         A + m.slot0 * (long long)NB * NB, W + m.slot0 * (long long)NB * NB, nel);
@@ -884,7 +887,7 @@ extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int pre
                                size_t work_bytes, void* stream) {
   if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !A || !W || !work || (prec != 0 && prec != 1))
     return GBX_ERR_ARG;
-  return launch_batch(1, &N, NB, A, W, prec, shift, nullptr, work, work_bytes, (cudaStream_t)stream);
+  return launch_batch(1, &N, NB, A, W, prec, shift, nullptr, work, work_bytes, (cudaStream_t)stream, false);
 }
 
 extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes) {
@@ -901,7 +904,7 @@ extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const do
   size_t need = 0;
   if (int e = gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &need)) return e;
   if (!A || !W || !work || (prec != 0 && prec != 1)) return GBX_ERR_ARG;
-  return launch_batch(batch, n, NB, A, W, prec, shift, sel, work, work_bytes, (cudaStream_t)stream);
+  return launch_batch(batch, n, NB, A, W, prec, shift, sel, work, work_bytes, (cudaStream_t)stream, false);
 }
 
 extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info,

@@ -32,6 +32,13 @@ extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const i
                                             float* cond_est, void* stream);
 
 namespace gbx {
+namespace mixed {
+int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
+                 const unsigned char* sel, void* work, size_t work_bytes, cudaStream_t s, bool w_ready);
+}  // namespace mixed
+}  // namespace gbx
+
+namespace gbx {
 namespace refine {
 
 constexpr int kMaxRhs = 16;
@@ -369,12 +376,96 @@ __global__ void symm_cols_batched(const RMat* mats, const int* list, const doubl
 // Error about 2^-47 relative to sum |a x|, far below the 1e-14 backward-error target, at FP32 rates
 // (GB300 runs FP32 FMAs ~67x faster than FP64 ones). Intrinsics keep the compiler from contracting
 // the error-free transformations.
-__global__ void split_kernel(const double* A, float* hi, float* lo, long long n) {
+//
+// The split by integer arithmetic on the bit pattern (IEEE-754 round to nearest, ties to even): with
+// a = (2^52 + m) 2^(e-1075), hi keeps the top 23 bits of m, rounded on the low 29 bits, and
+// a - hi = +-r 2^(e-1075) with |r| <= 2^28, so lo = fl32(r) 2^(e-1075) exactly. Bitwise equal to the
+// FP64 route hi = fl32(a), lo = fl32(a - hi) whenever hi and lo are FP32 normal numbers (biased
+// exponent e in [950, 1149]); other values (zero, tiny, huge, Inf, NaN) take the FP64 route, which
+// costs four FP64-pipe operations per element and would bound a pass over A on this GPU.
+__device__ __forceinline__ void split_f64(double a, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e >= 950 && e <= 1149) {
+    const unsigned t = (unsigned)((b >> 29) & 0x7FFFFFu), rem = (unsigned)(b & 0x1FFFFFFFu);
+    const bool up = rem > 0x10000000u || (rem == 0x10000000u && (t & 1u));
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    hi = __uint_as_float(sgn | ((((unsigned)(e - 896) << 23) | t) + (up ? 1u : 0u)));
+    int r = up ? (int)rem - (1 << 29) : (int)rem;
+    if (sgn) r = -r;
+    lo = __int2float_rn(r) * __uint_as_float((unsigned)(e - 948) << 23);  // r 2^(e-1075)
+  } else {
+    hi = __double2float_rn(a);
+    lo = __double2float_rn(a - (double)hi);
+  }
+}
+
+// One pass over the FP64 tiles of every listed matrix (one CTA per tile slot, padding included):
+// W = fl32(A), the factor's working copy; Ah + Al = A, the split for the double-float residual
+// products; and the row sums of |A| for ||A||_inf, where the strictly lower part of each tile also
+// counts for the rows of its columns. Warps pair up on 64-row slabs, four columns at a time, with
+// coalesced 8-byte loads, eight in flight per thread. The sums of |fl32(a)| are carried in FP32
+// over at most 64 terms and added up in FP64 (relative error a few 1e-6, for a norm).
+__global__ void __launch_bounds__(256) prep_batched(const RMat* mats, const int* list, const double* A, float* W,
+                                                    float* Ah, float* Al, double* rs, int NB, int nrhs) {
+  GBX_MAT_OF_BLOCK();
+  __shared__ float s_col[2][1024];
+  __shared__ double s_row[4][64];
+  int m, n;
+  if (!slot_tile(blockIdx.x, mt.NT, m, n)) return;
+  const int mrows = tdim(m, mt.N, NB, mt.NT), ncols = tdim(n, mt.N, NB, mt.NT);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, cg = warp >> 1, half = warp & 1;
+  const bool diag = m == n;
+  const long long tb = (mt.slot0 + blockIdx.x) * (long long)NB * NB;
+  double* rsm = rs + mt.vec0 / nrhs;
+  for (int k = threadIdx.x; k < 2 * NB; k += blockDim.x) s_col[k / NB][k % NB] = 0.f;
+  __syncthreads();
+  for (int r0 = 0; r0 < NB; r0 += 64) {
+    const int i = r0 + half * 32 + lane;
+    double rsum = 0.0;
+    for (int c0 = cg; c0 < NB; c0 += 32) {  // columns c0, c0 + 4, ..., c0 + 28
+      double a[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) a[u] = __ldcs(A + tb + i + (long long)(c0 + 4 * u) * NB);
+      float part = 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int c = c0 + 4 * u;
+        const long long e = tb + i + (long long)c * NB;
+        float h, l;
+        split_f64(a[u], h, l);
+        W[e] = h;
+        Ah[e] = h;
+        Al[e] = l;
+        const float v = (i < mrows && c < ncols) ? fabsf(h) : 0.f;
+        if (!diag || c <= i) part += v;
+        float cv = (!diag || i > c) ? v : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cv += __shfl_xor_sync(0xffffffffu, cv, o);
+        if (lane == 0) s_col[half][c] += cv;  // (half, c) belongs to this warp alone
+      }
+      rsum += (double)part;
+    }
+    s_row[cg][half * 32 + lane] = rsum;
+    __syncthreads();
+    if (threadIdx.x < 64 && r0 + (int)threadIdx.x < mrows) {
+      const int t = threadIdx.x;
+      atomicAdd(rsm + (long long)m * NB + r0 + t, (s_row[0][t] + s_row[1][t]) + (s_row[2][t] + s_row[3][t]));
+    }
+    __syncthreads();
+  }
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x)
+    if (!diag || c + 1 < mrows) atomicAdd(rsm + (long long)n * NB + c, (double)s_col[0][c] + (double)s_col[1][c]);
+}
+
+// hi + lo = a elementwise (the split of the residual products, for vectors and for testing)
+__global__ void split_f64_kernel(const double* __restrict__ A, float* __restrict__ hi, float* __restrict__ lo,
+                                 long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const double a = A[i];
-    const float h = __double2float_rn(a);
+    float h, l;
+    split_f64(__ldcs(A + i), h, l);
     hi[i] = h;
-    lo[i] = __double2float_rn(a - (double)h);
+    lo[i] = l;
   }
 }
 
@@ -893,33 +984,6 @@ __global__ void scale_kernel(double* Y, long long n, double beta) {
     Y[i] = beta == 0.0 ? 0.0 : Y[i] * beta;
 }
 
-// row sums of |A| (for ||A||_inf)
-__device__ void absrow_body(const double* A, double* rs, int N, int NB, int NT) {
-  const int slot = blockIdx.x;
-  int m, n;
-  if (!slot_tile(slot, NT, m, n)) return;
-  const int mrows = tdim(m, N, NB, NT), ncols = tdim(n, N, NB, NT);
-  const double* T = A + (long long)slot * NB * NB;
-  for (int i = threadIdx.x; i < mrows; i += blockDim.x) {
-    double s = 0.0;
-    for (int c = 0; c < ncols; ++c)
-      if (m != n || c <= i) s += fabs(T[i + (long long)c * NB]);
-    atomicAdd(rs + (long long)m * NB + i, s);
-  }
-  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-    double s = 0.0;
-    for (int r = 0; r < mrows; ++r)
-      if (m != n || r > c) s += fabs(T[r + (long long)c * NB]);
-    atomicAdd(rs + (long long)n * NB + c, s);
-  }
-}
-__global__ void absrow_kernel(const double* A, double* rs, int N, int NB, int NT) { absrow_body(A, rs, N, NB, NT); }
-// row sums for every matrix of the list; rs holds one N-vector per matrix at offset vec0 / nrhs
-__global__ void absrow_batched(const RMat* mats, const int* list, const double* A, double* rs, int NB, int nrhs) {
-  GBX_MAT_OF_BLOCK();
-  absrow_body(A + mt.slot0 * NB * NB, rs + mt.vec0 / nrhs, mt.N, NB, mt.NT);
-}
-
 // per right-hand side j: out[j*3 + q] = reduction q of the columns (0: dot(a,b), 1: max|a|, 2: max|b|)
 __device__ void colstats_body(const double* a, const double* b, int N, double* out) {
   const int j = blockIdx.x;
@@ -1139,6 +1203,13 @@ BLayout blayout(int batch, const int* n, int NB, int nrhs) {
 }
 }  // namespace
 
+extern "C" int gbx_split_f64(const double* a, float* hi, float* lo, long long n, void* stream) {
+  if (n < 0 || (n > 0 && (!a || !hi || !lo))) return GBX_ERR_ARG;
+  if (n == 0) return GBX_OK;
+  split_f64_kernel<<<(unsigned)std::min<long long>(4096, (n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, hi, lo, n);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
 extern "C" int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes) {
   if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > 1024 || nrhs <= 0 || nrhs > kMaxRhs || !bytes) return GBX_ERR_ARG;
   for (int k = 0; k < batch; ++k)
@@ -1198,15 +1269,27 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
   std::vector<gbx_refine_info> inf(batch);
   std::memset(inf.data(), 0, batch * sizeof(gbx_refine_info));
 
+  // 0. one pass over A: W = fl32(A) for the first factorisation, the split of A for the residual
+  //    products, and the row sums of |A|
+  {
+    int slots = 0;
+    for (int k = 0; k < batch; ++k) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
+    if (cudaMemcpyAsync(dmats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(dlist, all.data(), batch * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(rowsum, 0, (size_t)(nvec / nrhs) * 8, s) != cudaSuccess)
+      return GBX_ERR_CUDA;
+    prep_batched<<<dim3(slots, 1, (unsigned)batch), 256, 0, s>>>(dmats, dlist, A, W, Ahi, Alo, rowsum, NB, nrhs);
+  }
   // 1. low-precision factorisation of every matrix; the ones that break down are factorised again,
-  //    alone, with a growing diagonal shift
+  //    alone, with a growing diagonal shift (from A again: W then holds the failed attempt)
   std::vector<unsigned char> sel(batch, 1);
   std::vector<int> finfo(batch, 0);
   std::vector<float> cond(batch, 0.f), cnow(batch);
   double shift = 0.0;
   int first_bad = 0;
   for (int attempt = 0; attempt < 8; ++attempt) {
-    if (int e = gbx_potrf_mixed_batched(batch, n, NB, A, W, prec, shift, sel.data(), fwork, L.fwork_bytes, stream))
+    if (int e = gbx::mixed::launch_batch(batch, n, NB, A, W, prec, shift, sel.data(), fwork, L.fwork_bytes, s,
+                                         attempt == 0))
       return e;
     if (int e = gbx_potrf_mixed_batched_info(fwork, batch, n, NB, finfo.data(), cnow.data(), stream)) return e;
     bool any = false;
@@ -1334,16 +1417,9 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
   if (cudaMemcpyAsync(dmats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
       !upload_list(live))
     return GBX_ERR_CUDA;
-  split_kernel<<<1024, 256, 0, s>>>(A, Ahi, Alo, slot * (long long)NB * NB);
   diag_inverse_batched<<<dim3(maxNT, (NB + kBlk - 1) / kBlk, (unsigned)live.size()), kThreads,
                          op_trsm_smem_elems<float>() * sizeof(float), s>>>(dmats, dlist, W, Inv, NB);
-  // ||A||_inf and ||b_j||_inf per matrix
-  cudaMemsetAsync(rowsum, 0, (size_t)(nvec / nrhs) * 8, s);
-  {
-    int slots = 0;
-    for (int k : live) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
-    absrow_batched<<<dim3(slots, 1, (unsigned)live.size()), 256, 0, s>>>(dmats, dlist, A, rowsum, NB, nrhs);
-  }
+  // ||A||_inf (row sums from the pass over A) and ||b_j||_inf per matrix
   colstats_batched<<<dim3(1, 1, (unsigned)live.size()), 256, 0, s>>>(dmats, dlist, rowsum, nullptr, nrhs, 1, stats);
   stats_of(live, B, nullptr, stats_x);
   if (!fetch_stats()) return GBX_ERR_CUDA;
