@@ -73,8 +73,9 @@ __device__ void diag_inverse_body(const float* W, float* Inv, int N, int NB, int
     if (r < m) out[(r0 + r) + (long long)c * NB] = (r0 + r == c) ? 1.f : 0.f;
   }
   __syncthreads();
-  const float* L = W + slot_of(K, K, NT) * (long long)NB * NB;
-  op_trsm<float>(L, NB, out + r0, NB, m, n, sm);
+  // row r of L^{-T} is zero left of column r: rows r0.. solve against the trailing L(r0:, r0:) only
+  const float* L = W + slot_of(K, K, NT) * (long long)NB * NB + r0 + (long long)r0 * NB;
+  op_trsm<float>(L, NB, out + r0 + (long long)r0 * NB, NB, m, n - r0, sm);
 }
 __global__ void __launch_bounds__(kThreads, 1) diag_inverse_kernel(const float* W, float* Inv, int N, int NB, int NT) {
   extern __shared__ __align__(16) float sm_f[];
