@@ -46,7 +46,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision configuration")
     p.add_argument("--no-batched", action="store_true", help="skip the batched configuration")
-    p.add_argument("--profile-case", choices=["dag", "mixed", "batched", "refine"], default=None,
+    p.add_argument("--profile-case", choices=["dag", "mixed", "batched", "refine", "batched_mixed"], default=None,
                    help="run one small case of one kernel (N=8192) for an ncu capture; prints no JSON")
     p.add_argument("--profile-N", type=int, default=8192, help="matrix order of --profile-case dag/mixed")
     return p.parse_args()
@@ -726,7 +726,12 @@ def profile_case(case, N=8192):
     from ttg_gb300 import workloads
     dev = torch.device("cuda:0")
     NB = 512
-    if case == "refine":  # the refinement of a kappa = 1e6 fp16 solve: sweeps and double-float products
+    if case == "batched_mixed":  # the 256-system batched mixed solve (fp16) of the benchmark, once
+        sizes = workloads.batch_sizes(256, 4, 32, 128, seed=42)
+        A, B = workloads.householder_batch(sizes, NB, 2, 1e4, 42, dev, nrhs=4)
+        X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, 4, prec="fp16", tol=1e-14)
+        assert st == 0
+    elif case == "refine":  # the refinement of a kappa = 1e6 fp16 solve: sweeps and double-float products
         A = workloads.householder_tiles(N, NB, 4, 1e6, 42, dev)
         B = torch.from_numpy(workloads.rhs(N, 8, 42)).to(dev)
         X, info, st = gbx.dposv_mixed(A, N, NB, B, prec="fp16", tol=1e-14)

@@ -171,7 +171,7 @@ int gbx_gemm_bf16_nt_f32(int M, int N, int K, const void* A, int lda, const void
 #define GBX_PREC_BF16 0
 #define GBX_PREC_FP16 1
 
-/* Bytes of workspace gbx_potrf_mixed needs (NB a multiple of 256, at most 1024). */
+/* Bytes of workspace gbx_potrf_mixed needs (NB 256 or 512). */
 int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes);
 
 /* Low-precision Cholesky of the FP64 tile-major lower matrix A into the FP32 tile-major factor W
@@ -220,7 +220,7 @@ int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, fl
 int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info, float* cond_est,
                                  void* stream);
 
-/* Bytes of workspace gbx_dposv_mixed needs. */
+/* Bytes of workspace gbx_dposv_mixed needs (NB 256 or 512, nrhs <= 16). */
 int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes);
 
 /* Solves A X = B (A FP64 tile-major lower, B and X column-major N x nrhs, nrhs <= 16) to the FP64

@@ -70,6 +70,7 @@ def test_batched_mixed_workspace_without_gpu(gbx):
     sz, one = ctypes.c_size_t(0), ctypes.c_size_t(0)
     assert L.gbx_dposv_mixed_batched_bufferSize(0, n, 256, 2, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
     assert L.gbx_dposv_mixed_batched_bufferSize(3, n, 200, 2, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_bufferSize(3, n, 1024, 2, ctypes.byref(sz)) == gbx.GBX_ERR_ARG  # NB 256 or 512
     assert L.gbx_dposv_mixed_batched_bufferSize(3, n, 256, 17, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
     bad = (ctypes.c_int * 2)(100, 0)
     assert L.gbx_potrf_mixed_batched_bufferSize(2, bad, 256, ctypes.byref(sz)) == gbx.GBX_ERR_ARG

@@ -403,60 +403,67 @@ __device__ __forceinline__ void split_f64(double a, float& hi, float& lo) {
 
 // One pass over the FP64 tiles of every listed matrix (one CTA per tile slot, padding included):
 // W = fl32(A), the factor's working copy; Ah + Al = A, the split for the double-float residual
-// products; and the row sums of |A| for ||A||_inf, where the strictly lower part of each tile also
-// counts for the rows of its columns. Warps pair up on 64-row slabs, four columns at a time, with
-// coalesced 8-byte loads, eight in flight per thread. The sums of |fl32(a)| are carried in FP32
-// over at most 64 terms and added up in FP64 (relative error a few 1e-6, for a norm).
+// products (both 0 outside the matrix's lower triangle); and the row sums of |A| for ||A||_inf,
+// where the strictly lower part of each tile also counts for the rows of its columns. Thread t
+// owns rows 2t, 2t + 1 and walks the columns, so a CTA reads each 4 KB column in one contiguous
+// burst (16-byte loads, eight columns in flight per thread) and keeps its row sums in registers;
+// the column sums meet in warp shuffles and shared memory. The sums of |fl32(a)| are carried in FP32 over at most 8 terms per thread and column
+// group and added up in FP64 (relative error about 1e-6, for a norm). NB <= 512.
 __global__ void __launch_bounds__(256) prep_batched(const RMat* mats, const int* list, const double* A, float* W,
                                                     float* Ah, float* Al, double* rs, int NB, int nrhs) {
   GBX_MAT_OF_BLOCK();
-  __shared__ float s_col[2][1024];
-  __shared__ double s_row[4][64];
+  __shared__ float s_col[8][512];
   int m, n;
   if (!slot_tile(blockIdx.x, mt.NT, m, n)) return;
   const int mrows = tdim(m, mt.N, NB, mt.NT), ncols = tdim(n, mt.N, NB, mt.NT);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, cg = warp >> 1, half = warp & 1;
-  const bool diag = m == n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = 2 * threadIdx.x;  // rows i0, i0 + 1
+  const bool diag = m == n, live = i0 < NB;
   const long long tb = (mt.slot0 + blockIdx.x) * (long long)NB * NB;
   double* rsm = rs + mt.vec0 / nrhs;
-  for (int k = threadIdx.x; k < 2 * NB; k += blockDim.x) s_col[k / NB][k % NB] = 0.f;
-  __syncthreads();
-  for (int r0 = 0; r0 < NB; r0 += 64) {
-    const int i = r0 + half * 32 + lane;
-    double rsum = 0.0;
-    for (int c0 = cg; c0 < NB; c0 += 32) {  // columns c0, c0 + 4, ..., c0 + 28
-      double a[8];
+  double rsum0 = 0.0, rsum1 = 0.0;
+  for (int c0 = 0; c0 < NB; c0 += 8) {
+    double2 a[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) a[u] = __ldcs(A + tb + i + (long long)(c0 + 4 * u) * NB);
-      float part = 0.f;
+    for (int u = 0; u < 8; ++u)
+      a[u] = live ? __ldcs((const double2*)(A + tb + i0 + (long long)(c0 + u) * NB)) : make_double2(0.0, 0.0);
+    float p0 = 0.f, p1 = 0.f;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int c = c0 + 4 * u;
-        const long long e = tb + i + (long long)c * NB;
-        float h, l;
-        split_f64(a[u], h, l);
-        W[e] = h;
-        Ah[e] = h;
-        Al[e] = l;
-        const float v = (i < mrows && c < ncols) ? fabsf(h) : 0.f;
-        if (!diag || c <= i) part += v;
-        float cv = (!diag || i > c) ? v : 0.f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) cv += __shfl_xor_sync(0xffffffffu, cv, o);
-        if (lane == 0) s_col[half][c] += cv;  // (half, c) belongs to this warp alone
+    for (int u = 0; u < 8; ++u) {
+      const int c = c0 + u;
+      // entries of the lower triangle inside the matrix; the rest (padding past N, the strict upper
+      // part of diagonal tiles) is never read by the factorisation or the products and becomes 0
+      const bool ok0 = c < ncols && i0 < mrows && (!diag || c <= i0);
+      const bool ok1 = c < ncols && i0 + 1 < mrows && (!diag || c <= i0 + 1);
+      float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+      if (ok0) split_f64(a[u].x, h0, l0);
+      if (ok1) split_f64(a[u].y, h1, l1);
+      if (live) {
+        const long long e = tb + i0 + (long long)c * NB;
+        *(float2*)(W + e) = make_float2(h0, h1);
+        *(float2*)(Ah + e) = make_float2(h0, h1);
+        *(float2*)(Al + e) = make_float2(l0, l1);
       }
-      rsum += (double)part;
+      const float v0 = fabsf(h0), v1 = fabsf(h1);
+      p0 += v0;
+      p1 += v1;
+      float cv = ((!diag || i0 != c) ? v0 : 0.f) + ((!diag || i0 + 1 != c) ? v1 : 0.f);  // strictly lower
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) cv += __shfl_xor_sync(0xffffffffu, cv, o);
+      if (lane == 0) s_col[warp][c] = cv;
     }
-    s_row[cg][half * 32 + lane] = rsum;
-    __syncthreads();
-    if (threadIdx.x < 64 && r0 + (int)threadIdx.x < mrows) {
-      const int t = threadIdx.x;
-      atomicAdd(rsm + (long long)m * NB + r0 + t, (s_row[0][t] + s_row[1][t]) + (s_row[2][t] + s_row[3][t]));
-    }
-    __syncthreads();
+    rsum0 += (double)p0;
+    rsum1 += (double)p1;
   }
-  for (int c = threadIdx.x; c < ncols; c += blockDim.x)
-    if (!diag || c + 1 < mrows) atomicAdd(rsm + (long long)n * NB + c, (double)s_col[0][c] + (double)s_col[1][c]);
+  if (i0 < mrows) atomicAdd(rsm + (long long)m * NB + i0, rsum0);
+  if (i0 + 1 < mrows) atomicAdd(rsm + (long long)m * NB + i0 + 1, rsum1);
+  __syncthreads();
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+    float t = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += s_col[w][c];
+    if (!diag || c + 1 < mrows) atomicAdd(rsm + (long long)n * NB + c, (double)t);
+  }
 }
 
 // hi + lo = a elementwise (the split of the residual products, for vectors and for testing)
@@ -1212,7 +1219,7 @@ extern "C" int gbx_split_f64(const double* a, float* hi, float* lo, long long n,
 }
 
 extern "C" int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes) {
-  if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > 1024 || nrhs <= 0 || nrhs > kMaxRhs || !bytes) return GBX_ERR_ARG;
+  if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > 512 || nrhs <= 0 || nrhs > kMaxRhs || !bytes) return GBX_ERR_ARG;
   for (int k = 0; k < batch; ++k)
     if (n[k] <= 0) return GBX_ERR_ARG;
   *bytes = blayout(batch, n, NB, nrhs).total;
