@@ -695,6 +695,17 @@ struct SweepTask {
 constexpr int kDiagSubs = 8;  // sub-tasks of a diagonal task: 64 output entries each
 constexpr int kUpdSubs = 8;   // sub-tasks of an off-diagonal task: 64 rows (forward) / columns (backward)
 
+// L2 prefetch of rows [r0, r1) of columns [c0, c1) of a column-major tile (one 128-byte line per
+// instruction), spread over the CTA
+__device__ __forceinline__ void prefetch_block(const float* T, int NB, int r0, int r1, int c0, int c1) {
+  if (r1 <= r0 || c1 <= c0) return;
+  const int nl = (r1 - r0 + 31) >> 5;
+  for (int idx = threadIdx.x; idx < (c1 - c0) * nl; idx += blockDim.x) {
+    const int c = c0 + idx / nl, l = idx % nl;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(T + r0 + 32 * l + (long long)c * NB));
+  }
+}
+
 // 16-byte load of rows r..r+3 of column c of a tile; rows at or past `lim` read as zero (the tile slot
 // holds NB rows, so a load that starts before `lim` stays inside it)
 __device__ __forceinline__ float4 ld4_rows(const float* T, int r, long long c, int NB, int lim) {
@@ -928,6 +939,19 @@ __global__ void __launch_bounds__(256) sweep_kernel(int dir, const RMat* mats, c
     const int N = mt.N, NT = mt.NT;
     int* c = cnt + mt.inv0;
     int* f = flag + mt.inv0;
+    {  // the task's block of the factor does not depend on the wait: start fetching it into L2
+      const int kn = tdim(tk.K, N, NB, NT), s64 = 64 * tk.sub;
+      if (tk.kind == 0) {
+        const float* out = Inv + (mt.inv0 + tk.K) * (long long)NB * NB;
+        if (dir == 0) prefetch_block(out, NB, 0, min(kn, s64 + 64), s64, min(kn, s64 + 64));
+        else prefetch_block(out, NB, s64, min(kn, s64 + 64), s64, kn);
+      } else {
+        const float* L = W + (mt.slot0 + slot_of(tk.M, tk.K, NT)) * (long long)NB * NB;
+        const int mrows = tdim(tk.M, N, NB, NT);
+        if (dir == 0) prefetch_block(L, NB, s64, min(mrows, s64 + 64), 0, kn);
+        else prefetch_block(L, NB, 0, mrows, s64, min(kn, s64 + 64));
+      }
+    }
     if (threadIdx.x == 0) {
       bool ok;
       if (dir == 0)
