@@ -595,13 +595,23 @@ __device__ void symm_cols_df_body(const float* Ah, const float* Al, const float*
       float sh[NR], sl[NR];
 #pragma unroll
       for (int j = 0; j < NR; ++j) sh[j] = sl[j] = 0.f;
-      for (int r = lane; r < rw; r += 32) {
-        if (m == n && r0 + r <= c) continue;  // strictly lower part only
-        const long long e = tb + (r0 + r) + (long long)c * NB;
-        const float ah = __ldg(Ah + e), al = __ldg(Al + e);
+      for (int r = lane; r < rw; r += 128) {  // rows r, r + 32, r + 64, r + 96: four load pairs in flight
+        float ah[4], al[4];
+        int xi[4];
 #pragma unroll
-        for (int j = 0; j < NR; ++j)
-          if (j < nrhs) df_fma(sh[j], sl[j], ah, al, xh[j * 512 + r], xl[j * 512 + r]);
+        for (int u = 0; u < 4; ++u) {
+          const int rr = r + 32 * u;
+          const bool ok = rr < rw && !(m == n && r0 + rr <= c);  // strictly lower part only
+          const long long e = tb + (r0 + rr) + (long long)c * NB;
+          ah[u] = ok ? __ldg(Ah + e) : 0.f;  // a masked entry adds an exact zero
+          al[u] = ok ? __ldg(Al + e) : 0.f;
+          xi[u] = ok ? rr : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int j = 0; j < NR; ++j)
+            if (j < nrhs) df_fma(sh[j], sl[j], ah[u], al[u], xh[j * 512 + xi[u]], xl[j * 512 + xi[u]]);
       }
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
