@@ -159,7 +159,8 @@ __device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, in
 // the later entries, so column c of Lp is read with 16-byte loads that do not depend on x, and the
 // chain per column is one multiply and one FMA. Lp is 16-byte aligned and ldp a multiple of 4. The
 // warp sync every 8 columns bounds how far ahead the compiler hoists the loads (register pressure
-// inside the persistent mixed kernel). Called by whole warps.
+// inside the persistent mixed kernel). It is a full-warp sync: every caller runs this on all 32
+// lanes of its warps (a partial warp would never meet the sync).
 __device__ __forceinline__ void col_solve32(float (&x)[32], const float* Lp, int ldp) {
 #pragma unroll
   for (int c = 0; c < 32; ++c) {
@@ -299,7 +300,9 @@ constexpr size_t op_trsm_smem_elems() {
   return (size_t)kPW * kBlk + (size_t)TrsmChunk<T>::value * kBlk + (size_t)TrsmChunk<T>::value * kPW + kPW * kPW;
 }
 
-template <typename T>
+// kColSolve (FP32 only): the panel solve in the column-wise form with the branch-free reciprocal,
+// for kernels with registers to spare; the default keeps the row-wise form and IEEE division.
+template <typename T, bool kColSolve = false>
 __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, int n, T* sm) {
   constexpr int KC = TrsmChunk<T>::value;
   T* P = sm;                    // [kPW][128]  panel, P[c*128 + r]
@@ -371,12 +374,20 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
         for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + 4 * tx + i] -= acc[i][j];
       __syncthreads();
     }
-    if (tid < m && tid < kBlk) {  // each thread solves its row of the panel in registers
+    // each thread solves its row of the panel in registers; the column-wise solve synchronises its
+    // warp, so it runs on whole warps (rows past m are zero in P and are never stored back)
+    const int solvers = kColSolve ? ((m + 31) & ~31) : m;
+    if (tid < solvers && tid < kBlk) {
       const int r = tid;
       T x[kPW];
 #pragma unroll
       for (int c = 0; c < kPW; ++c) x[c] = P[c * kBlk + r];
-      row_solve32<T>(x, Ld, kPW, pw);  // Ld holds L(p0+c, p0+c2) at c + 32*c2
+      if constexpr (kColSolve) {
+        if (pw == kPW) col_solve32(x, Ld, kPW);
+        else row_solve32<T>(x, Ld, kPW, pw);
+      } else {
+        row_solve32<T>(x, Ld, kPW, pw);  // Ld holds L(p0+c, p0+c2) at c + 32*c2
+      }
 #pragma unroll
       for (int c = 0; c < kPW; ++c) P[c * kBlk + r] = x[c];
     }

@@ -75,7 +75,7 @@ __device__ void diag_inverse_body(const float* W, float* Inv, int N, int NB, int
   __syncthreads();
   // row r of L^{-T} is zero left of column r: rows r0.. solve against the trailing L(r0:, r0:) only
   const float* L = W + slot_of(K, K, NT) * (long long)NB * NB + r0 + (long long)r0 * NB;
-  op_trsm<float>(L, NB, out + r0 + (long long)r0 * NB, NB, m, n - r0, sm);
+  op_trsm<float, true>(L, NB, out + r0 + (long long)r0 * NB, NB, m, n - r0, sm);
 }
 __global__ void __launch_bounds__(kThreads, 1) diag_inverse_kernel(const float* W, float* Inv, int N, int NB, int NT) {
   extern __shared__ __align__(16) float sm_f[];
