@@ -484,7 +484,8 @@ def run_batched(gbx, dev, count=4096, reps=3, cpu=True):
 def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, cpu_sample=16):
     """Batched mixed precision: 256 SPD systems, n uniform in 128*{4..32}, H diag(lam) H^T with 2
     reflectors (matrix k: seed 42 + k), kappa = 1e4, 4 right-hand sides each; one tensor-core
-    factorisation launch for the whole batch + batched FP64 PCG to backward error 1e-14. Against the
+    factorisation launch for the whole batch (fp16, bf16 and fp8-e4m3 operands) + batched FP64 PCG
+    to backward error 1e-14. Against the
     plain FP64 GPU path run matrix by matrix (gbx_dpotrf_tiled + gbx_dpotrs_tiled)."""
     import ctypes
 
@@ -521,7 +522,7 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
     del T, work
     torch.cuda.empty_cache()
     out["plain_fp64_per_matrix"] = {"ms": plain_ms, "tflops": flops / (plain_ms * 1e-3) / 1e12}
-    for prec in ("fp16", "bf16"):
+    for prec in ("fp16", "bf16", "fp8"):  # fp8: e4m3 operands on kind::f8f6f4
         W = torch.empty(total, dtype=torch.float32, device=dev)
         X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300, W=W)
         torch.cuda.synchronize()
@@ -537,6 +538,7 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
         out[prec] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "matrices_per_s": count / (ms * 1e-3),
                      "speedup_vs_plain_fp64": plain_ms / ms, "status": st, "iterations_max": int(max(it)),
                      "iterations_mean": float(np.mean(it)), "factor_retries": int(sum(i["factor_retries"] for i in infos)),
+                     "shift_max": float(max(i["shift"] for i in infos)),
                      "backward_error_max": float(max(be)), "forward_error_vs_fp64": fe}
         del W
         torch.cuda.empty_cache()

@@ -167,16 +167,17 @@ int gbx_gemm_bf16_nt_f32(int M, int N, int K, const void* A, int lda, const void
  * the reference (which has no solve and no mixed precision); built on the same flowgraph.
  * ========================================================================================== */
 
-/* Precision of the off-diagonal tensor-core operands. */
+/* Precision of the off-diagonal tensor-core operands (E4M3: fp8, tcgen05 kind::f8f6f4). */
 #define GBX_PREC_BF16 0
 #define GBX_PREC_FP16 1
+#define GBX_PREC_E4M3 2
 
 /* Bytes of workspace gbx_potrf_mixed needs (NB 256 or 512). */
 int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes);
 
 /* Low-precision Cholesky of the FP64 tile-major lower matrix A into the FP32 tile-major factor W
  * (same layout): diagonal POTRF and TRSM in FP32, SYRK/GEMM updates on the tensor cores with
- * bf16/fp16 operands scaled per row by powers of two and FP32 accumulation. The diagonal of A is
+ * bf16/fp16/fp8-e4m3 operands scaled per row by powers of two and FP32 accumulation. The diagonal of A is
  * multiplied by (1 + shift) first (0 for none). Asynchronous; the status (0, first bad pivot, or
  * GBX_ERR_TIMEOUT) and the largest diagonal-tile condition estimate come from
  * gbx_potrf_mixed_info, which synchronises the stream. */

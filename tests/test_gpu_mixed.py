@@ -23,7 +23,8 @@ def dense_from_tiles(t, N, NB):
 
 
 @pytest.mark.parametrize("N,NB,prec,tol", [(2048, 512, "bf16", 3e-2), (2048, 512, "fp16", 4e-3),
-                                           (1800, 256, "bf16", 3e-2), (1024, 256, "fp16", 4e-3)])
+                                           (1800, 256, "bf16", 3e-2), (1024, 256, "fp16", 4e-3),
+                                           (2048, 512, "fp8", 0.25), (1800, 256, "fp8", 0.25)])
 def test_mixed_factor_close_to_fp64(gbx, cuda, N, NB, prec, tol):
     import torch
     A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
@@ -36,6 +37,7 @@ def test_mixed_factor_close_to_fp64(gbx, cuda, N, NB, prec, tol):
     Lw = oracle.tiles_to_lower(W.double().cpu().numpy(), N, NB)
     L64 = oracle.tiles_to_lower(ref, N, NB)
     err = np.abs(Lw - L64).max() / np.abs(L64).max()
+    print("factor %s N=%d NB=%d: max|W - L64| / max|L64| = %.3g" % (prec, N, NB, err))
     assert err <= tol, err
     assert 1.0 <= cond < 10.0  # diagonally dominant tiles
 
@@ -60,14 +62,15 @@ def solve_and_check(gbx, cuda, A, N, NB, nrhs, prec, kappa):
     return info
 
 
-@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+@pytest.mark.parametrize("prec", ["bf16", "fp16", "fp8"])
 def test_dposv_mixed_well_conditioned(gbx, cuda, prec):
     import torch
     N, NB = 3000, 512
     A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
     gbx.gen_uniform_sym(A, N, NB, seed=42)
     info = solve_and_check(gbx, cuda, A, N, NB, 8, prec, kappa=10.0)
-    assert info["iterations"] <= 10, info
+    print("dposv_mixed %s kappa~10: %s" % (prec, info))
+    assert info["iterations"] <= (40 if prec == "fp8" else 10), info
 
 
 @pytest.mark.parametrize("kappa,prec", [(1e4, "bf16"), (1e6, "bf16"), (1e6, "fp16")])
@@ -106,7 +109,7 @@ def batch_dense(A, sizes, NB, k):
     return dense_from_tiles(t, n, NB)
 
 
-@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+@pytest.mark.parametrize("prec", ["fp16", "bf16", "fp8"])
 def test_dposv_mixed_batched_uneven(gbx, cuda, prec):
     """Uneven (ragged) orders in one batch, kappa = 1e4: every matrix to backward error 1e-14, and the
     factor of each matrix equal to the single-matrix launch's factor bit for bit (same tile order)."""

@@ -20,7 +20,7 @@ GBX_ERR_TIMEOUT = -3
 GBX_ERR_WORKSPACE = -4
 GBX_ERR_NOCONV = -5
 GBX_ERR_NOALLOC_LIMIT = -6
-PREC = {"bf16": 0, "fp16": 1}
+PREC = {"bf16": 0, "fp16": 1, "fp8": 2}
 
 _ERRNAMES = {GBX_ERR_ARG: "invalid argument", GBX_ERR_CUDA: "CUDA runtime error",
              GBX_ERR_TIMEOUT: "device-side wait timed out", GBX_ERR_WORKSPACE: "workspace too small",

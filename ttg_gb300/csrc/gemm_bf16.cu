@@ -158,6 +158,22 @@ int make_tmap_kmajor_16b(CUtensorMap* map, const void* base, uint64_t rows, uint
   return r == CUDA_SUCCESS ? GBX_OK : GBX_ERR_ARG;
 }
 
+// 8-bit (fp8) K-major operand: `rows` rows of `k` one-byte elements, row stride `ld` bytes; box
+// 128 x box_rows (128-byte rows, the same swizzled layout as the 16-bit box of 64)
+int make_tmap_kmajor_8b(CUtensorMap* map, const void* base, uint64_t rows, uint64_t k, uint64_t ld, uint32_t box_rows) {
+  auto enc = encode_fn();
+  if (!enc) return GBX_ERR_CUDA;
+  if (((uintptr_t)base & 15) || (ld & 15) || rows == 0 || k == 0) return GBX_ERR_ARG;
+  cuuint64_t dims[2] = {k, rows};
+  cuuint64_t strides[1] = {ld};
+  cuuint32_t box[2] = {128, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? GBX_OK : GBX_ERR_ARG;
+}
+
 }  // namespace tc
 }  // namespace gbx
 

@@ -14,6 +14,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +30,7 @@ namespace gbx {
 namespace tc {
 int make_tmap_kmajor_16b(CUtensorMap* map, const void* base, uint64_t rows, uint64_t k, uint64_t ld, uint32_t box_rows,
                          bool bf16);
+int make_tmap_kmajor_8b(CUtensorMap* map, const void* base, uint64_t rows, uint64_t k, uint64_t ld, uint32_t box_rows);
 }
 
 namespace mixed {
@@ -113,7 +115,8 @@ struct Params {
   void* Lb;  // bf16 or fp16, row-major per tile
   int* rowexp;
   int NB;
-  int f16;     // 1: fp16 operands, 0: bf16
+  int f16;     // 1: fp16 operands, 0: bf16 (or fp8, below)
+  int fp8;     // 1: fp8 e4m3 operands (row-major, one byte per entry, rows scaled into [128, 256))
   int sub_g;   // GEMM sub-tasks per tile = (NB/128)*(NB/256)
   int sub_t;   // TRSM sub-tasks per tile = NB/64
   int nb;      // 128-blocks per tile edge (the diagonal tile's POTRF is a mini flowgraph of them)
@@ -353,6 +356,7 @@ __device__ void task_trsm(const Params& P, const Cur& cm, int M, int K, int rb, 
   mx = fmaxf(fmaxf(s_q_max[r], s_q_max[r + 64]), fmaxf(s_q_max[r + 128], s_q_max[r + 192]));
   int e = 0;
   if (mx > 0.f) frexpf(mx, &e);  // mx * 2^-e in [0.5, 1)
+  if (P.fp8) e -= 8;              // fp8: the row into [128, 256), inside e4m3's range (448)
   const float inv = pow2f(-e);
   if (r < m) {
     const long long base = sM * (long long)NB * NB + (long long)(r0 + r) * NB;
@@ -360,6 +364,15 @@ __device__ void task_trsm(const Params& P, const Cur& cm, int M, int K, int rb, 
       float v[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) v[j] = (c0 + j < n) ? Bs[(c0 + j) * kTrsmRows + r] * inv : 0.f;
+      if (P.fp8) {  // one byte per entry, rows of NB bytes
+        uint2 p8;
+        uint16_t* w8 = (uint16_t*)&p8;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          w8[j] = __nv_cvt_float2_to_fp8x2(make_float2(v[2 * j], v[2 * j + 1]), __NV_SATFINITE, __NV_E4M3);
+        *(uint2*)((uint8_t*)P.Lb + base + c0) = p8;
+        continue;
+      }
       uint4 pk;
       uint32_t* w = (uint32_t*)&pk;
       if (P.f16) {
@@ -406,7 +419,8 @@ __global__ void __launch_bounds__(kThr, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
   const int NB = P.NB;
-  const int nkb = NB / kBK;
+  const int kbk = P.fp8 ? 2 * kBK : kBK;  // elements per 128-byte operand row of a stage
+  const int nkb = NB / kbk;
   uint32_t prod_it = 0, cons_it = 0, acc_phase = 0;  // pipeline positions, identical in every role
   int* err = &P.st->status;
 
@@ -559,11 +573,11 @@ __global__ void __launch_bounds__(kThr, 1)
           if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1, err, P.timeout_ns)) break;
           const uint32_t dst = smem_u32(smem + (size_t)s * kStageBytes);
           mbar_arrive_expect_tx(smem_u32(&full_bar[s]), kStageBytes);
-          tma_load_2d(dst, &tmA, smem_u32(&full_bar[s]), kb * kBK, (int)(sA * NB + r0));
-          tma_load_2d(dst + kABytes, &tmB, smem_u32(&full_bar[s]), kb * kBK, (int)(sB * NB + c0));
+          tma_load_2d(dst, &tmA, smem_u32(&full_bar[s]), kb * kbk, (int)(sA * NB + r0));
+          tma_load_2d(dst + kABytes, &tmB, smem_u32(&full_bar[s]), kb * kbk, (int)(sB * NB + c0));
         }
       } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = idesc_f16(kSubM, kSubN, !P.f16);
+        const uint32_t idesc = idesc_f16(kSubM, kSubN, !P.f16 && !P.fp8);  // e4m3: format fields 0 as for fp16
         for (int kb = 0; kb < nkb; ++kb, ++cons_it) {
           const int s = cons_it % kStages;
           const uint32_t ph = (cons_it / kStages) & 1;
@@ -571,8 +585,14 @@ __global__ void __launch_bounds__(kThr, 1)
           tc_fence_after();
           const uint32_t a_base = smem_u32(smem + (size_t)s * kStageBytes);
           const uint64_t ad = desc_kmajor_sw128(a_base), bd = desc_kmajor_sw128(a_base + kABytes);
+          // four instructions per 128-byte stage row: K = 16 (16-bit) or 32 (fp8), 32 bytes each
+          if (P.fp8) {
 #pragma unroll
-          for (int k = 0; k < kBK / 16; ++k) umma_f16(tmem, ad + 2 * k, bd + 2 * k, idesc, (kb | k) != 0 ? 1u : 0u);
+            for (int k = 0; k < 4; ++k) umma_f8(tmem, ad + 2 * k, bd + 2 * k, idesc, (kb | k) != 0 ? 1u : 0u);
+          } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) umma_f16(tmem, ad + 2 * k, bd + 2 * k, idesc, (kb | k) != 0 ? 1u : 0u);
+          }
           umma_commit(smem_u32(&empty_bar[s]));
         }
         umma_commit(smem_u32(&done_bar));
@@ -844,16 +864,21 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
   }
   CUtensorMap ta, tb;
   const bool bf16 = prec == 0;
-  if (int e = tc::make_tmap_kmajor_16b(&ta, base + w.lb, (uint64_t)w.slots * NB, (uint64_t)NB, (uint64_t)NB, kSubM, bf16))
-    return e;
-  if (int e = tc::make_tmap_kmajor_16b(&tb, base + w.lb, (uint64_t)w.slots * NB, (uint64_t)NB, (uint64_t)NB, kSubN, bf16))
-    return e;
+  const uint64_t lrows = (uint64_t)w.slots * NB;
+  if (prec == 2) {  // fp8: rows of NB bytes in the same buffer
+    if (int e = tc::make_tmap_kmajor_8b(&ta, base + w.lb, lrows, (uint64_t)NB, (uint64_t)NB, kSubM)) return e;
+    if (int e = tc::make_tmap_kmajor_8b(&tb, base + w.lb, lrows, (uint64_t)NB, (uint64_t)NB, kSubN)) return e;
+  } else {
+    if (int e = tc::make_tmap_kmajor_16b(&ta, base + w.lb, lrows, (uint64_t)NB, (uint64_t)NB, kSubM, bf16)) return e;
+    if (int e = tc::make_tmap_kmajor_16b(&tb, base + w.lb, lrows, (uint64_t)NB, (uint64_t)NB, kSubN, bf16)) return e;
+  }
   Params P;
   P.W = W;
   P.Lb = base + w.lb;
   P.rowexp = (int*)(base + w.rowexp);
   P.NB = NB;
   P.f16 = prec == 1;
+  P.fp8 = prec == 2;
   P.sub_g = sub_g;
   P.sub_t = sub_t;
   P.nb = nb;
@@ -885,7 +910,7 @@ extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes) {
 
 extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work,
                                size_t work_bytes, void* stream) {
-  if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !A || !W || !work || (prec != 0 && prec != 1))
+  if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !A || !W || !work || prec < 0 || prec > 2)
     return GBX_ERR_ARG;
   return launch_batch(1, &N, NB, A, W, prec, shift, nullptr, work, work_bytes, (cudaStream_t)stream, false);
 }
@@ -903,7 +928,7 @@ extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const do
                                        void* stream) {
   size_t need = 0;
   if (int e = gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &need)) return e;
-  if (!A || !W || !work || (prec != 0 && prec != 1)) return GBX_ERR_ARG;
+  if (!A || !W || !work || prec < 0 || prec > 2) return GBX_ERR_ARG;
   return launch_batch(batch, n, NB, A, W, prec, shift, sel, work, work_bytes, (cudaStream_t)stream, false);
 }
 

@@ -1265,7 +1265,7 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
                                        size_t work_bytes, gbx_refine_info* info, void* stream) {
   size_t need = 0;
   if (int e = gbx_dposv_mixed_batched_bufferSize(batch, n, NB, nrhs, &need)) return e;
-  if (!A || !B || !X || !W || !work || maxiter < 0 || (prec != 0 && prec != 1)) return GBX_ERR_ARG;
+  if (!A || !B || !X || !W || !work || maxiter < 0 || prec < 0 || prec > 2) return GBX_ERR_ARG;
   if (work_bytes < need) return GBX_ERR_WORKSPACE;
   if (int e = set_attrs()) return e;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1349,7 +1349,8 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
       }
     }
     if (!any) break;
-    shift = shift == 0.0 ? (prec == 1 ? 1.0 / 2048 : 1.0 / 256) : shift * 4;
+    // first shift about the operands' unit roundoff: fp16 2^-11, bf16 2^-8, fp8 e4m3 2^-4
+    shift = shift == 0.0 ? (prec == 1 ? 1.0 / 2048 : prec == 2 ? 1.0 / 32 : 1.0 / 256) : shift * 4;
   }
   for (int k = 0; k < batch; ++k) inf[k].cond_estimate = cond[k];
   bool factored = true;
