@@ -17,7 +17,7 @@ Metric: effective TFLOP/s = (N^3/3) / (factor + solve time), higher is better.
 
 --impl reference times that CPU restatement (the reference's own PaRSEC build is not available)
 on the same metric. Under torchrun every rank runs an independent replica ("replicas only":
-the tiled factorisation of one matrix on one GPU has no data-parallel split in this build).
+the tiled factorisation of one matrix runs on one GPU; its tiles are not split across GPUs).
 """
 import argparse
 import json

@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle — TEST INFRASTRUCTURE ONLY.
 
-Imported by the tests, by `__graft_entry__.smoke()` (as the checker) and by the CPU-baseline
+Imported by the tests, by `__graft_entry__.smoke()` (for the expected result) and by the CPU-baseline
 leg of `bench.py`. The product path never imports this package.
 """
 import ctypes

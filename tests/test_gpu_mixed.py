@@ -2,9 +2,9 @@
 refinement), through the C ABI.
 
 Tolerances:
-  * factor: max |W - L64| / max |L64| <= 3e-2 (bf16 operands, unit roundoff 2^-8 x growth) and
-    <= 4e-3 (fp16, 2^-11), L64 from the CPU oracle;
-  * solve: the spec bar, normwise backward error max_j ||b_j - A x_j||_inf /
+  * factor: max |W - L64| / max |L64| <= 3e-2 (bf16 operands, unit roundoff 2^-8 x growth),
+    <= 4e-3 (fp16, 2^-11) and <= 0.25 (fp8 e4m3, 2^-4), L64 from the CPU oracle;
+  * solve: the target accuracy, normwise backward error max_j ||b_j - A x_j||_inf /
     (||A||_inf ||x_j||_inf + ||b_j||_inf) <= 1e-14, and the forward error against an FP64 solve of
     the same system bounded by kappa(A) * 1e-14.
 """

@@ -29,7 +29,7 @@ def householder_factors(N, r, kappa, seed=42):
 
 
 def householder_dense(N, r, kappa, seed=42):
-    """The same matrix built by applying the reflectors one by one (checker for small N)."""
+    """The same matrix built by applying the reflectors one by one (a cross-check for small N)."""
     rng = np.random.default_rng(seed)
     V = rng.standard_normal((N, r))
     lam = float(kappa) ** (-np.arange(N, dtype=np.float64) / max(N - 1, 1))
