@@ -1055,9 +1055,6 @@ __device__ void colstats_body(const double* a, const double* b, int N, double* o
     out[j * 3 + 2] = s_mb[0];
   }
 }
-__global__ void colstats_kernel(const double* a, const double* b, int N, int nrhs, double* out) {
-  colstats_body(a, b, N, out);
-}
 // out: [matrix id][kMaxRhs][3]; `ncols` columns per matrix (nrhs, or 1 for the row-sum vector,
 // whose vectors are at vec0 / nrhs)
 __global__ void colstats_batched(const RMat* mats, const int* list, const double* a, const double* b, int nrhs,
@@ -1078,10 +1075,6 @@ __device__ void axpy_cols_body(double* y, const double* x, const double* coef, d
     else if (xscale_mode == 1) y[i] = x[i] + coef[j] * y[i];  // y = x + c*y
     else y[i] = 0.0;                                          // y = 0
   }
-}
-__global__ void axpy_cols_kernel(double* y, const double* x, const double* coef, double sign, int N, int nrhs,
-                                 int xscale_mode) {
-  axpy_cols_body(y, x, coef, sign, N, nrhs, xscale_mode);
 }
 // coef: [matrix id][kMaxRhs]
 __global__ void axpy_cols_batched(const RMat* mats, const int* list, double* y, const double* x, const double* coef,
