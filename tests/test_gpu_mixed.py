@@ -208,3 +208,18 @@ def test_dposv_mixed_batched_reports_non_spd_member(gbx, cuda):
     assert st == gbx.GBX_ERR_NOCONV
     assert infos[1]["backward_error"] == float("inf") and infos[1]["factor_retries"] == 8
     assert infos[0]["backward_error"] <= 1e-14 and infos[2]["backward_error"] <= 1e-14
+
+
+def test_tune_mixed_batched_picks_a_converged_configuration(gbx, cuda):
+    """The tile-size / precision tuner times all six candidates (fp16, bf16, fp8 at NB 256 and 512,
+    the 256 tiles made from the 512 ones on the device) and returns the fastest converged one."""
+    from ttg_gb300 import autotune
+    NB, nrhs = 512, 2
+    sizes = np.array([700, 300, 1300])
+    A, B = workloads.householder_batch(sizes, NB, 2, 1e3, 5, cuda, nrhs=nrhs)
+    best = autotune.tune_mixed_batched(A, sizes, NB, B, nrhs, tol=1e-14, use_cache=False)
+    assert best["ok"] and best["status"] == 0 and best["backward_error_max"] <= 1e-14, best
+    assert {(c["prec"], c["NB"]) for c in best["candidates"]} == {(p, nb) for p in ("fp16", "bf16", "fp8")
+                                                                 for nb in (256, 512)}
+    assert best["ms"] == min(c["ms"] for c in best["candidates"] if c["ok"])
+    assert sum(c["ok"] for c in best["candidates"]) >= 4, best["candidates"]

@@ -1,11 +1,18 @@
-"""Autotuner of the batched persistent solver (gbx_dposv_batched_ex).
+"""Autotuners of the batched solvers.
 
-For one batch (its size mix) it times every candidate of
+tune_batched (small systems, gbx_dposv_batched_ex): for one batch (its size mix) it times every
+candidate of
   * precision split: FP64, or FP32 factor + 1 or 2 FP64 refinement steps,
   * CTA schedule: queue order largest-first (longest processing time), natural, or
     interleaved large/small; and the number of CTAs (1 or 2 per SM for FP32, 1 per SM for FP64),
 keeps the candidates whose sampled backward error meets the tolerance, and returns the fastest.
-The choice is cached per (GPU, size histogram, nrhs, tolerance) in a JSON file next to this module.
+
+tune_mixed_batched (tiled systems, gbx_dposv_mixed_batched): times every tile size (256, 512) and
+tensor-core operand precision (fp16, bf16, fp8-e4m3) of the mixed solve on the batch, keeps the
+candidates with which every matrix met the tolerance, and returns the fastest. The tiles of the
+other tile sizes are made on the device by `retile`.
+
+Choices are cached per (GPU, size histogram, nrhs, tolerance) in a JSON file next to this module.
 """
 import hashlib
 import json
@@ -92,6 +99,105 @@ def tune_batched(batch, rhs, tol=1e-14, reps=2, use_cache=True, sample_every=97)
     best = dict(min(ok, key=lambda c: c["ms"]))
     best["candidates"] = cands
     batch.set_order(orders[best["schedule"]])
+    if use_cache:
+        cache[key] = best
+        try:
+            json.dump(cache, open(_CACHE, "w"), indent=1)
+        except OSError:
+            pass
+    return best
+
+
+# ---- tiled batches: tile size and operand precision of the mixed solver ----------------------
+
+def _lower_index(n, NB, device):
+    """Tile-storage offsets of the lower triangle (i >= j) of an n x n matrix, row-major over (i, j)."""
+    import torch
+    NT = (n + NB - 1) // NB
+    i, j = torch.tril_indices(n, n, device=device)
+    ti, tj = i // NB, j // NB
+    slot = tj * NT - tj * (tj - 1) // 2 + (ti - tj)
+    return slot * NB * NB + (i % NB) + (j % NB) * NB
+
+
+def retile(A, sizes, NB_from, NB_to):
+    """The concatenated tile-major lower matrices of a batch (ttg_gb300.batched_tile_offsets layout)
+    re-laid for another tile size, on A's device: the lower triangle is moved, everything else
+    (strict upper parts of diagonal tiles, padding) is zero."""
+    import torch
+    from . import batched_tile_offsets
+    if NB_from == NB_to:
+        return A
+    off1, _ = batched_tile_offsets(sizes, NB_from)
+    off2, total2 = batched_tile_offsets(sizes, NB_to)
+    out = torch.zeros(total2, dtype=A.dtype, device=A.device)
+    for k, n in enumerate(sizes):
+        n = int(n)
+        src = _lower_index(n, NB_from, A.device) + int(off1[k])
+        dst = _lower_index(n, NB_to, A.device) + int(off2[k])
+        out[dst] = A[src]
+    return out
+
+
+def select_mixed(run, candidates, tol):
+    """Runs `run(prec, NB)` for every candidate (it returns a dict with "ms", "status" and
+    "backward_error_max"), and returns the fastest candidate with status 0 and backward error
+    within tol, with every result under "candidates". Raises if none qualifies."""
+    results = []
+    for prec, nb in candidates:
+        r = dict(run(prec, nb))
+        r.update(prec=prec, NB=nb)
+        r["ok"] = bool(r["status"] == 0 and r["backward_error_max"] <= tol)
+        results.append(r)
+    ok = [r for r in results if r["ok"]]
+    if not ok:
+        raise RuntimeError("no candidate of the mixed solver met the tolerance %g" % tol)
+    best = dict(min(ok, key=lambda r: r["ms"]))
+    best["candidates"] = results
+    return best
+
+
+def tune_mixed_batched(A, sizes, NB, B, nrhs, tol=1e-14, precs=("fp16", "bf16", "fp8"), NBs=(256, 512), maxiter=300,
+                       reps=1, use_cache=True):
+    """Tile size and operand precision for gbx_dposv_mixed_batched on this batch (A: its tiles at
+    tile size NB on the device, B: its right-hand sides). Returns {"prec", "NB", "ms", ...,
+    "candidates": [...]}; the solution of the chosen candidate is not kept."""
+    import torch
+    from . import dposv_mixed_batched
+    sizes = np.asarray(sizes)
+    hist = np.bincount(sizes.astype(np.int64), minlength=1).tobytes()
+    key = "mixed|%s|%s|%d|%g" % (torch.cuda.get_device_name(), hashlib.sha1(hist).hexdigest()[:16], nrhs, tol)
+    cache = {}
+    if use_cache and os.path.exists(_CACHE):
+        try:
+            cache = json.load(open(_CACHE))
+        except (OSError, ValueError):
+            cache = {}
+    if use_cache and key in cache:
+        return cache[key]
+    tiles = {NB: A}
+
+    def run(prec, nb):
+        if nb not in tiles:
+            tiles[nb] = retile(A, sizes, NB, nb)
+        At = tiles[nb]
+        W = torch.empty(At.numel(), dtype=torch.float32, device=At.device)
+        X, infos, st = dposv_mixed_batched(At, sizes, nb, B, nrhs, prec=prec, tol=tol, maxiter=maxiter, W=W)
+        times = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            X, infos, st = dposv_mixed_batched(At, sizes, nb, B, nrhs, prec=prec, tol=tol, maxiter=maxiter, W=W)
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return {"ms": float(np.mean(times)), "status": int(st),
+                "backward_error_max": float(max(i["backward_error"] for i in infos)),
+                "iterations_max": int(max(i["iterations"] for i in infos)),
+                "factor_retries": int(sum(i["factor_retries"] for i in infos))}
+
+    best = select_mixed(run, [(p, nb) for nb in NBs for p in precs], tol)
     if use_cache:
         cache[key] = best
         try:
