@@ -220,7 +220,6 @@ def run_ours(args, ws, rank, local):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     N, NB, nrhs = args.N, args.NB, args.nrhs
-    NTb = (N + min(NB, 128) - 1) // min(NB, 128) if NB > 128 else (N + NB - 1) // NB
     numel = gbx.tiled_numel(N, NB)
     A0 = torch.empty(numel, dtype=torch.float64, device=dev)
     T = torch.empty_like(A0)
@@ -231,7 +230,7 @@ def run_ours(args, ws, rank, local):
     work = torch.empty(gbx.potrf_workspace_bytes(N, NB), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
-    launches_per_step = 1 + 2 * (2 * NTb - 1)
+    launches_per_step = 3  # potrf_dag_f64_kernel, then the two persistent solve sweeps (forward, backward)
 
     def step(events):
         e0, e1, e2 = events
