@@ -306,6 +306,16 @@ int gbx_dposv_batched_ex(int batch, const int* n, const long long* offA, const l
 int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_bytes, uint64_t timeout_ns,
                              void* stream);
 
+/* The task orders the persistent executors follow (host-side introspection, no GPU needed): task t
+ * of gbx_dpotrf_tiled's order over NTb x NTb blocks, and of the mixed factorisation's order over
+ * NT x NT tiles, written to key[4] = {type, a, b, c}: type 0 POTRF of block (a,a); 1 TRSM of
+ * block (a,b) by the factor of (b,b); 2 SYRK of block (b,b) with column a; 3 GEMM of block (a,b)
+ * with column c. Each returns the number of tasks in the order (t and key are ignored when
+ * t < 0), or GBX_ERR_ARG. The orders are the executors' task lists, in which every task's
+ * predecessors come earlier, so CTAs that take tasks in order cannot deadlock. */
+long long gbx_dag_task(int NTb, long long t, int* key);
+long long gbx_mixed_task(int NT, long long t, int* key);
+
 #ifdef __cplusplus
 }
 #endif

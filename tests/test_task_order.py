@@ -1,0 +1,71 @@
+"""The task orders of the persistent executors (CPU, through the C ABI's host-side decode):
+gbx_dpotrf_tiled's block order and the mixed factorisation's tile order. Each must list every
+task of the right-looking tiled Cholesky exactly once, and every task's predecessors before it,
+which is what lets CTAs take tasks in order and wait on their predecessors without deadlock:
+  POTRF(k)     after SYRK(j, k) for all j < k   (every update of the diagonal block)
+  TRSM(m, k)   after POTRF(k) and GEMM(m, k, j) for all j < k
+  SYRK(k, n)   after TRSM(n, k) and SYRK(k-1, n)
+  GEMM(m,n,k)  after TRSM(m, k), TRSM(n, k) and GEMM(m, n, k-1)
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+POTRF, TRSM, SYRK, GEMM = 0, 1, 2, 3
+
+
+def _order(gbx, fn, nt):
+    key = np.zeros(4, dtype=np.int32)
+    n = gbx.call(fn, nt, -1, None)
+    out = []
+    for t in range(n):
+        gbx.call(fn, nt, t, key.ctypes.data_as(ctypes.c_void_p))
+        out.append(tuple(int(v) for v in key))
+    return out
+
+
+def _expected(nt):
+    tasks = set()
+    for k in range(nt):
+        tasks.add((POTRF, k, 0, 0))
+        for m in range(k + 1, nt):
+            tasks.add((TRSM, m, k, 0))
+            tasks.add((SYRK, k, m, 0))
+            for n in range(k + 1, m):
+                tasks.add((GEMM, m, n, k))
+    return tasks
+
+
+def _deps(task):
+    ty, a, b, c = task
+    if ty == POTRF:
+        return [(SYRK, j, a, 0) for j in range(a)]
+    if ty == TRSM:
+        return [(POTRF, b, 0, 0)] + [(GEMM, a, b, j) for j in range(b)]
+    if ty == SYRK:
+        return [(TRSM, b, a, 0)] + ([(SYRK, a - 1, b, 0)] if a > 0 else [])
+    return [(TRSM, a, c, 0), (TRSM, b, c, 0)] + ([(GEMM, a, b, c - 1)] if c > 0 else [])
+
+
+@pytest.mark.parametrize("fn", ["gbx_dag_task", "gbx_mixed_task"])
+@pytest.mark.parametrize("nt", [1, 2, 3, 5, 8, 17, 33])
+def test_order_is_complete_and_topological(gbx, fn, nt):
+    order = _order(gbx, fn, nt)
+    assert len(order) == len(set(order)), "a task appears twice"
+    assert set(order) == _expected(nt)
+    pos = {t: i for i, t in enumerate(order)}
+    for t, i in pos.items():
+        for d in _deps(t):
+            assert pos[d] < i, (t, d)
+
+
+@pytest.mark.parametrize("fn", ["gbx_dag_task", "gbx_mixed_task"])
+def test_order_argument_checks(gbx, fn):
+    L = gbx.lib()
+    key = (ctypes.c_int * 4)()
+    assert getattr(L, fn)(0, -1, None) == gbx.GBX_ERR_ARG
+    n = getattr(L, fn)(4, -1, None)
+    assert n == len(_expected(4))
+    assert getattr(L, fn)(4, n, key) == gbx.GBX_ERR_ARG
+    assert getattr(L, fn)(4, 0, None) == gbx.GBX_ERR_ARG

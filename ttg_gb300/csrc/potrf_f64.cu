@@ -598,6 +598,20 @@ using namespace gbx;
 
 extern "C" {
 
+long long gbx_dag_task(int NTb, long long t, int* key) {
+  if (NTb <= 0) return GBX_ERR_ARG;
+  const long long n = dag_num_tasks(NTb);
+  if (t >= n || (t >= 0 && !key)) return GBX_ERR_ARG;
+  if (t >= 0) {
+    const TaskKey k = dag_decode(t, NTb);
+    key[0] = k.type;
+    key[1] = k.a;
+    key[2] = k.b;
+    key[3] = k.c;
+  }
+  return n;
+}
+
 int gbx_version(void) { return 100; }
 int gbx_built_arch(void) {
 #if defined(GBX_ARCH)

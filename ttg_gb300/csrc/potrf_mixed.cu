@@ -902,6 +902,20 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
 }  // namespace mixed
 }  // namespace gbx
 
+extern "C" long long gbx_mixed_task(int NT, long long t, int* key) {
+  if (NT <= 0) return GBX_ERR_ARG;
+  const long long n = num_tile_tasks(NT);
+  if (t >= n || (t >= 0 && !key)) return GBX_ERR_ARG;
+  if (t >= 0) {
+    const TileKey k = decode(t, NT);
+    key[0] = k.type;
+    key[1] = k.a;
+    key[2] = k.b;
+    key[3] = k.c;
+  }
+  return n;
+}
+
 extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes) {
   if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !bytes) return GBX_ERR_ARG;
   *bytes = layout(N, NB).total;
