@@ -54,6 +54,17 @@ def test_argument_validation_without_gpu(gbx):
     assert L.gbx_dgemm_nt_tile(10, 10, 10, None, 5, None, 10, None, 10, None) == gbx.GBX_ERR_ARG
     assert L.gbx_dtrsm_rlt_tile(10, 10, None, 10, None, 5, None) == gbx.GBX_ERR_ARG
     assert L.gbx_dpotrs_tiled(100, 32, None, 1, None, 50, None) == gbx.GBX_ERR_ARG
+    # split: negative count, missing pointers; an empty split does nothing
+    assert L.gbx_split_f64(None, None, None, -1, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_split_f64(None, None, None, 8, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_split_f64(None, None, None, 0, None) == 0
+    # mixed solvers: operand precision 0 (bf16), 1 (fp16) or 2 (fp8 e4m3); NB 256 or 512
+    dummy = ctypes.c_void_p(16)
+    assert L.gbx_potrf_mixed(1000, 256, dummy, dummy, 3, ctypes.c_double(0.0), dummy, 1 << 30, None) == \
+        gbx.GBX_ERR_ARG
+    assert L.gbx_potrf_mixed(1000, 768, dummy, dummy, 0, ctypes.c_double(0.0), dummy, 1 << 30, None) == \
+        gbx.GBX_ERR_ARG
+    assert L.gbx_potrf_mixed_bufferSize(1000, 1024, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
 
 
 def test_wait_timeout_setting(gbx):
