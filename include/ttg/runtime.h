@@ -384,8 +384,26 @@ inline void ttg_finalize() { finalize(); }
 inline void ttg_execute(World& w) { execute(w); }
 inline void ttg_fence(World& w) { fence(w); }
 
-/// The reference aborts the whole job here (MPI_Abort); a library cannot, so this throws.
-[[noreturn]] inline void abort() { throw std::runtime_error("ttg::abort() called"); }
+/// The reference aborts the whole job here (MPI_Abort). By default a library cannot, so this
+/// throws (the error then surfaces from ttg::fence). Opt-in, reference-faithful mode:
+/// set_abort_terminates(true), or the environment variable TTG_ABORT_TERMINATES=1, makes it end
+/// the process with std::abort().
+inline bool& abort_terminates_flag() {
+  static bool flag = [] {
+    const char* e = std::getenv("TTG_ABORT_TERMINATES");
+    return e != nullptr && e[0] == '1';
+  }();
+  return flag;
+}
+inline void set_abort_terminates(bool on) { abort_terminates_flag() = on; }
+inline bool abort_terminates() { return abort_terminates_flag(); }
+[[noreturn]] inline void abort() {
+  if (abort_terminates()) {
+    std::fputs("ttg::abort() called\n", stderr);
+    std::abort();
+  }
+  throw std::runtime_error("ttg::abort() called");
+}
 [[noreturn]] inline void ttg_abort() { abort(); }
 
 }  // namespace ttg

@@ -50,6 +50,16 @@ def test_host_task_semantics():
     assert rc == 0 and "ALL PASS" in out, out
 
 
+def test_abort_is_opt_in_process_termination():
+    """ttg::abort() throws by default; with set_abort_terminates(true) (the reference-faithful mode)
+    it ends the process with SIGABRT, as the reference's abort on a non-SPD pivot does."""
+    import signal
+    exe = _build(os.path.join(CPP, "host_tt.cc"), "host_tt")
+    rc, out = _run([exe, "abort"], timeout=120)
+    assert rc == -signal.SIGABRT, (rc, out)
+    assert "PASS abort-throws" in out and "ttg::abort() called" in out and "ALL PASS" not in out
+
+
 def _ref_bins():
     bins = obuild.build_ref_flowgraph()
     if bins is None:

@@ -167,6 +167,23 @@ int main(int argc, char** argv) {
     std::puts("PASS priorities");
     ttg::finalize();
   }
+  {  // ttg::abort(): throws by default (the error surfaces from fence); the opt-in reference-faithful
+     // mode ends the process, checked by the test driver in a child process (argument "abort")
+    REQUIRE(!ttg::abort_terminates());
+    bool thrown = false;
+    try {
+      ttg::abort();
+    } catch (const std::runtime_error&) {
+      thrown = true;
+    }
+    REQUIRE(thrown);
+    std::puts("PASS abort-throws");
+    if (argc > 1 && std::string(argv[1]) == "abort") {
+      ttg::set_abort_terminates(true);
+      std::fflush(stdout);
+      ttg::abort();  // does not return
+    }
+  }
   std::puts("ALL PASS");
   return 0;
 }

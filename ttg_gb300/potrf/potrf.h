@@ -5,10 +5,12 @@
 // 449-457, 578-586 and the DPLASMA priorities of potrf.h:742-752 — with each device body calling
 // this project's sm_103a tile kernels (include/gbx_potrf.h) on ttg::device::current_stream()
 // where the reference calls cuSOLVER/cuBLAS. A failing pivot raises potrf::NotPositiveDefinite
-// from ttg::fence instead of aborting the process (the reference calls ttg::abort()).
+// from ttg::fence instead of aborting the process (the reference calls ttg::abort()); with
+// ttg::set_abort_terminates(true) (or TTG_ABORT_TERMINATES=1) it ends the process as the reference does.
 #pragma once
 #include <ttg.h>
 
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -59,7 +61,13 @@ auto make_potrf(MatrixT& A, ttg::Edge<Key1, MatrixTile<double>>& from_dispatch, 
                                  lwork, info.device_ptr(), ttg::device::current_stream()),
                  "gbx_dpotrf_tile");
     co_await ttg::device::wait(info);
-    if (host_info != 0) throw NotPositiveDefinite(K, host_info);
+    if (host_info != 0) {
+      if (ttg::abort_terminates()) {  // reference-faithful mode: end the process (potrf.h:184-186)
+        std::fprintf(stderr, "POTRF(%d) failed: info %d\n", K, host_info);
+        ttg::abort();
+      }
+      throw NotPositiveDefinite(K, host_info);
+    }
     co_await ttg::device::forward(
         ttg::device::broadcast<0, 1>(std::make_tuple(Key2(K, K), std::move(trsm_keys)), std::move(tile), out));
   };
