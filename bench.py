@@ -322,8 +322,39 @@ def run_ours(args, ws, rank, local):
                                 "cores": cpu_cores(), "kind": "port",
                                 "sample": "N=%d NB=%d factor+solve, best of 2, %s tile kernels" %
                                           (args.cpu_N, NB, "OpenBLAS" if blas else "plain-loop")}
+    bf16_peak, bf16_src = measured_bf16_peak()
+    add_roofline_fractions(line, peak, bf16_peak)
+    line["peaks"]["bf16_source"] = bf16_src
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def measured_bf16_peak():
+    """Dense bf16 tensor-core rate from MEASURED_PEAKS.json (burst), else the fallback figure."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (burst)"
+    except (OSError, ValueError, KeyError, TypeError):
+        return 1900.0, "fallback 1.9 PFLOP/s bf16"
+
+
+def add_roofline_fractions(line, fp64_peak, bf16_peak):
+    """Adds `frac_of_peak` beside every `tflops` of the secondary configurations: FP64 results against
+    the FP64 GEMM rate measured in the run, bf16/fp16 results against the dense bf16 tensor-core
+    rate, fp8 against twice it (the nominal fp8:bf16 ratio; no fp8 rate is measured). FP32 results
+    (CUDA cores) get none."""
+    peaks = {"fp64": fp64_peak, "plain_fp64": fp64_peak, "plain_fp64_per_matrix": fp64_peak, "gpu": fp64_peak,
+             "bf16": bf16_peak, "fp16": bf16_peak, "fp8": 2.0 * bf16_peak}
+    for sec in ("mixed", "batched", "batched_mixed", "config_small", "potri"):
+        part = line.get(sec)
+        if not isinstance(part, dict):
+            continue
+        for key, res in part.items():
+            if key in peaks and isinstance(res, dict) and isinstance(res.get("tflops"), (int, float)):
+                res["frac_of_peak"] = res["tflops"] / peaks[key]
+    line["peaks"] = {"fp64_tflops": fp64_peak, "bf16_tflops": bf16_peak,
+                     "fp8_tflops": 2.0 * bf16_peak, "note": "fp8 = twice the bf16 rate (nominal ratio)"}
+    return line
 
 
 def backward_error(gbx, A0, T, X, b0, N, NB, dev):

@@ -1,0 +1,35 @@
+"""Host-side helpers of bench.py (CPU): the roofline fractions added to the secondary
+configurations of the JSON line."""
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def test_roofline_fractions_of_secondary_configurations():
+    line = {
+        "mixed": {"config": {}, "plain_fp64": {"ms": 1.0, "tflops": 1.1}, "bf16": {"tflops": 19.0},
+                  "fp16": {"tflops": 95.0}},
+        "batched": {"config": {}, "fp64": {"tflops": 0.5}, "fp32": {"tflops": 3.3},
+                    "cpu_baseline": {"value": 1.0}},
+        "batched_mixed": {"config": {}, "plain_fp64_per_matrix": {"tflops": 0.2}, "fp16": {"tflops": 18.7},
+                          "bf16": {"tflops": 15.9}, "fp8": {"tflops": 11.0}},
+        "config_small": {"gpu": {"tflops": 0.17}, "cpu_baseline": {"value": 0.4}},
+        "potri": {"gpu": {"tflops": 0.67}},
+    }
+    bench.add_roofline_fractions(line, 1.1, 1928.0)
+    assert abs(line["mixed"]["plain_fp64"]["frac_of_peak"] - 1.0) < 1e-12
+    assert abs(line["mixed"]["fp16"]["frac_of_peak"] - 95.0 / 1928.0) < 1e-12
+    assert abs(line["batched_mixed"]["fp8"]["frac_of_peak"] - 11.0 / 3856.0) < 1e-12
+    assert abs(line["potri"]["gpu"]["frac_of_peak"] - 0.67 / 1.1) < 1e-12
+    assert "frac_of_peak" not in line["batched"]["fp32"]           # CUDA-core FP32: no tensor roofline
+    assert "frac_of_peak" not in line["batched"]["cpu_baseline"]
+    assert line["peaks"]["fp8_tflops"] == 3856.0
+
+
+def test_measured_bf16_peak_has_a_source():
+    peak, src = bench.measured_bf16_peak()
+    assert peak > 100.0 and isinstance(src, str) and src
