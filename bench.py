@@ -16,7 +16,7 @@ Metric: effective TFLOP/s = (N^3/3) / (factor + solve time), higher is better.
            cores, on a bounded sample (N=16384).
 
 --impl reference times that CPU restatement (the reference's own PaRSEC build is not available)
-on the same metric. Under torchrun every rank runs an independent replica ("replicas only":
+on the same metric and the same workload (N=32768 every step, about 27 s per step on 16 cores). Under torchrun every rank runs an independent replica ("replicas only":
 the tiled factorisation of one matrix runs on one GPU; its tiles are not split across GPUs).
 """
 import argparse
@@ -164,10 +164,21 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
+def main_config(args, ws):
+    """The workload of a step, the same dictionary in both arms."""
+    N, NB, nrhs = args.N, args.NB, args.nrhs
+    return {"workload": "potrf+potrs FP64 N=%d NB=%d nrhs=%d" % (N, NB, nrhs), "N": N, "NB": NB,
+            "nrhs": nrhs, "generator": "(M+M^T)/2 + N*I, M~U[-0.5,0.5) seed 42",
+            "l2": "inputs 4.4 GB > L2; A restored (4.4 GB copy) between timed steps",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
 def run_reference(args, ws, rank):
+    """The reference's CPU potrf (restated flowgraph, OpenBLAS tile kernels, all host cores) on the
+    workload of the other arm: every step factorises and solves the full N x N system."""
     if rank != 0:
         return
-    N = args.cpu_N
+    N = args.N
     NB = args.NB
     times, blas = cpu_run(N, NB, args.warmup + args.steps)
     t = times[args.warmup:]
@@ -178,10 +189,9 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": "cholesky_solve_tflops", "value": val, "unit": "TFLOP/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "potrf+potrs FP64 N=%d NB=%d nrhs=1 (bounded CPU sample of the N=%d workload)"
-                   % (N, NB, args.N), "N": N, "NB": NB, "nrhs": 1},
+        "config": main_config(args, ws),
         "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                         "sample": "N=%d NB=%d factor+solve, %s tile kernels, %d threads" %
+                         "sample": "the whole N=%d NB=%d factor+solve every step, %s tile kernels, %d threads" %
                                    (N, NB, "OpenBLAS" if blas else "plain-loop", cores)},
         "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -276,10 +286,7 @@ def run_ours(args, ws, rank, local):
         "metric": "cholesky_solve_tflops", "value": value, "unit": "TFLOP/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "potrf+potrs FP64 N=%d NB=%d nrhs=%d" % (N, NB, nrhs), "N": N, "NB": NB,
-                   "nrhs": nrhs, "generator": "(M+M^T)/2 + N*I, M~U[-0.5,0.5) seed 42",
-                   "l2": "inputs 4.4 GB > L2; A restored (4.4 GB copy) between timed steps",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": main_config(args, ws),
         "backward_error": berr,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
@@ -360,7 +367,6 @@ def add_roofline_fractions(line, fp64_peak, bf16_peak):
 def backward_error(gbx, A0, T, X, b0, N, NB, dev):
     """||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) for the first rhs, with A from its lower tiles."""
     import torch
-    import oracle  # noqa: F401  (tile slot arithmetic only)
     nt = gbx.ntiles(N, NB)
     tv = A0.view(-1, NB, NB)
     x = X[0]
@@ -432,9 +438,12 @@ def run_mixed(gbx, dev, N=32768, NB=512, nrhs=8, kappa=1e6):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         fe = ((X - X64).abs().max() / X64.abs().max()).item()
+        # after the timed region: the residual again, from plain FP64 products over the tiles
+        be64 = max(gbx.backward_error_fp64(A, N, NB, B, X))
         out[prec] = {"ms": ms, "tflops": N ** 3 / 3 / (ms * 1e-3) / 1e12, "speedup_vs_plain_fp64": plain_ms / ms,
                      "status": st, "iterations": info["iterations"], "factor_retries": info["factor_retries"],
                      "shift": info["shift"], "backward_error": info["backward_error"],
+                     "backward_error_fp64_check": be64,
                      "forward_error_vs_fp64": fe, "cond_estimate_diag_tiles": info["cond_estimate"]}
         del W
         torch.cuda.empty_cache()
@@ -565,7 +574,17 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
         it = [i["iterations"] for i in infos]
         be = [i["backward_error"] for i in infos]
         fe = ((X - X64).abs().max() / X64.abs().max()).item()
+        # after the timed region: every matrix's residual again, from plain FP64 products
+        be64, vo = 0.0, 0
+        for k, n in enumerate(sizes):
+            n = int(n)
+            nt = (n + NB - 1) // NB
+            Ak = A[int(offs[k]):int(offs[k]) + nt * (nt + 1) // 2 * NB * NB]
+            Bk, Xk = B[vo:vo + n * nrhs].view(nrhs, n), X[vo:vo + n * nrhs].view(nrhs, n)
+            be64 = max(be64, max(gbx.backward_error_fp64(Ak, n, NB, Bk, Xk)))
+            vo += n * nrhs
         out[prec] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "matrices_per_s": count / (ms * 1e-3),
+                     "backward_error_fp64_check_max": be64,
                      "speedup_vs_plain_fp64": plain_ms / ms, "status": st, "iterations_max": int(max(it)),
                      "iterations_mean": float(np.mean(it)), "factor_retries": int(sum(i["factor_retries"] for i in infos)),
                      "shift_max": float(max(i["shift"] for i in infos)),

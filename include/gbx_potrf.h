@@ -24,8 +24,11 @@
  * back by the *_status calls, which synchronise the stream.
  *
  * Thread safety. Calls on different streams with disjoint workspaces may run concurrently.
- * The library keeps no mutable global state besides a per-device cache of launch attributes
- * guarded by a mutex.
+ * Mutable global state, each part guarded by a mutex or set only by its own setter: per-device
+ * caches of launch attributes and of the FP64 solve's scratch, the wait time limit
+ * (gbx_set_wait_timeout_ns), the trace buffer (gbx_set_trace_buffer), the copy streams and
+ * mapped flags of gbx_dposv_tiled_host (one caller at a time), and the static scratch of
+ * gbx_dpotrf_tiled_noalloc with its per-device address.
  */
 #ifndef GBX_POTRF_H
 #define GBX_POTRF_H
@@ -116,8 +119,11 @@ int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes
  * the process exits; it limits the problem to 512 blocks per edge (N <= 65536 with 128-blocks:
  * NB <= 128 gives blocks of NB, larger NB blocks of 128, 64 or 32) and larger problems return
  * GBX_ERR_NOALLOC_LIMIT. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress): make it before any stream capture. All calls share the array, so calls
- * that overlap on the GPU (other streams, other threads) race; serialise them. The factorisation
+ * (cudaGetSymbolAddress) and keeps it for later calls: make that first call before any stream
+ * capture. cudaDeviceReset invalidates the kept address (the module is loaded again at a new
+ * address), so do not call this entry point in a process after a cudaDeviceReset of that device.
+ * All calls share the array, so calls that overlap on the GPU (other streams, other threads) race;
+ * serialise them. The factorisation
  * status (0, first bad pivot, GBX_ERR_TIMEOUT) is written to the device int devInfo. Asynchronous. */
 int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* stream);
 
@@ -261,7 +267,10 @@ int gbx_dpotri_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes
  * column of L is copied back as soon as it is final (while the factorisation goes on), then
  * X = (L L^T)^{-1} B comes back. Returns once the factorisation has finished on the device (the
  * calling thread issues the copy-out as the columns complete); the solve and the last copies are
- * still queued on `stream`. gbx_dpotrf_tiled_status(work) gives the factorisation status. No
+ * still queued on `stream`. gbx_dpotrf_tiled_status(work) gives the factorisation status. If the
+ * factorisation stopped early (a non-positive pivot or a timed-out wait), the solve is skipped,
+ * the stream is synchronised, L_host holds the partial factor and the call returns the status
+ * itself (>0 first bad pivot, or GBX_ERR_TIMEOUT). No
  * counterpart in the reference, whose tiles reach the device through PaRSEC's stage-in
  * (parsec/ttg.h:1434-1672) and come back on wait() (parsec/devicefunc.h:232-256). */
 int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes);

@@ -10,7 +10,20 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("TTG_REFERENCE_ROOT", "/root/reference")
+
+
+def _find_reference():
+    """The reference checkout: $TTG_REFERENCE_ROOT, else a `reference` directory beside the
+    repository's own directory; None when neither holds examples/potrf."""
+    env = os.environ.get("TTG_REFERENCE_ROOT")
+    cands = [env] if env else [os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "examples", "potrf")):
+            return c
+    return None
+
+
+REF_ROOT = _find_reference() or ""
 
 
 def _newer(out, srcs):
@@ -33,7 +46,7 @@ def build_oracle(force=False):
 def build_ref(force=False):
     """Returns the path of the reference generator binary, or None without a reference checkout."""
     hdr = os.path.join(REF_ROOT, "examples", "potrf", "core_plgsy.h")
-    if not os.path.exists(hdr):
+    if not REF_ROOT or not os.path.exists(hdr):
         return None
     src = os.path.join(HERE, "ref_plgsy_main.cpp")
     outdir = os.path.join(HERE, "_ref")
@@ -59,7 +72,7 @@ def build_ref_flowgraph(force=False):
     ttg.h, with the PaRSEC/LAPACK stand-ins of oracle/ref_shim and the oracle's tile kernels.
     Returns (ref_potrf, testing_dpotrf) paths, or None without a reference checkout."""
     potrf_dir = os.path.join(REF_ROOT, "examples", "potrf")
-    if not os.path.exists(os.path.join(potrf_dir, "potrf.h")):
+    if not REF_ROOT or not os.path.exists(os.path.join(potrf_dir, "potrf.h")):
         return None
     root = os.path.dirname(HERE)
     outdir = os.path.join(HERE, "_ref")

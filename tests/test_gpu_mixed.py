@@ -83,6 +83,31 @@ def test_dposv_mixed_householder(gbx, cuda, kappa, prec):
     solve_and_check(gbx, cuda, A, N, NB, 8, prec, kappa=kappa)
 
 
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_dposv_mixed_householder_8192_fp64_checked(gbx, cuda, prec):
+    """The mixed-precision configuration (A = H diag(lam) H^T, 4 reflectors, kappa = 1e6, 8 rhs) at
+    N=8192: the solver's own backward error (double-float residual), the same figure from plain FP64
+    products on the device (gbx_dsymm_tiled) and an FP64 residual on the host all meet 1e-14."""
+    import torch
+    N, NB, nrhs = 8192, 512, 8
+    A = workloads.householder_tiles(N, NB, 4, 1e6, 42, cuda)
+    Bn = workloads.rhs(N, nrhs, seed=42)
+    B = torch.from_numpy(Bn).to(cuda)
+    X, info, st = gbx.dposv_mixed(A, N, NB, B, prec=prec, tol=1e-14, maxiter=300)
+    assert st == 0, info
+    assert info["backward_error"] <= 1e-14, info
+    dev = gbx.backward_error_fp64(A, N, NB, B, X)
+    assert max(dev) <= 1e-14, dev
+    Ad = dense_from_tiles(A.cpu().numpy(), N, NB)
+    Xn = X.cpu().numpy()
+    anorm = np.abs(Ad).sum(1).max()
+    host = [np.abs(Bn[j] - Ad @ Xn[j]).max() / (anorm * np.abs(Xn[j]).max() + np.abs(Bn[j]).max())
+            for j in range(nrhs)]
+    print("N=8192 %s: solver %.3g, device FP64 %.3g, host FP64 %.3g" % (prec, info["backward_error"], max(dev),
+                                                                       max(host)))
+    assert max(host) <= 1e-14, host
+
+
 def test_dsymm_tiled_matches_dense(gbx, cuda):
     import ctypes
     import torch

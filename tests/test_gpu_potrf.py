@@ -197,7 +197,15 @@ def test_dag_potrf_8192_vs_cpu_oracle(gbx, cuda):
     got = run_dag(gbx, cuda, N, NB, t0)
     ref = t0.copy()
     assert oracle.potrf_tiled(ref, N, NB, nthreads=0, use_blas=True)[0] == 0
-    assert_factor_close(oracle.tiles_to_lower(got, N, NB), oracle.tiles_to_lower(ref, N, NB))
+    L = oracle.tiles_to_lower(got, N, NB)
+    assert_factor_close(L, oracle.tiles_to_lower(ref, N, NB))
+    # the factorisation bar of the plain path at this size too: ||A - L L^T||_F / (N ||A||_F) <= 1e-15
+    # (FP64 product on the host, numpy's multithreaded BLAS)
+    A0 = oracle.tiles_to_lower(t0, N, NB)
+    A0 = A0 + np.tril(A0, -1).T
+    res = np.linalg.norm(A0 - L @ L.T) / (N * np.linalg.norm(A0))
+    print("N=8192 ||A - L L^T||_F / (N ||A||_F) = %.3g" % res)
+    assert res <= 1e-15
 
 
 def test_dag_reports_first_bad_pivot(gbx, cuda):
@@ -362,7 +370,8 @@ def test_dposv_tiled_host_non_spd_completes(gbx, cuda):
     need = ctypes.c_size_t(0)
     gbx.call("gbx_dposv_tiled_host_bufferSize", N, NB, ctypes.byref(need))
     work = torch.empty(need.value, dtype=torch.uint8, device=cuda)
-    L_host, X_host, _ = gbx.dposv_tiled_host(A_host, N, NB, B_host, work=work, check=False)
+    L_host, X_host, st0 = gbx.dposv_tiled_host(A_host, N, NB, B_host, work=work, check=False)
+    assert st0 == 2 * NB + 5 + 1  # the call itself reports the pivot and skips the solve
     _wait_stream(torch)
     st = gbx.call("gbx_dpotrf_tiled_status", ctypes.c_void_p(work.data_ptr()),
                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))

@@ -57,7 +57,7 @@ def test_reference_arm_under_torchrun_prints_once(gbx):
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "1", "--cpu-N", "512", "--NB", "128"]
+           "--gpus", "2", "--steps", "1", "--warmup", "1", "--N", "512", "--NB", "128"]
     env = dict(os.environ, OMP_NUM_THREADS="1")
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -66,3 +66,12 @@ def test_reference_arm_under_torchrun_prints_once(gbx):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # the reference arm times the same workload as the GPU arm
+    assert d["config"] == bench_config(512, 128, 1, 2)
+
+
+def bench_config(N, NB, nrhs, ws):
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    return bench.main_config(argparse.Namespace(N=N, NB=NB, nrhs=nrhs), ws)

@@ -241,6 +241,24 @@ def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=N
     return X, info.as_dict(), st
 
 
+def backward_error_fp64(A_tiles, N, NB, B, X, stream=None):
+    """Normwise backward error of each right-hand side, max_j ||b_j - A x_j||_inf / (||A||_inf
+    ||x_j||_inf + ||b_j||_inf), from plain FP64 products over the lower tiles (gbx_dsymm_tiled), not
+    from the solver's own double-float residual. B, X: (nrhs, N) CUDA float64, nrhs <= 16. Returns a
+    list of nrhs floats."""
+    import torch
+    nrhs = B.shape[0]
+    R = B.clone()
+    call("gbx_dsymm_tiled", N, NB, _ptr(A_tiles), nrhs, -1.0, _ptr(X), 1.0, _ptr(R), _stream(stream))
+    absA = A_tiles.abs()
+    ones = torch.ones(1, N, dtype=torch.float64, device=A_tiles.device)
+    rows = torch.zeros(1, N, dtype=torch.float64, device=A_tiles.device)
+    call("gbx_dsymm_tiled", N, NB, _ptr(absA), 1, 1.0, _ptr(ones), 0.0, _ptr(rows), _stream(stream))
+    anorm = rows.max()
+    den = anorm * X.abs().amax(dim=1) + B.abs().amax(dim=1)
+    return (R.abs().amax(dim=1) / den).tolist()
+
+
 def split_f64(a, stream=None):
     """(hi, lo) FP32 tensors with hi + lo = a for an FP64 CUDA tensor (gbx_split_f64)."""
     import torch
@@ -266,7 +284,8 @@ def dposv_tiled_host(A_host, N, NB, B_host, tiles=None, X=None, work=None, L_hos
                      check=True):
     """Factor + solve from host buffers with the copies overlapped (gbx_dposv_tiled_host).
     A_host: tile-major lower FP64 (pinned CPU tensor); B_host: (nrhs, N) pinned CPU tensor.
-    Returns (L_host, X_host, status); with check=True the stream is synchronised first."""
+    Returns (L_host, X_host, status); with check=True the stream is synchronised first. A status > 0
+    (first bad pivot) is returned whatever `check` says: the solve was skipped."""
     import torch
     dev = torch.device("cuda", torch.cuda.current_device())
     nrhs = 1 if B_host.dim() == 1 else B_host.shape[0]
@@ -279,9 +298,10 @@ def dposv_tiled_host(A_host, N, NB, B_host, tiles=None, X=None, work=None, L_hos
     L_host = torch.empty(A_host.shape, dtype=torch.float64, pin_memory=True) if L_host is None else L_host
     X_host = torch.empty(B_host.shape, dtype=torch.float64, pin_memory=True) if X_host is None else X_host
     s = _stream(stream)
-    call("gbx_dposv_tiled_host", N, NB, _ptr(A_host), _ptr(L_host), nrhs, _ptr(B_host), _ptr(X_host), _ptr(tiles),
-         _ptr(X), _ptr(work), need.value, s)
-    st = call("gbx_dpotrf_tiled_status", _ptr(work), s) if check else None
+    st = call("gbx_dposv_tiled_host", N, NB, _ptr(A_host), _ptr(L_host), nrhs, _ptr(B_host), _ptr(X_host),
+              _ptr(tiles), _ptr(X), _ptr(work), need.value, s)
+    if st == 0:  # > 0: the factorisation stopped at that pivot and the solve was skipped
+        st = call("gbx_dpotrf_tiled_status", _ptr(work), s) if check else None
     return L_host, X_host, st
 
 

@@ -759,19 +759,18 @@ int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, in
 }
 
 // ---- factorisation and solve from host buffers, the copies overlapped ---------------------------
-//   copy-in:  tile columns go to HBM one by one on a copy stream, each followed by a 4-byte copy
-//             that raises its arrival flag in device memory; executor tasks check (bounded) the
-//             flags of the columns they touch until the flag "every column is in" is up, after
-//             which they stop checking;
+//   copy-in:  one cudaMemcpyAsync of the whole tile array, then one of the right-hand sides, both
+//             on the caller's stream ahead of the executor launch (copies interleaved with other
+//             stream operations ran many times slower on this platform than one large copy);
 //   copy-out: each finished POTRF/TRSM block adds to the count of its group of tile columns
 //             (about eight groups); the block that completes a group raises the group's flag in
 //             mapped pinned host memory, and the calling thread, which polls those flags, issues
 //             that group's copy back (its tiles are contiguous) on a second copy stream, so L
 //             streams out while the factorisation runs.
 // Stream memory operations were measured to signal a quarter of a second late on this platform,
-// hence plain copies and a polling thread. The executor raises every group flag on any early
+// hence plain copies and a polling thread. The executor raises every group flag (to 2) on any early
 // exit, and the thread also stops when the launch has finished, so no side waits on a flag that
-// cannot come.
+// cannot come; after an early exit the solve is skipped.
 namespace {
 struct HostOverlap {
   cudaStream_t out = nullptr;
@@ -846,9 +845,11 @@ int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, in
     return GBX_ERR_CUDA;
   if (int e = launch_dag(V, NTb, work, dag, s, 0, gbx_get_wait_timeout_ns(), col_done, h->flags_dev, G * r)) return e;
   if (cudaEventRecord(h->ev_kernel, s) != cudaSuccess) return GBX_ERR_CUDA;
-  // copy-out: each group as soon as the executor raises its flag
+  // copy-out: each group as soon as the executor raises its flag (2: the executor stopped early)
+  bool stopped = false;
   for (int g = 0; g < ngroups;) {
     if (out_flag[g] != 0) {
+      if (out_flag[g] == 2) stopped = true;
       const int k0 = g * G, k1 = std::min(NT, k0 + G);
       const long long off = col_off(k0), cnt = col_off(k1) - off;
       if (cudaMemcpyAsync(L_host + off, tiles + off, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, h->out) !=
@@ -866,6 +867,11 @@ int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, in
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
   if (cudaEventRecord(h->ev_out, h->out) != cudaSuccess) return GBX_ERR_CUDA;
+  if (stopped) {  // bad pivot or timed-out wait: no solve on a partial factor; report the status
+    if (cudaStreamWaitEvent(s, h->ev_out, 0) != cudaSuccess) return GBX_ERR_CUDA;
+    const int st = gbx_dpotrf_tiled_status(work, stream);
+    return st != 0 ? st : GBX_ERR_CUDA;  // an early exit always leaves a nonzero status
+  }
   if (nrhs > 0) {
     if (int e = gbx_dpotrs_tiled(N, NB, tiles, nrhs, X, N, stream)) return e;
     if (cudaMemcpyAsync(X_host, X, (size_t)N * nrhs * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess)
@@ -933,7 +939,8 @@ std::mutex g_noalloc_mtx;
 std::vector<void*> g_noalloc_ptr;  // device address of g_noalloc_scratch, per device
 
 // One-time set-up per device, with that device current: the symbol's device address. In host code
-// the array's name is only a host-side stand-in and must never be passed to a kernel.
+// the array's name is only a host-side stand-in and must never be passed to a kernel. The address
+// is kept for the life of the process; a cudaDeviceReset of the device would make it stale.
 int noalloc_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GBX_ERR_CUDA;

@@ -1376,7 +1376,7 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
   std::vector<int> swept;  // matrices of the uploaded task lists
   int nf = 0, nb = 0;
   const uint64_t tmo = gbx_get_wait_timeout_ns();
-  auto precond = [&](const std::vector<int>& l, const double* r, double* z) {
+  auto precond = [&](const std::vector<int>& l, const double* r, double* z) -> int {
     float* xf = tmp;
     float* yf = tmp + nvec;
     d2s_kernel<<<512, 256, 0, s>>>(r, xf, nvec);
@@ -1409,18 +1409,21 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
       nf = (int)tf.size();
       nb = (int)tb.size();
       tf.insert(tf.end(), tb.begin(), tb.end());
-      cudaMemcpyAsync(d_tasks, tf.data(), tf.size() * sizeof(SweepTask), cudaMemcpyHostToDevice, s);
+      if (cudaMemcpyAsync(d_tasks, tf.data(), tf.size() * sizeof(SweepTask), cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return GBX_ERR_CUDA;
       swept = l;
     }
     // fresh queue heads and counters; status and abort stay, so a wait that ran out is reported
-    cudaMemsetAsync(&sw_st[0].head, 0, sizeof(unsigned long long), s);
-    cudaMemsetAsync(&sw_st[1].head, 0, sizeof(unsigned long long), s);
-    cudaMemsetAsync(sw_cnt, 0, (size_t)4 * invt * sizeof(int), s);
+    if (cudaMemsetAsync(&sw_st[0].head, 0, sizeof(unsigned long long), s) != cudaSuccess ||
+        cudaMemsetAsync(&sw_st[1].head, 0, sizeof(unsigned long long), s) != cudaSuccess ||
+        cudaMemsetAsync(sw_cnt, 0, (size_t)4 * invt * sizeof(int), s) != cudaSuccess)
+      return GBX_ERR_CUDA;
     const int gf = std::max(1, std::min(2 * sms, nf)), gb = std::max(1, std::min(2 * sms, nb));
     launch_sweep(0, gf, s, dmats, d_tasks, nf, W, Inv, xf, yf, NB, nrhs, sw_cnt, sw_cnt + invt, sw_st, tmo);
     launch_sweep(1, gb, s, dmats, d_tasks + nf, nb, W, Inv, xf, yf, NB, nrhs, sw_cnt + 2 * invt, sw_cnt + 3 * invt,
                  sw_st + 1, tmo);
     s2d_kernel<<<512, 256, 0, s>>>(xf, z, nvec);
+    return GBX_OK;
   };
   // y := y + alpha A x for the matrices of l (double-float arithmetic on the split A)
   auto symm = [&](const std::vector<int>& l, double alpha, const double* x, double* y) {
@@ -1481,10 +1484,10 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
   };
 
   // 2. x0 = M^{-1} b ; r = b - A x0 ; z = M^{-1} r ; p = z
-  precond(live, B, X);
+  if (int e = precond(live, B, X)) return e;
   copy_vecs(live, R, B);
   symm(live, -1.0, X, R);
-  precond(live, R, Z);
+  if (int e = precond(live, R, Z)) return e;
   copy_vecs(live, P, Z);
   stats_of(live, R, Z, stats);
   stats_of(live, X, nullptr, stats_x);
@@ -1520,7 +1523,7 @@ extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const do
       copy_vecs(act, R, B);
       symm(act, -1.0, X, R);
     }
-    precond(act, R, Z);
+    if (int e = precond(act, R, Z)) return e;
     stats_of(act, R, Z, stats);
     stats_of(act, X, nullptr, stats_x);
     if (!fetch_stats()) return GBX_ERR_CUDA;

@@ -182,7 +182,6 @@ auto make_potrf_ttg(MatrixT& A, ttg::Edge<Key2, MatrixTile<double>>& input, ttg:
   auto tt_trsm = make_trsm(A, disp_trsm, potrf_trsm, gemm_trsm, trsm_syrk, trsm_gemm_row, trsm_gemm_col, output);
   auto tt_syrk = make_syrk(A, disp_syrk, trsm_syrk, syrk_syrk, syrk_potrf, syrk_syrk);
   auto tt_gemm = make_gemm(A, disp_gemm, trsm_gemm_row, trsm_gemm_col, gemm_gemm, gemm_trsm, gemm_gemm);
-  for (ttg::TTBase* t : {(ttg::TTBase*)tt_dispatch.get()}) (void)t;
   tt_dispatch->set_defer_writer(defer_write);
   tt_potrf->set_defer_writer(defer_write);
   tt_trsm->set_defer_writer(defer_write);
