@@ -16,8 +16,9 @@ Metric: effective TFLOP/s = (N^3/3) / (factor + solve time), higher is better.
            cores, on a bounded sample (N=16384).
 
 --impl reference times that CPU restatement (the reference's own PaRSEC build is not available)
-on the same metric and the same workload (N=32768 every step, about 27 s per step on 16 cores). Under torchrun every rank runs an independent replica ("replicas only":
-the tiled factorisation of one matrix runs on one GPU; its tiles are not split across GPUs).
+on the same metric and the same workload (N=32768 every step, about 27 s per step on 16 cores).
+Under torchrun every rank runs an independent replica ("replicas only": the tiled factorisation
+of one matrix runs on one GPU; its tiles are not split across GPUs).
 """
 import argparse
 import json
@@ -345,6 +346,15 @@ def measured_bf16_peak():
         return 1900.0, "fallback 1.9 PFLOP/s bf16"
 
 
+def measured_hbm_peak():
+    """Copy bandwidth (GB/s) from MEASURED_PEAKS.json, else the fallback figure."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError, TypeError):
+        return 6800.0
+
+
 def add_roofline_fractions(line, fp64_peak, bf16_peak):
     """Adds `frac_of_peak` beside every `tflops` of the secondary configurations: FP64 results against
     the FP64 GEMM rate measured in the run, bf16/fp16 results against the dense bf16 tensor-core
@@ -561,16 +571,31 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
     del T, work
     torch.cuda.empty_cache()
     out["plain_fp64_per_matrix"] = {"ms": plain_ms, "tflops": flops / (plain_ms * 1e-3) / 1e12}
+    bf16_peak, _ = measured_bf16_peak()
+    hbm = measured_hbm_peak()
     for prec in ("fp16", "bf16", "fp8"):  # fp8: e4m3 operands on kind::f8f6f4
+        # the whole solve (factorisation with its retry loop, CG to 1e-14 with device-side
+        # coefficients and convergence tests) captured once in a CUDA graph, replayed
         W = torch.empty(total, dtype=torch.float32, device=dev)
-        X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300, W=W)
-        torch.cuda.synchronize()
-        e0, e1 = _events()
-        e0.record()
-        X, infos, st = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec=prec, tol=1e-14, maxiter=300, W=W)
-        e1.record()
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
+        X = torch.empty_like(B)
+        solver = gbx.MixedBatchedSolver(sizes, NB, nrhs, prec=prec, device=dev)
+        side = torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+            solver.run(A, B, X, W, tol=1e-14, maxiter=300, stream=side)
+        times = []
+        for _ in range(3):  # the first replay is a warm-up
+            torch.cuda.synchronize()
+            with torch.cuda.stream(side):
+                e0, e1 = _events()
+                e0.record()
+                g.replay()
+                e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = statistics.median(times[1:])
+        infos, st = solver.result()
+        del g, solver
         it = [i["iterations"] for i in infos]
         be = [i["backward_error"] for i in infos]
         fe = ((X - X64).abs().max() / X64.abs().max()).item()
@@ -583,7 +608,16 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
             Bk, Xk = B[vo:vo + n * nrhs].view(nrhs, n), X[vo:vo + n * nrhs].view(nrhs, n)
             be64 = max(be64, max(gbx.backward_error_fp64(Ak, n, NB, Bk, Xk)))
             vo += n * nrhs
+        # size-mix roofline: per matrix, its factorisation at the tensor-core rate plus the HBM
+        # bytes of the refinement (one pass over A writing W and the split: 10 n^2 B; the factor's
+        # W read and written: 4 n^2; start-up sweeps and product: 12 n^2; each iteration one product
+        # over the split A and two sweeps over W: 8 n^2; the final check: 4 n^2)
+        peak_tc = (2.0 if prec == "fp8" else 1.0) * bf16_peak * 1e12
+        t_roof = sum((float(n) ** 3 / 3) / peak_tc + (30.0 + 8.0 * i["iterations"]) * float(n) ** 2 / (hbm * 1e9)
+                     for n, i in zip(sizes, infos))
         out[prec] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "matrices_per_s": count / (ms * 1e-3),
+                     "cuda_graph": True, "size_mix_roofline_ms": t_roof * 1e3,
+                     "frac_of_size_mix_roofline": t_roof * 1e3 / ms,
                      "backward_error_fp64_check_max": be64,
                      "speedup_vs_plain_fp64": plain_ms / ms, "status": st, "iterations_max": int(max(it)),
                      "iterations_mean": float(np.mean(it)), "factor_retries": int(sum(i["factor_retries"] for i in infos)),

@@ -184,12 +184,18 @@ int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes);
 /* Low-precision Cholesky of the FP64 tile-major lower matrix A into the FP32 tile-major factor W
  * (same layout): diagonal POTRF and TRSM in FP32, SYRK/GEMM updates on the tensor cores with
  * bf16/fp16/fp8-e4m3 operands scaled per row by powers of two and FP32 accumulation. The diagonal of A is
- * multiplied by (1 + shift) first (0 for none). Asynchronous; the status (0, first bad pivot, or
- * GBX_ERR_TIMEOUT) and the largest diagonal-tile condition estimate come from
- * gbx_potrf_mixed_info, which synchronises the stream. */
-int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work, size_t work_bytes,
-                    void* stream);
-int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, void* stream);
+ * multiplied by (1 + shift) first (0 for none).
+ * fp64_diag_cond: a diagonal tile whose condition estimate, max_i a_ii / min_i a_ii of the tile after
+ * its updates (a lower bound of its condition number), exceeds this threshold (or which has a
+ * non-positive diagonal entry) is factorised in FP64 instead (the reference's diagonal POTRF is
+ * FP64, examples/potrf/potrf.h:62-66); 0 sends every diagonal tile to FP64, a huge value (1e300)
+ * none. The FP64 route uses one NB x NB FP64 scratch tile per diagonal tile in the workspace.
+ * Asynchronous; the status (0, first bad pivot, or GBX_ERR_TIMEOUT), the largest diagonal-tile
+ * condition estimate (from the factor's diagonal) and the number of diagonal tiles factorised in
+ * FP64 come from gbx_potrf_mixed_info, which synchronises the stream. */
+int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, double fp64_diag_cond,
+                    void* work, size_t work_bytes, void* stream);
+int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, int* fp64_tiles, void* stream);
 
 /* Inverses of the FP32 diagonal factor tiles: Inv holds NT tiles of NB*NB floats, tile K =
  * L_KK^{-T} column-major. */
@@ -212,6 +218,7 @@ typedef struct gbx_refine_info {
   double backward_error; /* max over right-hand sides of ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) */
   double anorm;          /* ||A||_inf */
   float cond_estimate;   /* largest diagonal-tile condition estimate seen by the factorisation */
+  int fp64_diag_tiles;   /* diagonal tiles the factorisation sent to the FP64 route */
 } gbx_refine_info;
 
 /* Batched mixed-precision factorisation: the flowgraphs of many SPD matrices of uneven orders
@@ -223,30 +230,55 @@ typedef struct gbx_refine_info {
  * No counterpart in the reference. */
 int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes);
 int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
-                            const unsigned char* sel, void* work, size_t work_bytes, void* stream);
+                            double fp64_diag_cond, const unsigned char* sel, void* work, size_t work_bytes,
+                            void* stream);
 int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info, float* cond_est,
-                                 void* stream);
+                                 int* fp64_tiles, void* stream);
 
 /* Bytes of workspace gbx_dposv_mixed needs (NB 256 or 512, nrhs <= 16). */
 int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes);
 
 /* Solves A X = B (A FP64 tile-major lower, B and X column-major N x nrhs, nrhs <= 16) to the FP64
- * backward error `tol`: low-precision factorisation into W, then CG in FP64 preconditioned by W.
- * Synchronises the stream. Returns 0, a positive pivot index if every shifted factorisation broke
- * down, GBX_ERR_NOCONV if `maxiter` iterations did not reach `tol`, or another error. */
-int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec, double tol,
-                    int maxiter, float* W, void* work, size_t work_bytes, gbx_refine_info* info, void* stream);
+ * backward error `tol`: low-precision factorisation into W (fp64_diag_cond as for
+ * gbx_potrf_mixed), then CG in FP64 preconditioned by W. Synchronises the stream. Returns 0, a
+ * positive pivot index if every shifted factorisation broke down, GBX_ERR_NOCONV if `maxiter`
+ * iterations did not reach `tol`, or another error. */
+int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec,
+                    double fp64_diag_cond, double tol, int maxiter, float* W, void* work, size_t work_bytes,
+                    gbx_refine_info* info, void* stream);
 
 /* Batched gbx_dposv_mixed: matrices as for gbx_potrf_mixed_batched, right-hand sides and solutions
  * of matrix k column-major n[k] x nrhs, concatenated in batch order. One factorisation launch for
- * the batch (matrices that break down are factorised again, alone, with a growing diagonal shift),
- * then preconditioned CG in FP64 where every step is one launch over the matrices that have not yet
- * met `tol`. info (optional) receives one record per matrix. Returns 0 when every matrix met `tol`,
- * GBX_ERR_NOCONV otherwise (or another error). No counterpart in the reference. */
+ * the batch (matrices that break down are factorised again with a growing diagonal shift, up to 8
+ * attempts), then preconditioned CG in FP64 in which every step runs over the matrices that have
+ * not yet met `tol`. The PCG coefficients, the convergence tests and the selection of the matrices
+ * still iterating are computed on the device; the retries and the iterations are CUDA-graph WHILE
+ * nodes, so the whole solve is one graph with no host synchronisation. No counterpart in the
+ * reference.
+ *   _plan:   builds the task tables of a batch shape (batch, n, NB, nrhs, prec) and uploads them
+ *            into `work`; synchronises `stream`. Not capturable. Once per shape and workspace.
+ *   _exec:   the solve itself, asynchronous on `stream`: no host synchronisation, no allocation, no
+ *            host-to-device copy. When `stream` is capturing, the solve's nodes (with its two
+ *            conditional nodes) are added to the caller's graph, which can then be replayed; else
+ *            the library builds, launches and releases a graph of its own. Needs a plan of the
+ *            same shape in `work` (a mismatch makes the run do nothing and _result return
+ *            GBX_ERR_ARG) made earlier in this process on this device.
+ *   _result: synchronises `stream` and returns 0 when every matrix met `tol`, GBX_ERR_NOCONV
+ *            otherwise, a pivot index for a one-matrix batch whose every factorisation broke
+ *            down, or GBX_ERR_TIMEOUT / GBX_ERR_ARG; info (optional) receives one record per
+ *            matrix.
+ * gbx_dposv_mixed_batched = _plan + _exec + _result. */
 int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes);
+int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, void* work, size_t work_bytes,
+                                 void* stream);
+int gbx_dposv_mixed_batched_exec(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
+                                 double* X, int prec, double fp64_diag_cond, double tol, int maxiter, float* W,
+                                 void* work, size_t work_bytes, void* stream);
+int gbx_dposv_mixed_batched_result(int batch, const int* n, int NB, int nrhs, double tol, const void* work,
+                                   gbx_refine_info* info, void* stream);
 int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B, double* X,
-                            int prec, double tol, int maxiter, float* W, void* work, size_t work_bytes,
-                            gbx_refine_info* info, void* stream);
+                            int prec, double fp64_diag_cond, double tol, int maxiter, float* W, void* work,
+                            size_t work_bytes, gbx_refine_info* info, void* stream);
 
 /* hi[i] + lo[i] = a[i] for n FP64 values: hi = fl32(a), lo = fl32(a - hi), rounded to nearest even
  * (the double-float split of the refinement's residual products, computed on the bit pattern;

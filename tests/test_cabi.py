@@ -60,9 +60,11 @@ def test_argument_validation_without_gpu(gbx):
     assert L.gbx_split_f64(None, None, None, 0, None) == 0
     # mixed solvers: operand precision 0 (bf16), 1 (fp16) or 2 (fp8 e4m3); NB 256 or 512
     dummy = ctypes.c_void_p(16)
-    assert L.gbx_potrf_mixed(1000, 256, dummy, dummy, 3, ctypes.c_double(0.0), dummy, 1 << 30, None) == \
+    assert L.gbx_potrf_mixed(1000, 256, dummy, dummy, 3, ctypes.c_double(0.0), ctypes.c_double(1e4), dummy, 1 << 30,
+                             None) == \
         gbx.GBX_ERR_ARG
-    assert L.gbx_potrf_mixed(1000, 768, dummy, dummy, 0, ctypes.c_double(0.0), dummy, 1 << 30, None) == \
+    assert L.gbx_potrf_mixed(1000, 768, dummy, dummy, 0, ctypes.c_double(0.0), ctypes.c_double(1e4), dummy, 1 << 30,
+                             None) == \
         gbx.GBX_ERR_ARG
     assert L.gbx_potrf_mixed_bufferSize(1000, 1024, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
 
@@ -90,3 +92,25 @@ def test_batched_mixed_workspace_without_gpu(gbx):
     assert sz.value > slots * 256 * 256 * 2  # at least the low-precision copies
     assert L.gbx_dposv_mixed_bufferSize(700, 256, 2, ctypes.byref(one)) == 0
     assert 0 < one.value < sz.value
+
+
+def test_batched_mixed_plan_exec_result_argument_checks(gbx):
+    """The split batched solve rejects bad arguments before any device work (no GPU needed)."""
+    L = gbx.lib()
+    n = (ctypes.c_int * 2)(700, 300)
+    dummy = ctypes.c_void_p(16)
+    d = ctypes.c_double
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 200, 2, 0, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 3, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 0, dummy, 16, None) == gbx.GBX_ERR_WORKSPACE
+    ex = L.gbx_dposv_mixed_batched_exec
+    assert ex(2, n, 256, dummy, 2, dummy, dummy, 0, d(1e4), d(0.0), 10, dummy, dummy, 1 << 40, None) == \
+        gbx.GBX_ERR_ARG  # tolerance must be positive
+    assert ex(2, n, 256, dummy, 2, dummy, dummy, 0, d(-1.0), d(1e-14), 10, dummy, dummy, 1 << 40, None) == \
+        gbx.GBX_ERR_ARG  # FP64-route threshold must be >= 0
+    assert ex(2, n, 256, None, 2, dummy, dummy, 0, d(1e4), d(1e-14), 10, dummy, dummy, 1 << 40, None) == \
+        gbx.GBX_ERR_ARG
+    assert ex(2, n, 256, dummy, 2, dummy, dummy, 0, d(1e4), d(1e-14), 10, dummy, dummy, 16, None) == \
+        gbx.GBX_ERR_WORKSPACE
+    assert L.gbx_dposv_mixed_batched_result(2, n, 256, 2, d(1e-14), None, None, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_potrf_mixed(1000, 256, dummy, dummy, 0, d(0.0), d(-1.0), dummy, 1 << 30, None) == gbx.GBX_ERR_ARG

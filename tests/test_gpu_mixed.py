@@ -171,11 +171,11 @@ def test_dposv_mixed_batched_uneven(gbx, cuda, prec):
     work = torch.empty(need.value, dtype=torch.uint8, device=cuda)
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     gbx.call("gbx_potrf_mixed_batched", len(sizes), n32.ctypes.data_as(ctypes.c_void_p), NB,
-             ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(Wb.data_ptr()), gbx.PREC[prec], 0.0, None,
-             ctypes.c_void_p(work.data_ptr()), need.value, s)
+             ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(Wb.data_ptr()), gbx.PREC[prec], 0.0, gbx.FP64_DIAG_COND,
+             None, ctypes.c_void_p(work.data_ptr()), need.value, s)
     info = np.zeros(len(sizes), dtype=np.int32)
     gbx.call("gbx_potrf_mixed_batched_info", ctypes.c_void_p(work.data_ptr()), len(sizes),
-             n32.ctypes.data_as(ctypes.c_void_p), NB, info.ctypes.data_as(ctypes.c_void_p), None, s)
+             n32.ctypes.data_as(ctypes.c_void_p), NB, info.ctypes.data_as(ctypes.c_void_p), None, None, s)
     assert not info.any()
     for k, n in enumerate(sizes):
         n = int(n)
@@ -248,3 +248,80 @@ def test_tune_mixed_batched_picks_a_converged_configuration(gbx, cuda):
                                                                  for nb in (256, 512)}
     assert best["ms"] == min(c["ms"] for c in best["candidates"] if c["ok"])
     assert sum(c["ok"] for c in best["candidates"]) >= 4, best["candidates"]
+
+
+# ---- FP64 route of the diagonal POTRF ------------------------------------------------------------
+def test_fp64_diag_route_threshold(gbx, cuda):
+    """Threshold 0 sends every diagonal tile to the FP64 POTRF, a huge one none; either factor stays
+    within the bf16 tolerance of the FP64 factor."""
+    import torch
+    N, NB = 2048, 512
+    A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
+    gbx.gen_uniform_sym(A, N, NB, seed=42)
+    ref = A.cpu().numpy().copy()
+    oracle.load_openblas()
+    assert oracle.potrf_tiled(ref, N, NB, nthreads=0, use_blas=oracle.lib().orc_blas_loaded())[0] == 0
+    L64 = oracle.tiles_to_lower(ref, N, NB)
+    for thr, expect in ((0.0, N // NB), (1e300, 0)):
+        W, work, st, cond, nf = gbx.potrf_mixed(A, N, NB, prec="bf16", fp64_diag_cond=thr, with_fp64_tiles=True)
+        assert st == 0 and nf == expect, (thr, st, nf)
+        Lw = oracle.tiles_to_lower(W.double().cpu().numpy(), N, NB)
+        assert np.abs(Lw - L64).max() / np.abs(L64).max() <= 3e-2
+
+
+def test_fp64_diag_route_by_condition_estimate(gbx, cuda):
+    """A diagonal tile scaled to a diagonal ratio of 1e6 (D A D, D = 10^(3 i / NB) on the first tile's
+    rows) exceeds the default threshold and alone takes the FP64 route; the solve still reaches
+    1e-14, and the FP64 route can be forced for every tile of the same system."""
+    import torch
+    N, NB, nrhs = 1536, 512, 2
+    Ad = oracle.uniform_sym_full(N, 11)
+    d = np.ones(N)
+    d[:NB] = 10.0 ** (3.0 * np.arange(NB) / NB)
+    Ad = Ad * d[:, None] * d[None, :]
+    A = torch.from_numpy(np.ascontiguousarray(oracle.tiles_from_full(Ad, NB))).to(cuda)
+    Bn = workloads.rhs(N, nrhs, seed=3)
+    B = torch.from_numpy(Bn).to(cuda)
+    for thr, expect in ((gbx.FP64_DIAG_COND, 1), (0.0, N // NB)):
+        X, info, st = gbx.dposv_mixed(A, N, NB, B, prec="fp16", tol=1e-14, maxiter=300, fp64_diag_cond=thr)
+        assert st == 0, info
+        assert info["fp64_diag_tiles"] == expect, info
+        assert info["backward_error"] <= 1e-14, info
+        Xn = X.cpu().numpy()
+        anorm = np.abs(Ad).sum(1).max()
+        for j in range(nrhs):
+            be = np.abs(Bn[j] - Ad @ Xn[j]).max() / (anorm * np.abs(Xn[j]).max() + np.abs(Bn[j]).max())
+            assert be <= 1.5e-14, be
+
+
+# ---- the batched solve as one CUDA graph -----------------------------------------------------------
+def test_batched_mixed_solve_captured_in_cuda_graph(gbx, cuda):
+    """Plan once, capture the run (factorisation with its retry loop, CG with device-side
+    coefficients and convergence tests as WHILE nodes) in a torch CUDA graph, replay it twice on
+    fresh right-hand sides: every matrix meets 1e-14 and the solution agrees with the uncaptured
+    solve."""
+    import torch
+    NB, nrhs = 256, 2
+    sizes = np.array([700, 256, 1300, 1024, 90, 513])
+    A, B = workloads.householder_batch(sizes, NB, 2, 1e4, 7, cuda, nrhs=nrhs)
+    X0, infos0, st0 = gbx.dposv_mixed_batched(A, sizes, NB, B, nrhs, prec="fp16", tol=1e-14, maxiter=300)
+    assert st0 == 0
+    solver = gbx.MixedBatchedSolver(sizes, NB, nrhs, prec="fp16", device=cuda)
+    W = torch.empty(A.numel(), dtype=torch.float32, device=cuda)
+    Bg = torch.zeros_like(B)
+    X = torch.zeros_like(B)
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+        solver.run(A, Bg, X, W, tol=1e-14, maxiter=300, stream=side)
+    for rep in range(2):
+        Bg.copy_(B * (1 + rep))
+        X.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        infos, st = solver.result()
+        assert st == 0, infos
+        assert all(i["backward_error"] <= 1e-14 for i in infos), infos
+        assert [i["iterations"] for i in infos] == [i["iterations"] for i in infos0] or rep == 1
+        rel = ((X - X0 * (1 + rep)).abs().max() / (X0 * (1 + rep)).abs().max()).item()
+        assert rel <= 1e4 * 1e-13, rel

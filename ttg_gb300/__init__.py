@@ -61,8 +61,8 @@ SIGNATURES = {
     "gbx_gemm_bf16_nt_f32": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp]),
     "gbx_dgen_lowrank_sym_tiled": (_i, [_i, _i, _vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "gbx_potrf_mixed_bufferSize": (_i, [_i, _i, _szp]),
-    "gbx_potrf_mixed": (_i, [_i, _i, _vp, _vp, _i, _d, _vp, _sz, _vp]),
-    "gbx_potrf_mixed_info": (_i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_float), _vp]),
+    "gbx_potrf_mixed": (_i, [_i, _i, _vp, _vp, _i, _d, _d, _vp, _sz, _vp]),
+    "gbx_potrf_mixed_info": (_i, [_vp, _i, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), _vp]),
     "gbx_spotri_diag": (_i, [_i, _i, _vp, _vp, _vp]),
     "gbx_sprecond": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp]),
     "gbx_dsymm_tiled": (_i, [_i, _i, _vp, _i, _d, _vp, _d, _vp, _vp]),
@@ -71,7 +71,7 @@ SIGNATURES = {
     "gbx_dgen_uniform_sym_batched": (_i, [_i, _vp, _vp, _ull, _vp, _vp]),
     "gbx_dposv_batched": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
     "gbx_dposv_batched_ex": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp, _i, _vp, _sz, _vp]),
-    "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
+    "gbx_dposv_mixed": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _sz, _vp, _vp]),
     "gbx_dpotri_tiled_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dpotri_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
     "gbx_split_f64": (_i, [_vp, _vp, _vp, ctypes.c_longlong, _vp]),
@@ -80,10 +80,13 @@ SIGNATURES = {
     "gbx_dposv_tiled_host_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dposv_tiled_host": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "gbx_potrf_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _szp]),
-    "gbx_potrf_mixed_batched": (_i, [_i, _vp, _i, _vp, _vp, _i, _d, _vp, _vp, _sz, _vp]),
-    "gbx_potrf_mixed_batched_info": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp]),
+    "gbx_potrf_mixed_batched": (_i, [_i, _vp, _i, _vp, _vp, _i, _d, _d, _vp, _vp, _sz, _vp]),
+    "gbx_potrf_mixed_batched_info": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
     "gbx_dposv_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _i, _szp]),
-    "gbx_dposv_mixed_batched": (_i, [_i, _vp, _i, _vp, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp, _vp]),
+    "gbx_dposv_mixed_batched": (_i, [_i, _vp, _i, _vp, _i, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _sz, _vp, _vp]),
+    "gbx_dposv_mixed_batched_plan": (_i, [_i, _vp, _i, _i, _i, _vp, _sz, _vp]),
+    "gbx_dposv_mixed_batched_exec": (_i, [_i, _vp, _i, _vp, _i, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _sz, _vp]),
+    "gbx_dposv_mixed_batched_result": (_i, [_i, _vp, _i, _i, _d, _vp, _vp, _vp]),
 }
 
 
@@ -198,15 +201,23 @@ class RefineInfo(ctypes.Structure):
     """gbx_refine_info of include/gbx_potrf.h."""
     _fields_ = [("iterations", ctypes.c_int), ("factor_retries", ctypes.c_int), ("shift", ctypes.c_double),
                 ("backward_error", ctypes.c_double), ("anorm", ctypes.c_double),
-                ("cond_estimate", ctypes.c_float)]
+                ("cond_estimate", ctypes.c_float), ("fp64_diag_tiles", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
-def potrf_mixed(A_tiles, N, NB, prec="bf16", shift=0.0, W=None, work=None, stream=None):
+# Diagonal tiles whose condition estimate (max a_ii / min a_ii after their updates, a lower bound of
+# the tile's condition number) exceeds this go to the FP64 POTRF route of the mixed factorisation:
+# an FP32 Cholesky of a 512-tile can break down from about 1e4 on.
+FP64_DIAG_COND = 1e4
+
+
+def potrf_mixed(A_tiles, N, NB, prec="bf16", shift=0.0, W=None, work=None, stream=None, fp64_diag_cond=FP64_DIAG_COND,
+                with_fp64_tiles=False):
     """Low-precision factorisation of an FP64 tile-major lower matrix into FP32 tiles W.
-    Returns (W, work, status, cond_estimate)."""
+    Returns (W, work, status, cond_estimate) (and the number of diagonal tiles factorised in FP64
+    with with_fp64_tiles=True)."""
     import torch
     need = _sz(0)
     call("gbx_potrf_mixed_bufferSize", N, NB, ctypes.byref(need))
@@ -215,13 +226,18 @@ def potrf_mixed(A_tiles, N, NB, prec="bf16", shift=0.0, W=None, work=None, strea
     if work is None or work.numel() < need.value:
         work = torch.empty(need.value, dtype=torch.uint8, device=A_tiles.device)
     s = _stream(stream)
-    call("gbx_potrf_mixed", N, NB, _ptr(A_tiles), _ptr(W), PREC[prec], float(shift), _ptr(work), need.value, s)
+    call("gbx_potrf_mixed", N, NB, _ptr(A_tiles), _ptr(W), PREC[prec], float(shift), float(fp64_diag_cond), _ptr(work),
+         need.value, s)
     cond = ctypes.c_float(0)
-    st = call("gbx_potrf_mixed_info", _ptr(work), N, NB, ctypes.byref(cond), s)
+    nf = ctypes.c_int(0)
+    st = call("gbx_potrf_mixed_info", _ptr(work), N, NB, ctypes.byref(cond), ctypes.byref(nf), s)
+    if with_fp64_tiles:
+        return W, work, st, cond.value, nf.value
     return W, work, st, cond.value
 
 
-def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=None, work=None, W=None):
+def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=None, work=None, W=None,
+                fp64_diag_cond=FP64_DIAG_COND):
     """Solves A X = B to FP64 backward error `tol` (B: (nrhs, N) CUDA float64, rows = right-hand
     sides). Returns (X, info dict, status)."""
     import torch
@@ -234,8 +250,9 @@ def dposv_mixed(A_tiles, N, NB, B, prec="bf16", tol=1e-14, maxiter=200, stream=N
         W = torch.empty(A_tiles.numel(), dtype=torch.float32, device=A_tiles.device)
     X = torch.empty_like(B)
     info = RefineInfo()
-    st = lib().gbx_dposv_mixed(N, NB, _ptr(A_tiles), nrhs, _ptr(B), _ptr(X), PREC[prec], float(tol), int(maxiter),
-                               _ptr(W), _ptr(work), need.value, ctypes.byref(info), _stream(stream))
+    st = lib().gbx_dposv_mixed(N, NB, _ptr(A_tiles), nrhs, _ptr(B), _ptr(X), PREC[prec], float(fp64_diag_cond),
+                               float(tol), int(maxiter), _ptr(W), _ptr(work), need.value, ctypes.byref(info),
+                               _stream(stream))
     if st < 0 and st != GBX_ERR_NOCONV:
         raise GbxError("gbx_dposv_mixed", st)
     return X, info.as_dict(), st
@@ -315,7 +332,7 @@ def batched_tile_offsets(sizes, NB):
 
 
 def dposv_mixed_batched(A_tiles, sizes, NB, B, nrhs, prec="fp16", tol=1e-14, maxiter=200, stream=None, work=None,
-                        W=None):
+                        W=None, fp64_diag_cond=FP64_DIAG_COND):
     """Batched mixed-precision solve. A_tiles: concatenated tile-major lower matrices (CUDA float64,
     batched_tile_offsets layout); B: concatenated column-major n_k x nrhs right-hand sides (CUDA
     float64). Returns (X, list of per-matrix info dicts, status)."""
@@ -333,11 +350,48 @@ def dposv_mixed_batched(A_tiles, sizes, NB, B, nrhs, prec="fp16", tol=1e-14, max
     X = torch.empty_like(B)
     infos = (RefineInfo * batch)()
     st = lib().gbx_dposv_mixed_batched(batch, n.ctypes.data_as(ctypes.c_void_p), NB, _ptr(A_tiles), nrhs, _ptr(B),
-                                       _ptr(X), PREC[prec], float(tol), int(maxiter), _ptr(W), _ptr(work),
-                                       need.value, ctypes.cast(infos, ctypes.c_void_p), _stream(stream))
+                                       _ptr(X), PREC[prec], float(fp64_diag_cond), float(tol), int(maxiter), _ptr(W),
+                                       _ptr(work), need.value, ctypes.cast(infos, ctypes.c_void_p), _stream(stream))
     if st < 0 and st != GBX_ERR_NOCONV:
         raise GbxError("gbx_dposv_mixed_batched", st)
     return X, [i.as_dict() for i in infos], st
+
+
+class MixedBatchedSolver:
+    """The batched mixed-precision solve split as the C ABI offers it: the plan (task tables, once per
+    batch shape; synchronises), the run (no host synchronisation, no allocation: capturable in a
+    CUDA graph, e.g. torch.cuda.graph) and the result (synchronises). A, B, X, W: CUDA float64
+    tensors laid out as for dposv_mixed_batched; X receives the solutions."""
+
+    def __init__(self, sizes, NB, nrhs, prec="fp16", device=None, work=None):
+        import numpy as np
+        import torch
+        self.n = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32))
+        self.batch, self.NB, self.nrhs, self.prec = len(self.n), NB, nrhs, prec
+        need = _sz(0)
+        call("gbx_dposv_mixed_batched_bufferSize", self.batch, self._n(), NB, nrhs, ctypes.byref(need))
+        self.work_bytes = need.value
+        if work is None or work.numel() < need.value:
+            work = torch.empty(need.value, dtype=torch.uint8, device=device)
+        self.work = work
+        call("gbx_dposv_mixed_batched_plan", self.batch, self._n(), NB, nrhs, PREC[prec], _ptr(work), need.value,
+             _stream(None))
+
+    def _n(self):
+        return self.n.ctypes.data_as(ctypes.c_void_p)
+
+    def run(self, A_tiles, B, X, W, tol=1e-14, maxiter=200, fp64_diag_cond=FP64_DIAG_COND, stream=None):
+        call("gbx_dposv_mixed_batched_exec", self.batch, self._n(), self.NB, _ptr(A_tiles), self.nrhs, _ptr(B), _ptr(X),
+             PREC[self.prec], float(fp64_diag_cond), float(tol), int(maxiter), _ptr(W), _ptr(self.work),
+             self.work_bytes, _stream(stream))
+
+    def result(self, tol=1e-14, stream=None):
+        infos = (RefineInfo * self.batch)()
+        st = lib().gbx_dposv_mixed_batched_result(self.batch, self._n(), self.NB, self.nrhs, float(tol), _ptr(self.work),
+                                                  ctypes.cast(infos, ctypes.c_void_p), _stream(stream))
+        if st < 0 and st != GBX_ERR_NOCONV:
+            raise GbxError("gbx_dposv_mixed_batched_result", st)
+        return [i.as_dict() for i in infos], st
 
 
 def gen_lowrank(tiles, N, NB, lam, U, V, G, stream=None):

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <mutex>
 #include <vector>
 
@@ -96,7 +97,8 @@ __host__ __device__ inline TileKey decode(long long t, int NT) {
 struct MixMat {
   long long slot0;
   int N, NT, cnt0, id;  // id: index into the per-matrix info / condition arrays
-  int dcnt0, pad;       // first counter of the diagonal tiles' 128-block counters (NT * nb * nb)
+  int dcnt0;            // first counter of the diagonal tiles' 128-block counters (NT * nb * nb)
+  int dt0;              // first diagonal tile in the per-diagonal-tile arrays (FP64 scratch, route)
 };
 // a run of consecutive queue positions [start, next segment's start) holding, `mult` slots each,
 // the tile tasks task0.. of one matrix's own task order. Segments are ordered by phase (phase p of a matrix: its
@@ -132,13 +134,18 @@ struct Params {
   int* cnt;
   int* minfo;       // per matrix: 0 or the first bad pivot (1-based, global row)
   float* cond_est;  // per matrix: max over diagonal tiles of (max L_ii / min L_ii)^2
+  double* D64;      // FP64 scratch tile of every diagonal tile (FP64 route), NB x NB each
+  int* route;       // per diagonal tile: 1 when its POTRF took the FP64 route
+  int* nfp64;       // per matrix: diagonal tiles factorised in FP64
+  float fp64_cond;  // diagonal-ratio threshold of the FP64 route (+inf: never)
+  const int* dsel;  // per matrix (device): factorise only the matrices with dsel[id] != 0; null: all
   uint64_t timeout_ns;
 };
 
 // the matrix a task belongs to, as every thread of the CTA sees it
 struct Cur {
   long long slot0;
-  int N, NT, id;
+  int N, NT, id, dt0;  // dt0: index of its first diagonal tile in the per-diagonal-tile arrays
   int* cnt;
 };
 
@@ -188,16 +195,113 @@ __device__ inline Mini mini_decode(int sub, int nb) {
   return Mini{2, p, j + u, j};
 }
 
+// Route of a diagonal tile's POTRF, chosen by its first mini-task PF(0) from the tile after all its
+// SYRK updates: FP64 when the tile's condition estimate max_i a_ii / min_i a_ii (a lower bound of its
+// 2-norm condition number) exceeds P.fp64_cond, or when a diagonal entry is not positive; else FP32.
+// The FP64 route copies the tile's lower triangle into its FP64 scratch tile, runs the same
+// mini-flowgraph in FP64 there (op_potrf / op_trsm / op_gemm_nt<double>), and each block's final
+// writer (PF(j) for block (j,j), PT(j,i) for block (i,j)) also rounds the block into W.
+__device__ bool choose_fp64_route(const Params& P, const float* A, int n, float* sm) {
+  float mn = 3.0e38f, mx = 0.f;
+  for (int i = threadIdx.x; i < n; i += kThr) {
+    const float d = __ldcg(A + i + (long long)i * P.NB);
+    mn = fminf(mn, d);
+    mx = fmaxf(mx, d);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    sm[warp] = mn;
+    sm[8 + warp] = mx;
+  }
+  __syncthreads();
+  mn = sm[0];
+  mx = sm[8];
+  for (int w = 1; w < kThr / 32; ++w) {
+    mn = fminf(mn, sm[w]);
+    mx = fmaxf(mx, sm[8 + w]);
+  }
+  __syncthreads();
+  return !(mn > 0.f) || mx > P.fp64_cond * mn;
+}
+
+__device__ void round_block_to_w(const double* D, float* A, int ld, int di, int dj, bool diag) {
+  for (int idx = threadIdx.x; idx < kBlk * dj; idx += kThr) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    if (i < di && (!diag || i >= j)) A[i + (long long)j * ld] = (float)D[i + (long long)j * ld];
+  }
+}
+
+// One mini-task of the FP64 route on the tile's FP64 scratch D (NB x NB, column-major); the final
+// writer of a block also rounds it into W (A). Kept out of line: the FP64 block ops need many
+// registers, and inlined they would make the compiler spill in the kernel's FP32 and tensor paths.
+__device__ __noinline__ int potrf_mini_fp64(double* D, float* A, int NB, int n, const Mini& mk, double* sm) {
+  auto blk = [&](int i, int j) { return A + kBlk * i + (long long)kBlk * j * NB; };
+  auto dblk = [&](int i, int j) { return D + kBlk * i + (long long)kBlk * j * NB; };
+  auto bdim = [&](int i) { return min(kBlk, n - kBlk * i); };
+  const int dp = bdim(mk.p);
+  if (dp <= 0) return 0;
+  if (mk.kind == 0) {
+    const int info = op_potrf<double>(dblk(mk.p, mk.p), NB, dp, sm);
+    __syncthreads();
+    round_block_to_w(dblk(mk.p, mk.p), blk(mk.p, mk.p), NB, dp, dp, true);
+    return info;
+  }
+  const int di = bdim(mk.i);
+  if (di <= 0) return 0;
+  if (mk.kind == 1) {
+    op_trsm<double>(dblk(mk.p, mk.p), NB, dblk(mk.i, mk.p), NB, di, dp, sm);
+    __syncthreads();
+    round_block_to_w(dblk(mk.i, mk.p), blk(mk.i, mk.p), NB, di, dp, false);
+    return 0;
+  }
+  const int dj = bdim(mk.j);
+  if (dj > 0) op_gemm_nt<double>(dblk(mk.i, mk.p), NB, dblk(mk.j, mk.p), NB, dblk(mk.i, mk.j), NB, di, dj, dp,
+                                 mk.i == mk.j, sm);
+  return 0;
+}
+
 // returns 0 or the 1-based pivot index within the block (PF only)
 __device__ int task_potrf_mini(const Params& P, const Cur& cm, int K, const Mini& mk, float* sm) {
   const int NB = P.NB, n = tdim(K, cm, NB);
   float* A = P.W + (cm.slot0 + slot_of(K, K, cm.NT)) * (long long)NB * NB;
+  double* D = P.D64 + (cm.dt0 + K) * (long long)NB * NB;  // the tile's FP64 scratch
+  int* route = P.route + cm.dt0 + K;
   auto blk = [&](int i, int j) { return A + kBlk * i + (long long)kBlk * j * NB; };
   auto bdim = [&](int i) { return min(kBlk, n - kBlk * i); };  // <= 0: past the ragged edge
   const int dp = bdim(mk.p);
+  __shared__ int s_route;
+  if (mk.kind == 0 && mk.p == 0) {  // PF(0) decides the tile's route for every later mini-task
+    const bool f64 = choose_fp64_route(P, A, n, sm);
+    if (f64) {
+      for (long long idx = threadIdx.x; idx < (long long)n * NB; idx += kThr) {
+        const int i = (int)(idx % NB), j = (int)(idx / NB);
+        if (i < n && i >= j) D[idx] = (double)__ldcg(A + idx);
+      }
+      if (threadIdx.x == 0) atomicAdd(P.nfp64 + cm.id, 1);
+    }
+    if (threadIdx.x == 0) {
+      *(volatile int*)route = f64 ? 1 : 0;  // made visible with the block's completion signal
+      s_route = f64;
+    }
+    __syncthreads();
+  } else {
+    if (threadIdx.x == 0) s_route = ld_volatile(route);  // PF(0) precedes every mini-task of the tile
+    __syncthreads();
+  }
+  const bool f64 = s_route != 0;
+  if (f64 && mk.kind != 0) {
+    potrf_mini_fp64(D, A, NB, n, mk, (double*)sm);
+    __syncthreads();
+    return 0;
+  }
   if (mk.kind == 0) {
     if (dp <= 0) return 0;
-    const int info = op_potrf<float>(blk(mk.p, mk.p), NB, dp, sm);
+    const int info = f64 ? potrf_mini_fp64(D, A, NB, n, mk, (double*)sm) : op_potrf<float>(blk(mk.p, mk.p), NB, dp, sm);
+    __syncthreads();
     if (info == 0 && threadIdx.x == 0) {  // condition estimate of the block from its factor's diagonal
       float mn = 3.0e38f, mx = 0.f;
       for (int i = 0; i < dp; ++i) {
@@ -403,7 +507,7 @@ __global__ void __launch_bounds__(kThr, 1)
   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ long long s_task, s_slot0;
-  __shared__ int s_go, s_info, s_N, s_NT, s_cnt0, s_id, s_dcnt0, s_sub;
+  __shared__ int s_go, s_info, s_N, s_NT, s_cnt0, s_id, s_dcnt0, s_sub, s_dt0;
   __shared__ float s_colscale[kSubN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -446,18 +550,24 @@ __global__ void __launch_bounds__(kThr, 1)
         s_NT = mm.NT;
         s_cnt0 = mm.cnt0;
         s_id = mm.id;
+        s_dt0 = mm.dt0;
+        // a matrix not selected for this launch: its whole task graph is skipped (tasks of one
+        // matrix wait only on the same matrix's counters)
+        if (P.dsel && !P.dsel[mm.id]) s_task = -2;
       } else {
         s_task = -1;
       }
     }
     __syncthreads();
     const long long t = s_task;
+    if (t == -2) continue;
     if (t < 0) break;
     Cur cm;
     cm.slot0 = s_slot0;
     cm.N = s_N;
     cm.NT = s_NT;
     cm.id = s_id;
+    cm.dt0 = s_dt0;
     cm.cnt = P.cnt + s_cnt0;
     const int NT = cm.NT;
     const TileKey tk = decode(t, NT);
@@ -687,8 +797,8 @@ __global__ void shift_diag_kernel(float* W, int N, int NB, int NT, float shift) 
 // workspace layout for a batch (one matrix is the batch of one): run state, completion counters,
 // per-matrix condition estimates and info, the matrix table, row exponents, low-precision copies
 struct Ws {
-  size_t state, cnt, dcnt, cond, minfo, mats, segs, rowexp, lb, total;
-  long long slots, cnts, nsegs, dcnts;
+  size_t state, cnt, dcnt, cond, minfo, nfp64, route, mats, segs, sel, rowexp, lb, d64, total;
+  long long slots, cnts, nsegs, dcnts, dtiles;
 };
 inline size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 int npot_of(int NB) {  // mini-tasks of one POTRF
@@ -698,29 +808,35 @@ int npot_of(int NB) {  // mini-tasks of one POTRF
   return c;
 }
 inline Ws layout_batch(int batch, const int* n, int NB) {
-  long long slots = 0, nsegs = 0, dcnts = 0;
+  long long slots = 0, nsegs = 0, dcnts = 0, dtiles = 0;
   const long long nb = NB / kBlk;
   for (int k = 0; k < batch; ++k) {
     const long long nt = (n[k] + NB - 1) / NB;
     slots += nt * (nt + 1) / 2;
     nsegs += (4 + npot_of(NB)) * nt;  // queue segments: per phase, three groups + POTRF mini-tasks
     dcnts += nt * nb * nb;
+    dtiles += nt;
   }
   Ws w;
   w.nsegs = nsegs;
   w.slots = slots;
   w.cnts = slots;  // one counter per tile
   w.dcnts = dcnts;
+  w.dtiles = dtiles;
   w.state = 0;
   w.cnt = sizeof(DagState);
   w.dcnt = up(w.cnt + (size_t)w.cnts * sizeof(int), 256);
   w.cond = up(w.dcnt + (size_t)w.dcnts * sizeof(int), 256);
   w.minfo = up(w.cond + (size_t)batch * sizeof(float), 256);
-  w.mats = up(w.minfo + (size_t)batch * sizeof(int), 256);
+  w.nfp64 = up(w.minfo + (size_t)batch * sizeof(int), 256);
+  w.route = up(w.nfp64 + (size_t)batch * sizeof(int), 256);
+  w.mats = up(w.route + (size_t)dtiles * sizeof(int), 256);
   w.segs = up(w.mats + (size_t)batch * sizeof(MixMat), 256);
-  w.rowexp = up(w.segs + (size_t)nsegs * sizeof(MixSeg), 1024);
+  w.sel = up(w.segs + (size_t)nsegs * sizeof(MixSeg), 256);
+  w.rowexp = up(w.sel + (size_t)batch * sizeof(int), 1024);
   w.lb = up(w.rowexp + (size_t)slots * NB * sizeof(int), 1024);
-  w.total = w.lb + (size_t)slots * NB * NB * 2;
+  w.d64 = up(w.lb + (size_t)slots * NB * NB * 2, 256);
+  w.total = w.d64 + (size_t)dtiles * NB * NB * sizeof(double);
   return w;
 }
 inline Ws layout(int N, int NB) { return layout_batch(1, &N, NB); }
@@ -745,46 +861,69 @@ using namespace gbx::mixed;
 
 namespace gbx {
 namespace mixed {
-// factorises the selected matrices of a batch (sel[k] != 0; all when sel is null) in one launch.
+// Host side of a batched launch in two parts.
+// plan_batch: the matrix table and the queue segments of every matrix of the batch, uploaded into
+//   the workspace (host to device copies; not capturable).
+// run_batch: clears the run state and counters and launches the persistent kernel over the planned
+//   queue (no host synchronisation, no host to device copy: capturable in a CUDA graph). dsel
+//   (device, per matrix, may be null) selects the matrices to factorise; the others' tasks are
+//   skipped. W must already hold the (shifted) FP32 copy of every selected matrix.
 // A, W: the matrices' tile-major lower storage concatenated in batch order (matrix k's slots follow
-// matrix k-1's). The table is ordered largest first so the longest critical paths start first.
-// w_ready: W already holds fl32(A) for every selected matrix (written by the refinement's single
-// pass over A), so the conversion launches are skipped; only valid with shift == 0.
-int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
-                 const unsigned char* sel, void* work, size_t work_bytes, cudaStream_t s, bool w_ready) {
+// matrix k-1's). The queue puts larger matrices first so the longest critical paths start first.
+struct Shape {
+  int sub_g, sub_t, sub_s, nslot, nb, npot;
+  long long ntasks, nsegs;
+};
+Shape shape_of(int batch, const int* n, int NB) {
+  Shape h;
+  h.sub_g = (NB / kSubM) * (NB / kSubN);
+  h.sub_t = NB / kTrsmRows;
+  h.sub_s = sub_syrk(NB);
+  h.nslot = std::max(std::max(h.sub_g, h.sub_t), h.sub_s);
+  h.nb = NB / kBlk;
+  h.npot = npot_of(NB);
+  h.ntasks = 0;
+  h.nsegs = 0;
+  for (int k = 0; k < batch; ++k) {  // queue slots of a matrix: one per POTRF mini-task, nslot per other task
+    const long long nt = (n[k] + NB - 1) / NB;
+    h.ntasks += nt * h.npot + (num_tile_tasks((int)nt) - nt) * h.nslot;
+  }
+  return h;
+}
+
+int set_kernel_attrs() {
+  std::lock_guard<std::mutex> lk(g_mtx);
+  if (g_attr) return GBX_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaFuncSetAttribute(potrf_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) !=
+      cudaSuccess)
+    return GBX_ERR_CUDA;
+  g_attr = true;
+  return GBX_OK;
+}
+
+int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, cudaStream_t s) {
   const Ws w = layout_batch(batch, n, NB);
   if (work_bytes < w.total) return GBX_ERR_WORKSPACE;
-  {
-    std::lock_guard<std::mutex> lk(g_mtx);
-    if (!g_attr) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      if (cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
-      if (cudaFuncSetAttribute(potrf_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) !=
-          cudaSuccess)
-        return GBX_ERR_CUDA;
-      g_attr = true;
-    }
-  }
-  const int sub_g = (NB / kSubM) * (NB / kSubN);
-  const int sub_t = NB / kTrsmRows;
-  const int nslot = std::max(std::max(sub_g, sub_t), sub_syrk(NB));
-  const int nb = NB / kBlk;
-  int npot = 0;  // mini-tasks of one POTRF
-  for (int p = 0; p < nb; ++p) npot += panel_minis(nb, p);
+  if (int e = set_kernel_attrs()) return e;
+  const Shape h = shape_of(batch, n, NB);
+  const int nb = h.nb, npot = h.npot, nslot = h.nslot;
   // matrix table: slot / counter offsets in batch order, queue order largest first
-  std::vector<long long> slot0(batch), dcnt0(batch);
-  long long acc = 0, dacc = 0;
+  std::vector<long long> slot0(batch), dcnt0(batch), dt0(batch);
+  long long acc = 0, dacc = 0, tacc = 0;
   for (int k = 0; k < batch; ++k) {
     slot0[k] = acc;
     dcnt0[k] = dacc;
+    dt0[k] = tacc;
     const long long nt = (n[k] + NB - 1) / NB;
     acc += nt * (nt + 1) / 2;
     dacc += nt * nb * nb;
+    tacc += nt;
   }
-  std::vector<int> order;
-  for (int k = 0; k < batch; ++k)
-    if (!sel || sel[k]) order.push_back(k);
+  std::vector<int> order(batch);
+  for (int k = 0; k < batch; ++k) order[k] = k;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return n[a] > n[b]; });
   std::vector<MixMat> mats(order.size());
   int maxNT = 0;
@@ -797,14 +936,17 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
     mats[q].cnt0 = (int)slot0[k];
     mats[q].id = k;
     mats[q].dcnt0 = (int)dcnt0[k];
-    mats[q].pad = 0;
+    mats[q].dt0 = (int)dt0[k];
     maxNT = std::max(maxNT, nt);
   }
-  // queue: phase by phase; within a phase, group by group (1: the updates of the next panel's
-  // column, 2: its POTRF, 3: its TRSMs, 4: the trailing updates), within a group the matrices
-  // largest first; the POTRF group goes mini-task by mini-task across the matrices. The CTAs then
-  // find whole groups of independent tasks of many matrices instead of one matrix's dependent
-  // chain.
+  // queue: phase by phase (phase p of a matrix: the tasks between POTRF(p) and POTRF(p+1) in its
+  // own order); within a phase, group by group: 1 the updates of column p by panel p-1, 2 POTRF(p),
+  // 4 the trailing updates of the columns right of p by panel p-1, 3 the TRSMs of column p; within
+  // a group the matrices largest first; the POTRF group goes mini-task by mini-task across the
+  // matrices. The trailing updates do not depend on POTRF(p), so CTAs work on them while the
+  // POTRF mini-flowgraph runs instead of waiting on its TRSMs. Every task's predecessors stay
+  // earlier in the queue (group 4 of phase p needs TRSMs of phase p-1 and updates of phase p-1;
+  // group 3 needs groups 1 and 2 of phase p), so in-order grabbing cannot deadlock.
   std::vector<MixSeg> segs;
   long long task0 = 0;
   auto group_range = [&](int nt, int p, int g, long long& first, long long& last) {
@@ -819,8 +961,10 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
     first = base + lo[g];
     last = base + hi[g];
   };
+  const int group_order[4] = {1, 2, 4, 3};
   for (int p = 0; p < maxNT; ++p)
-    for (int g = 1; g <= 4; ++g) {
+    for (int gi = 0; gi < 4; ++gi) {
+      const int g = group_order[gi];
       if (g == 2)  // the single POTRF of this phase, one slot per mini-task
         for (int u = 0; u < npot; ++u)
           for (size_t q = 0; q < mats.size(); ++q) {
@@ -841,30 +985,33 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
         task0 += (last - first) * nslot;
       }
     }
-  if ((long long)segs.size() > w.nsegs) return GBX_ERR_WORKSPACE;  // the table must fit its reserved space
+  if ((long long)segs.size() > w.nsegs || task0 != h.ntasks) return GBX_ERR_ARG;  // the tables must fit their space
+  // the reserved segment slots past the last one start beyond every queue position, so that the
+  // kernel's search over all w.nsegs slots finds the right segment
+  segs.resize((size_t)w.nsegs, MixSeg{LLONG_MAX, 0, 0, 1, 0, 0});
   char* base = (char*)work;
-  // state, counters, condition estimates and info are cleared for every matrix; the copies and
-  // exponents of the selected matrices are all rewritten by their TRSM tasks before any read
-  if (cudaMemsetAsync(base, 0, w.mats, s) != cudaSuccess) return GBX_ERR_CUDA;
-  if (mats.empty()) return GBX_OK;
   if (cudaMemcpyAsync(base + w.mats, mats.data(), mats.size() * sizeof(MixMat), cudaMemcpyHostToDevice, s) !=
           cudaSuccess ||
       cudaMemcpyAsync(base + w.segs, segs.data(), segs.size() * sizeof(MixSeg), cudaMemcpyHostToDevice, s) !=
           cudaSuccess)
     return GBX_ERR_CUDA;
-  // rows of a ragged tile's low-precision copy past the matrix edge are never written; the tensor
-  // cores read them, but they only reach rows / columns of C that the epilogue does not store
-  for (const MixMat& m : mats) {
-    if (w_ready && shift == 0.0) break;
-    const long long nsl = (long long)m.NT * (m.NT + 1) / 2, nel = nsl * (long long)NB * NB;
-    convert_kernel<<<std::min<long long>(g_sms * 8, (nel + 255) / 256), 256, 0, s>>>(
-        A + m.slot0 * (long long)NB * NB, W + m.slot0 * (long long)NB * NB, nel);
-    if (shift != 0.0)
-      shift_diag_kernel<<<m.NT, 256, 0, s>>>(W + m.slot0 * (long long)NB * NB, m.N, NB, m.NT, (float)shift);
-  }
+  return GBX_OK;
+}
+
+int run_batch(int batch, const int* n, int NB, float* W, int prec, double fp64_cond, const int* dsel, void* work,
+              size_t work_bytes, cudaStream_t s) {
+  const Ws w = layout_batch(batch, n, NB);
+  if (work_bytes < w.total) return GBX_ERR_WORKSPACE;
+  if (int e = set_kernel_attrs()) return e;
+  const Shape h = shape_of(batch, n, NB);
+  char* base = (char*)work;
+  // run state, counters, condition estimates, info, FP64-route counts and routes of every matrix
+  if (cudaMemsetAsync(base, 0, w.mats, s) != cudaSuccess) return GBX_ERR_CUDA;
   CUtensorMap ta, tb;
   const bool bf16 = prec == 0;
   const uint64_t lrows = (uint64_t)w.slots * NB;
+  // rows of a ragged tile's low-precision copy past the matrix edge are never written; the tensor
+  // cores read them, but they only reach rows / columns of C that the epilogue does not store
   if (prec == 2) {  // fp8: rows of NB bytes in the same buffer
     if (int e = tc::make_tmap_kmajor_8b(&ta, base + w.lb, lrows, (uint64_t)NB, (uint64_t)NB, kSubM)) return e;
     if (int e = tc::make_tmap_kmajor_8b(&tb, base + w.lb, lrows, (uint64_t)NB, (uint64_t)NB, kSubN)) return e;
@@ -879,24 +1026,61 @@ int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int
   P.NB = NB;
   P.f16 = prec == 1;
   P.fp8 = prec == 2;
-  P.sub_g = sub_g;
-  P.sub_t = sub_t;
-  P.nb = nb;
-  P.npot = npot;
+  P.sub_g = h.sub_g;
+  P.sub_t = h.sub_t;
+  P.nb = h.nb;
+  P.npot = h.npot;
   P.dcnt = (int*)(base + w.dcnt);
-  P.sub_s = sub_syrk(NB);
-  P.ntasks = task0;
+  P.sub_s = h.sub_s;
+  P.ntasks = h.ntasks;
   P.mats = (const MixMat*)(base + w.mats);
-  P.nmats = (int)mats.size();
+  P.nmats = batch;
   P.segs = (const MixSeg*)(base + w.segs);
-  P.nsegs = (int)segs.size();
+  P.nsegs = (int)w.nsegs;
   P.st = (DagState*)base;
   P.cnt = (int*)(base + w.cnt);
   P.minfo = (int*)(base + w.minfo);
   P.cond_est = (float*)(base + w.cond);
+  P.D64 = (double*)(base + w.d64);
+  P.route = (int*)(base + w.route);
+  P.nfp64 = (int*)(base + w.nfp64);
+  P.fp64_cond = fp64_cond >= 3.0e38 ? INFINITY : (float)fp64_cond;
+  P.dsel = dsel;
   P.timeout_ns = gbx_get_wait_timeout_ns();
   P.trace = current_trace();
   potrf_mixed_kernel<<<g_sms, kThr, kSmemBytes, s>>>(ta, tb, P);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+// device addresses of a batched factorisation's results in its workspace
+struct InfoPtrs {
+  const DagState* st;
+  const int* minfo;
+  const float* cond;
+  const int* nfp64;
+};
+InfoPtrs info_ptrs(int batch, const int* n, int NB, const void* work) {
+  const Ws w = layout_batch(batch, n, NB);
+  const char* b = (const char*)work;
+  return InfoPtrs{(const DagState*)b, (const int*)(b + w.minfo), (const float*)(b + w.cond), (const int*)(b + w.nfp64)};
+}
+
+// W = fl32(A) for the selected matrices (sel host array, null: all), the diagonal scaled by (1 + shift)
+int convert_host_sel(int batch, const int* n, int NB, const double* A, float* W, double shift,
+                     const unsigned char* sel, cudaStream_t s) {
+  if (int e = set_kernel_attrs()) return e;
+  long long slot0 = 0;
+  for (int k = 0; k < batch; ++k) {
+    const int nt = (n[k] + NB - 1) / NB;
+    const long long nsl = (long long)nt * (nt + 1) / 2, nel = nsl * (long long)NB * NB;
+    if (!sel || sel[k]) {
+      convert_kernel<<<std::min<long long>(g_sms * 8, (nel + 255) / 256), 256, 0, s>>>(
+          A + slot0 * (long long)NB * NB, W + slot0 * (long long)NB * NB, nel);
+      if (shift != 0.0)
+        shift_diag_kernel<<<nt, 256, 0, s>>>(W + slot0 * (long long)NB * NB, n[k], NB, nt, (float)shift);
+    }
+    slot0 += nsl;
+  }
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 }  // namespace mixed
@@ -922,11 +1106,10 @@ extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes) {
   return GBX_OK;
 }
 
-extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work,
-                               size_t work_bytes, void* stream) {
-  if (N <= 0 || NB <= 0 || NB % 256 || NB > kMaxNB || !A || !W || !work || prec < 0 || prec > 2)
-    return GBX_ERR_ARG;
-  return launch_batch(1, &N, NB, A, W, prec, shift, nullptr, work, work_bytes, (cudaStream_t)stream, false);
+extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, double fp64_diag_cond,
+                               void* work, size_t work_bytes, void* stream) {
+  if (N <= 0) return GBX_ERR_ARG;
+  return gbx_potrf_mixed_batched(1, &N, NB, A, W, prec, shift, fp64_diag_cond, nullptr, work, work_bytes, stream);
 }
 
 extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes) {
@@ -938,16 +1121,29 @@ extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int N
 }
 
 extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec,
-                                       double shift, const unsigned char* sel, void* work, size_t work_bytes,
-                                       void* stream) {
+                                       double shift, double fp64_diag_cond, const unsigned char* sel, void* work,
+                                       size_t work_bytes, void* stream) {
   size_t need = 0;
   if (int e = gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &need)) return e;
-  if (!A || !W || !work || prec < 0 || prec > 2) return GBX_ERR_ARG;
-  return launch_batch(batch, n, NB, A, W, prec, shift, sel, work, work_bytes, (cudaStream_t)stream, false);
+  if (!A || !W || !work || prec < 0 || prec > 2 || !(fp64_diag_cond >= 0.0)) return GBX_ERR_ARG;
+  if (work_bytes < need) return GBX_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (int e = plan_batch(batch, n, NB, work, work_bytes, s)) return e;
+  if (int e = convert_host_sel(batch, n, NB, A, W, shift, sel, s)) return e;
+  const int* dsel = nullptr;
+  if (sel) {
+    const Ws w = layout_batch(batch, n, NB);
+    std::vector<int> hs(batch);
+    for (int k = 0; k < batch; ++k) hs[k] = sel[k] ? 1 : 0;
+    if (cudaMemcpyAsync((char*)work + w.sel, hs.data(), batch * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return GBX_ERR_CUDA;
+    dsel = (const int*)((char*)work + w.sel);
+  }
+  return run_batch(batch, n, NB, W, prec, fp64_diag_cond, dsel, work, work_bytes, s);
 }
 
 extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info,
-                                            float* cond_est, void* stream) {
+                                            float* cond_est, int* fp64_tiles, void* stream) {
   if (!work || batch <= 0 || !n || NB <= 0) return GBX_ERR_ARG;
   const Ws w = layout_batch(batch, n, NB);
   cudaStream_t s = (cudaStream_t)stream;
@@ -959,20 +1155,25 @@ extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const i
   if (cond_est && cudaMemcpyAsync(cond_est, (const char*)work + w.cond, batch * sizeof(float), cudaMemcpyDeviceToHost,
                                   s) != cudaSuccess)
     return GBX_ERR_CUDA;
+  if (fp64_tiles && cudaMemcpyAsync(fp64_tiles, (const char*)work + w.nfp64, batch * sizeof(int),
+                                    cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return GBX_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
   return st < 0 ? st : GBX_OK;  // < 0: the launch itself failed (timeout)
 }
 
-extern "C" int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, void* stream) {
+extern "C" int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, int* fp64_tiles, void* stream) {
   if (!work || N <= 0 || NB <= 0) return GBX_ERR_ARG;
   const Ws w = layout(N, NB);
-  int st = 0;
+  int st = 0, nf = 0;
   cudaStream_t s = (cudaStream_t)stream;
   if (cudaMemcpyAsync(&st, work, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GBX_ERR_CUDA;
   float c = 0.f;
-  if (cudaMemcpyAsync(&c, (const char*)work + w.cond, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+  if (cudaMemcpyAsync(&c, (const char*)work + w.cond, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&nf, (const char*)work + w.nfp64, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return GBX_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return GBX_ERR_CUDA;
   if (cond_est) *cond_est = c;
+  if (fp64_tiles) *fp64_tiles = nf;
   return st;
 }

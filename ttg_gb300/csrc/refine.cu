@@ -14,27 +14,26 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "block_ops.cuh"
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
 
-extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes);
-extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, void* work,
-                               size_t work_bytes, void* stream);
-extern "C" int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, void* stream);
-extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int NB, size_t* bytes);
-extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec,
-                                       double shift, const unsigned char* sel, void* work, size_t work_bytes,
-                                       void* stream);
-extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info,
-                                            float* cond_est, void* stream);
-
 namespace gbx {
 namespace mixed {
-int launch_batch(int batch, const int* n, int NB, const double* A, float* W, int prec, double shift,
-                 const unsigned char* sel, void* work, size_t work_bytes, cudaStream_t s, bool w_ready);
+int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, cudaStream_t s);
+int run_batch(int batch, const int* n, int NB, float* W, int prec, double fp64_cond, const int* dsel, void* work,
+              size_t work_bytes, cudaStream_t s);
+// device addresses of a batched factorisation's results in its workspace
+struct InfoPtrs {
+  const DagState* st;
+  const int* minfo;
+  const float* cond;
+  const int* nfp64;
+};
+InfoPtrs info_ptrs(int batch, const int* n, int NB, const void* work);
 }  // namespace mixed
 }  // namespace gbx
 
@@ -57,8 +56,13 @@ struct RMat {
 };
 
 // Every kernel body below works on one matrix (pointers already offset to it); the single-matrix
-// kernels call it directly, the batched kernels with the matrix list[blockIdx.z] of the table.
-#define GBX_MAT_OF_BLOCK() const RMat& mt = mats[list[blockIdx.z]]
+// kernels call it directly, the batched kernels with matrix list[1 + blockIdx.z] of the table. A
+// list lives in device memory as {count, table index, ...}: launches cover the largest possible
+// count in z and the slices at or past the current count return at once, so the lists can change
+// on the device between launches of a captured graph.
+#define GBX_MAT_OF_BLOCK()                       \
+  if ((int)blockIdx.z >= list[0]) return;        \
+  const RMat& mt = mats[list[1 + blockIdx.z]]
 
 // Out = L_KK^{-T} (column-major), i.e. row r of Out holds column r of L_KK^{-1}; 128 rows per CTA
 __device__ void diag_inverse_body(const float* W, float* Inv, int N, int NB, int NT, float* sm) {
@@ -121,12 +125,6 @@ __global__ void fwd_diag_kernel(const float* Inv, const float* X, float* Y, int 
   extern __shared__ float xs_f[];  // [nrhs][NB]
   fwd_diag_body(Inv, X, Y, N, NB, NT, K, nrhs, xs_f);
 }
-__global__ void fwd_diag_batched(const RMat* mats, const int* list, const float* Inv, const float* X, float* Y, int NB,
-                                 int K, int nrhs) {
-  extern __shared__ float xs_f[];
-  GBX_MAT_OF_BLOCK();
-  fwd_diag_body(Inv + mt.inv0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, K, nrhs, xs_f);
-}
 
 // forward step, column update: x_M -= L_MK y_K for every M > K; thread per row, y_K in smem
 __device__ void fwd_update_body(const float* W, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs,
@@ -163,12 +161,6 @@ __device__ void fwd_update_body(const float* W, const float* Y, float* X, int N,
 __global__ void fwd_update_kernel(const float* W, const float* Y, float* X, int N, int NB, int NT, int K, int nrhs) {
   extern __shared__ float ys_f[];  // [nrhs][NB]
   fwd_update_body(W, Y, X, N, NB, NT, K, nrhs, ys_f);
-}
-__global__ void fwd_update_batched(const RMat* mats, const int* list, const float* W, const float* Y, float* X, int NB,
-                                   int K, int nrhs) {
-  extern __shared__ float ys_f[];
-  GBX_MAT_OF_BLOCK();
-  fwd_update_body(W + mt.slot0 * NB * NB, Y + mt.vec0, X + mt.vec0, mt.N, NB, mt.NT, K, nrhs, ys_f);
 }
 
 // backward step, diagonal part: z_K = L_KK^{-T} y_K. A CTA owns 32 output rows (lanes, coalesced
@@ -210,12 +202,6 @@ __global__ void bwd_diag_kernel(const float* Inv, const float* Y, float* X, int 
   extern __shared__ float ys_f[];  // [nrhs][NB] then [8 warps][nrhs][32] partial sums
   bwd_diag_body(Inv, Y, X, N, NB, NT, K, nrhs, ys_f);
 }
-__global__ void bwd_diag_batched(const RMat* mats, const int* list, const float* Inv, const float* Y, float* X, int NB,
-                                 int K, int nrhs) {
-  extern __shared__ float ys_f[];
-  GBX_MAT_OF_BLOCK();
-  bwd_diag_body(Inv + mt.inv0 * NB * NB, Y + mt.vec0, X + mt.vec0, mt.N, NB, mt.NT, K, nrhs, ys_f);
-}
 
 // backward step, column update: y_J -= L_KJ^T z_K for every J < K; warp per output element c
 __device__ void bwd_update_body(const float* W, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs,
@@ -249,12 +235,6 @@ __device__ void bwd_update_body(const float* W, const float* X, float* Y, int N,
 __global__ void bwd_update_kernel(const float* W, const float* X, float* Y, int N, int NB, int NT, int K, int nrhs) {
   extern __shared__ float zs_f[];  // [nrhs][NB]
   bwd_update_body(W, X, Y, N, NB, NT, K, nrhs, zs_f);
-}
-__global__ void bwd_update_batched(const RMat* mats, const int* list, const float* W, const float* X, float* Y, int NB,
-                                   int K, int nrhs) {
-  extern __shared__ float zs_f[];
-  GBX_MAT_OF_BLOCK();
-  bwd_update_body(W + mt.slot0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, K, nrhs, zs_f);
 }
 
 __global__ void d2s_kernel(const double* in, float* out, long long n) {
@@ -317,12 +297,6 @@ __global__ void symm_rows_kernel(const double* A, const double* X, double* Y, in
   extern __shared__ double xs_d[];  // [nrhs][512]
   symm_rows_body(A, X, Y, N, NB, NT, nrhs, alpha, xs_d);
 }
-__global__ void symm_rows_batched(const RMat* mats, const int* list, const double* A, const double* X, double* Y, int NB,
-                                  int nrhs, double alpha) {
-  extern __shared__ double xs_d[];
-  GBX_MAT_OF_BLOCK();
-  symm_rows_body(A + mt.slot0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xs_d);
-}
 
 __device__ void symm_cols_body(const double* A, const double* X, double* Y, int N, int NB, int NT, int nrhs,
                                double alpha, double* xs_d) {
@@ -362,12 +336,6 @@ __global__ void symm_cols_kernel(const double* A, const double* X, double* Y, in
                                  double alpha) {
   extern __shared__ double xs_d[];  // [nrhs][512]
   symm_cols_body(A, X, Y, N, NB, NT, nrhs, alpha, xs_d);
-}
-__global__ void symm_cols_batched(const RMat* mats, const int* list, const double* A, const double* X, double* Y, int NB,
-                                  int nrhs, double alpha) {
-  extern __shared__ double xs_d[];
-  GBX_MAT_OF_BLOCK();
-  symm_cols_body(A + mt.slot0 * NB * NB, X + mt.vec0, Y + mt.vec0, mt.N, NB, mt.NT, nrhs, alpha, xs_d);
 }
 
 // ---- the same product in double-float arithmetic (FP32 pairs) for the refinement's residuals ----
@@ -931,8 +899,9 @@ __device__ void sweep_bwd_upd(const float* L, const float* X, float* Y, int N, i
 
 template <int NR>
 __global__ void __launch_bounds__(256) sweep_kernel(int dir, const RMat* mats, const SweepTask* tasks, int ntasks,
-                                                    const float* W, const float* Inv, float* Xf, float* Yf, int NB,
-                                                    int nrhs, int* cnt, int* flag, DagState* st, uint64_t timeout_ns) {
+                                                    const int* active, const float* W, const float* Inv, float* Xf,
+                                                    float* Yf, int NB, int nrhs, int* cnt, int* flag, DagState* st,
+                                                    uint64_t timeout_ns) {
   extern __shared__ __align__(16) float vs_f[];  // [NR][512] vector, then [16][NR][64] partial sums
   __shared__ int s_t, s_ok;
   for (;;) {
@@ -945,6 +914,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(int dir, const RMat* mats, c
     __syncthreads();
     if (s_t < 0) break;
     const SweepTask tk = tasks[s_t];
+    // tasks of a matrix that is not in this sweep: skipped (no task of another matrix waits on them)
+    if (active && !active[tk.q]) continue;
     const RMat& mt = mats[tk.q];
     const int N = mt.N, NT = mt.NT;
     int* c = cnt + mt.inv0;
@@ -1007,12 +978,13 @@ int set_sweep_attrs(int big) {
 // shared memory of a sweep CTA: the vector, then the partial sums
 inline size_t sweep_smem(int NR) { return (size_t)NR * 512 * sizeof(float) + (size_t)16 * NR * 64 * sizeof(float); }
 void launch_sweep(int dir, int grid, cudaStream_t s, const RMat* mats, const SweepTask* tasks, int ntasks,
-                  const float* W, const float* Inv, float* Xf, float* Yf, int NB, int nrhs, int* cnt, int* flag,
-                  DagState* st, uint64_t timeout_ns) {
+                  const int* active, const float* W, const float* Inv, float* Xf, float* Yf, int NB, int nrhs,
+                  int* cnt, int* flag, DagState* st, uint64_t timeout_ns) {
   const int NRb = nrhs <= 1 ? 1 : nrhs <= 2 ? 2 : nrhs <= 4 ? 4 : nrhs <= 8 ? 8 : 16;
   const size_t vs = sweep_smem(NRb);
-#define GBX_SWEEP(NR)                                                                                              \
-  sweep_kernel<NR><<<grid, 256, vs, s>>>(dir, mats, tasks, ntasks, W, Inv, Xf, Yf, NB, nrhs, cnt, flag, st, timeout_ns)
+#define GBX_SWEEP(NR)                                                                                          \
+  sweep_kernel<NR><<<grid, 256, vs, s>>>(dir, mats, tasks, ntasks, active, W, Inv, Xf, Yf, NB, nrhs, cnt, flag, st, \
+                                         timeout_ns)
   if (nrhs <= 1) GBX_SWEEP(1);
   else if (nrhs <= 2) GBX_SWEEP(2);
   else if (nrhs <= 4) GBX_SWEEP(4);
@@ -1059,7 +1031,8 @@ __device__ void colstats_body(const double* a, const double* b, int N, double* o
 // whose vectors are at vec0 / nrhs)
 __global__ void colstats_batched(const RMat* mats, const int* list, const double* a, const double* b, int nrhs,
                                  int ncols, double* out) {
-  const int id = list[blockIdx.z];
+  if ((int)blockIdx.z >= list[0]) return;
+  const int id = list[1 + blockIdx.z];
   const RMat& mt = mats[id];
   const long long off = ncols == nrhs ? mt.vec0 : mt.vec0 / nrhs;
   colstats_body(a + off, b ? b + off : nullptr, mt.N, out + (long long)id * kMaxRhs * 3);
@@ -1079,13 +1052,14 @@ __device__ void axpy_cols_body(double* y, const double* x, const double* coef, d
 // coef: [matrix id][kMaxRhs]
 __global__ void axpy_cols_batched(const RMat* mats, const int* list, double* y, const double* x, const double* coef,
                                   double sign, int nrhs, int xscale_mode) {
-  const int id = list[blockIdx.z];
+  if ((int)blockIdx.z >= list[0]) return;
+  const int id = list[1 + blockIdx.z];
   const RMat& mt = mats[id];
   axpy_cols_body(y + mt.vec0, x + mt.vec0, coef + (long long)id * kMaxRhs, sign, mt.N, nrhs, xscale_mode);
 }
 // y := x (the matrix's vectors)
 __global__ void copy_vec_batched(const RMat* mats, const int* list, double* y, const double* x, int nrhs) {
-  const RMat& mt = mats[list[blockIdx.z]];
+  GBX_MAT_OF_BLOCK();
   const long long n = (long long)mt.N * nrhs;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     y[mt.vec0 + i] = x[mt.vec0 + i];
@@ -1111,12 +1085,6 @@ int set_attrs() {
       cudaFuncSetAttribute(symm_cols_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       cudaFuncSetAttribute(diag_inverse_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(fwd_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(fwd_update_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(bwd_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(bwd_update_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(symm_rows_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
-      cudaFuncSetAttribute(symm_cols_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, big) != cudaSuccess ||
       set_df_attrs<1>(big) || set_df_attrs<2>(big) || set_df_attrs<4>(big) || set_df_attrs<8>(big) ||
       set_df_attrs<16>(big) || set_sweep_attrs<1>(big) || set_sweep_attrs<2>(big) || set_sweep_attrs<4>(big) ||
       set_sweep_attrs<8>(big) || set_sweep_attrs<16>(big))
@@ -1185,21 +1153,55 @@ extern "C" int gbx_dsymm_tiled(int N, int NB, const double* A, int nrhs, double 
 }
 
 namespace {
+// ---- the batched refinement: plan once, then a device-driven run ----------------------------------
+// Per-matrix record kept on the device during a run; the host reads it once at the end.
+struct DevRec {
+  double shift, backward_error, anorm;
+  float cond;
+  int iterations, retries, fp64_tiles, piv;  // piv: first bad pivot of the last failed attempt, else 0
+  int live;                                 // 1 when the matrix has a factor
+  int pad;
+};
+// Run state of one workspace.
+struct RunState {
+  unsigned long long sig;  // signature of the plan in this workspace (written by the plan)
+  int status;              // 0, GBX_ERR_ARG (exec does not match the plan) or GBX_ERR_TIMEOUT (factorisation)
+  int attempt;             // factorisations launched
+  int it;                  // CG iterations run (by any matrix)
+  int pad;
+  double shift;            // diagonal shift of the next factorisation attempt
+};
+
 // workspace of the batched refinement (the factor's workspace first)
 struct BLayout {
-  size_t fwork_bytes, inv, R, Z, P, Q, tmp, rowsum, stats, coef, mats, list, ahi, alo, sweep, tasks, total;
+  size_t fwork_bytes, inv, R, Z, P, Q, tmp, rowsum, stats, coef, mats, ahi, alo, sweep, tasks, rs, rec, fail, lists,
+      flags, rz, norms, total;
+  long long nf, nb;  // forward / backward sweep tasks
+  long long nvec, sumN, sumNT;  // vector entries (sum of n * nrhs), sum of orders, sum of tile counts
+  int maxNT, maxslots, maxN;
 };
 BLayout blayout(int batch, const int* n, int NB, int nrhs) {
   BLayout b;
   b.fwork_bytes = 0;
   gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &b.fwork_bytes);
   long long sumNT = 0, sumN = 0, slots = 0;
+  b.maxNT = b.maxslots = b.maxN = 0;
+  b.nf = b.nb = 0;
   for (int k = 0; k < batch; ++k) {
     const long long nt = (n[k] + NB - 1) / NB;
     sumNT += nt;
     sumN += n[k];
     slots += nt * (nt + 1) / 2;
+    b.maxNT = std::max(b.maxNT, (int)nt);
+    b.maxslots = std::max(b.maxslots, (int)(nt * (nt + 1) / 2));
+    b.maxN = std::max(b.maxN, n[k]);
+    // forward: NT diagonal tasks + NT(NT-1)/2 updates; backward the same
+    b.nf += nt * kDiagSubs + nt * (nt - 1) / 2 * kUpdSubs;
   }
+  b.nb = b.nf;
+  b.sumN = sumN;
+  b.sumNT = sumNT;
+  b.nvec = sumN * nrhs;
   auto up = [](size_t x) { return (x + 255) / 256 * 256; };
   const size_t vec = (size_t)sumN * nrhs;
   size_t o = up(b.fwork_bytes);
@@ -1223,18 +1225,507 @@ BLayout blayout(int batch, const int* n, int NB, int nrhs) {
   o += up((size_t)2 * batch * kMaxRhs * 8);
   b.mats = o;
   o += up((size_t)batch * sizeof(RMat));
-  b.list = o;
-  o += up((size_t)batch * sizeof(int));
   b.ahi = o;  // A split into FP32 pairs for the double-float residuals
   o += up((size_t)slots * NB * NB * sizeof(float));
   b.alo = o;
   o += up((size_t)slots * NB * NB * sizeof(float));
   b.sweep = o;  // two run states, then forward / backward row counters and flags
   o += up(2 * sizeof(DagState) + (size_t)4 * sumNT * sizeof(int));
-  b.tasks = o;  // forward then backward task lists (sub-tasks of every tile)
-  o += up((size_t)2 * slots * std::max(kDiagSubs, kUpdSubs) * sizeof(SweepTask));
+  b.tasks = o;  // forward then backward task lists (sub-tasks of every tile of every matrix)
+  o += up((size_t)(b.nf + b.nb) * sizeof(SweepTask));
+  b.rs = o;
+  o += up(sizeof(RunState));
+  b.rec = o;
+  o += up((size_t)batch * sizeof(DevRec));
+  b.fail = o;  // per matrix: selected for the next factorisation attempt
+  o += up((size_t)batch * sizeof(int));
+  b.lists = o;  // five lists {count, entries}: all (largest first), live, active, true-residual, refactor
+  o += up((size_t)5 * (batch + 1) * sizeof(int));
+  b.flags = o;  // per matrix: live, active (the sweeps' selection)
+  o += up((size_t)2 * batch * sizeof(int));
+  b.rz = o;
+  o += up((size_t)batch * kMaxRhs * 8);
+  b.norms = o;  // anorm [batch], bnorm [batch][kMaxRhs], backward error [batch]
+  o += up((size_t)batch * (2 + kMaxRhs) * 8);
   b.total = o + 4096;
   return b;
+}
+
+unsigned long long plan_signature(int batch, const int* n, int NB, int nrhs, int prec) {
+  unsigned long long h = 1469598103934665603ull;  // FNV-1a over the plan's arguments
+  auto mix = [&](unsigned long long v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (v >> (8 * i)) & 0xff;
+      h *= 1099511628211ull;
+    }
+  };
+  mix((unsigned long long)batch);
+  mix((unsigned long long)NB);
+  mix((unsigned long long)nrhs);
+  mix((unsigned long long)prec);
+  for (int k = 0; k < batch; ++k) mix((unsigned long long)n[k]);
+  return h;
+}
+
+// ---- device side of the run ----------------------------------------------------------------------
+struct RunPtrs {
+  RunState* rs;
+  DevRec* rec;
+  int* fail;
+  int *l_all, *l_live, *l_act, *l_true, *l_fail;
+  int *live_flag, *act_flag;
+  double *rz, *anorm, *bnorm, *be;
+  double *stats, *stats_x, *coef, *coef_b;
+  int batch, nrhs, maxiter, prec;
+  double tol;
+  unsigned long long sig;
+};
+__device__ __forceinline__ double st_at(const double* h, int k, int j, int q) { return h[((size_t)k * kMaxRhs + j) * 3 + q]; }
+
+// normwise backward error of matrix k from the residual stats (max|r_j|) and the solution stats
+__device__ double backward_of(const RunPtrs& p, int k) {
+  double b = 0.0;
+  for (int j = 0; j < p.nrhs; ++j) {
+    const double den = p.anorm[k] * st_at(p.stats_x, k, j, 1) + p.bnorm[(size_t)k * kMaxRhs + j];
+    b = fmax(b, den > 0 ? st_at(p.stats, k, j, 1) / den : 0.0);
+  }
+  return b;
+}
+
+// start of a run: checks the plan signature; selects every matrix for the first factorisation
+__global__ void run_init_kernel(RunPtrs p) {
+  if (threadIdx.x == 0) {
+    const bool ok = p.rs->sig == p.sig;
+    p.rs->status = ok ? 0 : GBX_ERR_ARG;
+    p.rs->attempt = 0;
+    p.rs->it = 0;
+    p.rs->shift = 0.0;
+    if (!ok) p.l_all[0] = 0;  // nothing runs; the result reports GBX_ERR_ARG
+    p.l_live[0] = p.l_act[0] = p.l_true[0] = p.l_fail[0] = 0;
+  }
+  for (int k = threadIdx.x; k < p.batch; k += blockDim.x) {
+    p.rec[k] = DevRec{0.0, INFINITY, 0.0, 0.f, 0, 0, 0, 0, 0, 0};
+    p.fail[k] = p.rs->sig == p.sig ? 1 : 0;
+    p.live_flag[k] = p.act_flag[k] = 0;
+  }
+}
+
+// after a factorisation attempt: records the selected matrices' outcome, selects the failed ones for
+// the next attempt (diagonal shift: about the operands' unit roundoff, then 4x per attempt) and sets
+// the retry loop's condition; rebuilds the live list (matrices with a factor), largest first
+__global__ void factor_check_kernel(RunPtrs p, const DagState* fst, const int* finfo, const float* fcond,
+                                    const int* fnf, cudaGraphConditionalHandle retry) {
+  if (threadIdx.x != 0) return;
+  RunState* rs = p.rs;
+  if (rs->status == 0 && fst->status < 0) rs->status = fst->status;  // a timed-out wait
+  int any = 0;
+  for (int k = 0; k < p.batch; ++k) {
+    if (!p.fail[k]) continue;
+    DevRec& r = p.rec[k];
+    r.cond = fcond[k];
+    r.fp64_tiles = fnf[k];
+    r.shift = rs->shift;
+    if (finfo[k] != 0) {
+      r.piv = finfo[k];
+      ++r.retries;
+      ++any;
+    } else {
+      r.piv = 0;
+      p.fail[k] = 0;
+    }
+  }
+  ++rs->attempt;
+  rs->shift = rs->shift == 0.0 ? (p.prec == 1 ? 1.0 / 2048 : p.prec == 2 ? 1.0 / 32 : 1.0 / 256) : rs->shift * 4;
+  int nl = 0, nf = 0;
+  const int nall = p.l_all[0];
+  for (int q = 0; q < nall; ++q) {
+    const int k = p.l_all[1 + q];
+    const bool live = rs->status == 0 && !p.fail[k];
+    p.live_flag[k] = live;
+    p.rec[k].live = live;
+    if (live) p.l_live[1 + nl++] = k;
+    else if (p.fail[k]) p.l_fail[1 + nf++] = k;
+  }
+  p.l_live[0] = nl;
+  p.l_fail[0] = nf;
+  cudaGraphSetConditional(retry, (rs->status == 0 && any > 0 && rs->attempt < 8) ? 1u : 0u);
+}
+
+// W = fl32(A) for the matrices of the refactorisation list, the diagonal scaled by (1 + shift)
+__global__ void convert_shift_batched(const RMat* mats, const int* list, const double* A, float* W,
+                                      const RunState* rs, int NB) {
+  GBX_MAT_OF_BLOCK();
+  int m, n;
+  if (!slot_tile(blockIdx.x, mt.NT, m, n)) return;
+  const long long base = (mt.slot0 + blockIdx.x) * (long long)NB * NB;
+  const float f = (float)(1.0 + rs->shift);
+  for (long long e = threadIdx.x; e < (long long)NB * NB; e += blockDim.x) {
+    float v = (float)A[base + e];
+    if (m == n && e % NB == e / NB) v *= f;
+    W[base + e] = v;
+  }
+}
+
+// ||A||_inf and ||b_j||_inf of the live matrices (from the row sums and the right-hand sides' stats)
+__global__ void norms_kernel(RunPtrs p) {
+  for (int q = threadIdx.x; q < p.l_live[0]; q += blockDim.x) {
+    const int k = p.l_live[1 + q];
+    p.anorm[k] = st_at(p.stats, k, 0, 1);
+    for (int j = 0; j < p.nrhs; ++j) p.bnorm[(size_t)k * kMaxRhs + j] = st_at(p.stats_x, k, j, 1);
+  }
+}
+
+// the active list: the matrices of `from` whose backward error is above the loop's target (half the
+// tolerance, so that the final check on the true residual meets the tolerance itself) and which have
+// iterations left; sets the CG loop's condition
+__device__ void select_active(const RunPtrs& p, const int* from, cudaGraphConditionalHandle loop) {
+  int na = 0;
+  const int nfrom = from[0];
+  for (int q = 0; q < nfrom; ++q) {
+    const int k = from[1 + q];
+    const bool go = p.be[k] > 0.5 * p.tol && p.rec[k].iterations < p.maxiter;
+    p.act_flag[k] = go;
+    if (go) p.l_act[1 + na++] = k;
+  }
+  p.l_act[0] = na;
+  p.l_true[0] = 0;
+  cudaGraphSetConditional(loop, na > 0 ? 1u : 0u);
+}
+
+// start of CG: rz = r.z, the backward error of x0, the first active list
+__global__ void pcg_start_kernel(RunPtrs p, cudaGraphConditionalHandle loop) {
+  if (threadIdx.x != 0) return;
+  for (int q = 0; q < p.l_live[0]; ++q) {
+    const int k = p.l_live[1 + q];
+    for (int j = 0; j < p.nrhs; ++j) p.rz[(size_t)k * kMaxRhs + j] = st_at(p.stats, k, j, 0);
+    p.be[k] = backward_of(p, k);
+  }
+  select_active(p, p.l_live, loop);
+}
+
+// alpha = (r.z) / (p.q); every 8th iteration the true residual replaces the recursive one
+__global__ void pcg_alpha_kernel(RunPtrs p) {
+  if (threadIdx.x != 0) return;
+  const int na = p.l_act[0];
+  for (int q = 0; q < na; ++q) {
+    const int k = p.l_act[1 + q];
+    for (int j = 0; j < p.nrhs; ++j) {
+      const double pq = st_at(p.stats, k, j, 0);
+      p.coef[(size_t)k * kMaxRhs + j] = pq != 0.0 ? p.rz[(size_t)k * kMaxRhs + j] / pq : 0.0;
+    }
+  }
+  const bool due = (p.rs->it + 1) % 8 == 0;
+  p.l_true[0] = due ? na : 0;
+  if (due)
+    for (int q = 0; q < na; ++q) p.l_true[1 + q] = p.l_act[1 + q];
+}
+
+// after the preconditioner: the backward error, beta = (r.z)_new / (r.z)_old
+__global__ void pcg_beta_kernel(RunPtrs p) {
+  if (threadIdx.x != 0) return;
+  for (int q = 0; q < p.l_act[0]; ++q) {
+    const int k = p.l_act[1 + q];
+    ++p.rec[k].iterations;
+    p.be[k] = backward_of(p, k);
+    for (int j = 0; j < p.nrhs; ++j) {
+      const double rz_new = st_at(p.stats, k, j, 0), old = p.rz[(size_t)k * kMaxRhs + j];
+      p.coef_b[(size_t)k * kMaxRhs + j] = old != 0.0 ? rz_new / old : 0.0;
+      p.rz[(size_t)k * kMaxRhs + j] = rz_new;
+    }
+  }
+}
+
+// end of a CG iteration: the next active list (a subset of the current one) and the loop condition
+__global__ void pcg_select_kernel(RunPtrs p, cudaGraphConditionalHandle loop) {
+  if (threadIdx.x != 0) return;
+  ++p.rs->it;
+  // select_active writes l_act while reading it: entries only move forward, so copy it first
+  int* from = p.l_true;  // free at this point of the iteration (rebuilt by the next alpha kernel)
+  const int na = p.l_act[0];
+  from[0] = na;
+  for (int q = 0; q < na; ++q) from[1 + q] = p.l_act[1 + q];
+  select_active(p, from, loop);
+}
+
+// final check on the true residual of every live matrix
+__global__ void pcg_final_kernel(RunPtrs p) {
+  for (int q = threadIdx.x; q < p.l_live[0]; q += blockDim.x) {
+    const int k = p.l_live[1 + q];
+    p.rec[k].backward_error = backward_of(p, k);
+    p.rec[k].anorm = p.anorm[k];
+  }
+}
+
+// ---- host side ------------------------------------------------------------------------------------
+struct DevStreams {
+  cudaStream_t side = nullptr;  // capture stream of the CG loop's bodies and of uncaptured runs
+  bool ready = false;
+};
+std::mutex g_run_mtx;
+DevStreams g_run[64];
+
+int run_streams(DevStreams*& d) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return GBX_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_run_mtx);
+  d = &g_run[dev];
+  if (!d->ready) {
+    if (cudaStreamCreateWithFlags(&d->side, cudaStreamNonBlocking) != cudaSuccess) return GBX_ERR_CUDA;
+    d->ready = true;
+  }
+  return GBX_OK;
+}
+
+// Adds a WHILE conditional node (default condition 0, set by upstream kernels) at the capture
+// position of the capturing stream `s`, and starts capturing its body on `body_s`.
+int begin_while(cudaStream_t s, cudaStream_t body_s, cudaGraphConditionalHandle h, cudaGraphNode_t& node) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return GBX_ERR_CUDA;
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // the remaining fields zero
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &np) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaStreamBeginCaptureToGraph(body_s, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeRelaxed) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  return GBX_OK;
+}
+int end_while(cudaStream_t s, cudaStream_t body_s, cudaGraphNode_t node) {
+  cudaGraph_t body = nullptr;
+  if (cudaStreamEndCapture(body_s, &body) != cudaSuccess) return GBX_ERR_CUDA;
+  return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess
+             ? GBX_OK
+             : GBX_ERR_CUDA;
+}
+int conditional_handle(cudaStream_t s, cudaGraphConditionalHandle& h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return GBX_ERR_CUDA;
+  return cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) == cudaSuccess ? GBX_OK
+                                                                                               : GBX_ERR_CUDA;
+}
+
+struct Run {
+  int batch, NB, nrhs, prec;
+  const int* n;
+  const double *A, *B;
+  double* X;
+  float* W;
+  char* base;
+  size_t work_bytes;
+  double fp64_cond;
+  BLayout L;
+  RunPtrs p;
+  int sms;
+  uint64_t tmo;
+};
+
+// z := M^{-1} r for the matrices flagged in `flags` (FP32 sweeps over the planned task lists of every
+// matrix; the others' tasks are skipped)
+int emit_precond(const Run& r, cudaStream_t s, const int* flags, const double* rv, double* z) {
+  const BLayout& L = r.L;
+  const long long nvec = L.nvec, sumNT = L.sumNT;
+  float* xf = (float*)(r.base + L.tmp);
+  float* yf = xf + nvec;
+  DagState* sw_st = (DagState*)(r.base + L.sweep);
+  int* sw_cnt = (int*)(r.base + L.sweep + 2 * sizeof(DagState));
+  const SweepTask* tasks = (const SweepTask*)(r.base + L.tasks);
+  const RMat* dmats = (const RMat*)(r.base + L.mats);
+  const float* Inv = (const float*)(r.base + L.inv);
+  d2s_kernel<<<512, 256, 0, s>>>(rv, xf, nvec);
+  // fresh queue heads and counters; status and abort stay, so a wait that ran out is reported
+  if (cudaMemsetAsync(&sw_st[0].head, 0, sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(&sw_st[1].head, 0, sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(sw_cnt, 0, (size_t)4 * sumNT * sizeof(int), s) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  const int gf = (int)std::max(1LL, std::min<long long>(2 * r.sms, L.nf));
+  const int gb = (int)std::max(1LL, std::min<long long>(2 * r.sms, L.nb));
+  launch_sweep(0, gf, s, dmats, tasks, (int)L.nf, flags, r.W, Inv, xf, yf, r.NB, r.nrhs, sw_cnt, sw_cnt + sumNT,
+               sw_st, r.tmo);
+  launch_sweep(1, gb, s, dmats, tasks + L.nf, (int)L.nb, flags, r.W, Inv, xf, yf, r.NB, r.nrhs, sw_cnt + 2 * sumNT,
+               sw_cnt + 3 * sumNT, sw_st + 1, r.tmo);
+  s2d_kernel<<<512, 256, 0, s>>>(xf, z, nvec);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+// y := y + alpha A x for the matrices of `list` (double-float arithmetic on the split A)
+void emit_symm(const Run& r, cudaStream_t s, const int* list, double alpha, const double* x, double* y) {
+  const BLayout& L = r.L;
+  const long long nvec = L.nvec;
+  const size_t vs = (size_t)2 * r.nrhs * 512 * sizeof(float);
+  float* xh = (float*)(r.base + L.tmp);  // the preconditioner's FP32 buffers are free between its calls
+  float* xl = xh + nvec;
+  split_vec_kernel<<<512, 256, 0, s>>>(x, xh, xl, nvec);
+  symm_df(dim3(L.maxslots, (r.NB + 127) / 128, r.batch), dim3(L.maxslots, std::max(1, r.NB / 64), r.batch), vs, s,
+          (const RMat*)(r.base + L.mats), list, (const float*)(r.base + L.ahi), (const float*)(r.base + L.alo), xh, xl,
+          y, r.NB, r.nrhs, alpha);
+}
+void emit_stats(const Run& r, cudaStream_t s, const int* list, const double* a, const double* b, double* out) {
+  colstats_batched<<<dim3(r.nrhs, 1, (unsigned)r.batch), 256, 0, s>>>((const RMat*)(r.base + r.L.mats), list, a, b,
+                                                                        r.nrhs, r.nrhs, out);
+}
+unsigned vec_grid(const Run& r) { return (unsigned)std::min<long long>(64, ((long long)r.L.maxN * r.nrhs + 255) / 256); }
+void emit_copy(const Run& r, cudaStream_t s, const int* list, double* y, const double* x) {
+  copy_vec_batched<<<dim3(vec_grid(r), 1, (unsigned)r.batch), 256, 0, s>>>((const RMat*)(r.base + r.L.mats), list, y,
+                                                                             x, r.nrhs);
+}
+void emit_axpy(const Run& r, cudaStream_t s, const int* list, double* y, const double* x, const double* coef,
+               double sign, int mode) {
+  axpy_cols_batched<<<dim3(vec_grid(r), 1, (unsigned)r.batch), 256, 0, s>>>((const RMat*)(r.base + r.L.mats), list, y,
+                                                                              x, coef, sign, r.nrhs, mode);
+}
+
+// The whole solve, emitted on the capturing stream `s` (its own capture, or the caller's).
+int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
+  const BLayout& L = r.L;
+  RunPtrs& p = r.p;
+  const RMat* dmats = (const RMat*)(r.base + L.mats);
+  double* R = (double*)(r.base + L.R);
+  double* Z = (double*)(r.base + L.Z);
+  double* P = (double*)(r.base + L.P);
+  double* Q = (double*)(r.base + L.Q);
+  double* rowsum = (double*)(r.base + L.rowsum);
+  float* Ahi = (float*)(r.base + L.ahi);
+  float* Alo = (float*)(r.base + L.alo);
+  float* Inv = (float*)(r.base + L.inv);
+  void* fwork = r.base;
+  // factorisation results in the factor's workspace
+  const size_t fw = L.fwork_bytes;
+  const gbx::mixed::InfoPtrs fi = gbx::mixed::info_ptrs(r.batch, r.n, r.NB, fwork);
+
+  run_init_kernel<<<1, 256, 0, s>>>(p);
+  // 0. one pass over A: W = fl32(A) for the first factorisation, the split of A for the residual
+  //    products, and the row sums of |A|
+  if (cudaMemsetAsync(rowsum, 0, (size_t)L.sumN * 8, s) != cudaSuccess) return GBX_ERR_CUDA;
+  prep_batched<<<dim3(L.maxslots, 1, (unsigned)r.batch), 256, 0, s>>>(dmats, p.l_all, r.A, r.W, Ahi, Alo, rowsum, r.NB,
+                                                                      r.nrhs);
+  // 1. low-precision factorisation of every matrix; the ones that break down are factorised again,
+  //    alone, with a growing diagonal shift (a WHILE node: at most 8 attempts in all)
+  cudaGraphConditionalHandle h_retry, h_cg;
+  if (int e = conditional_handle(s, h_retry)) return e;
+  if (int e = conditional_handle(s, h_cg)) return e;
+  if (int e = gbx::mixed::run_batch(r.batch, r.n, r.NB, r.W, r.prec, r.fp64_cond, p.fail, fwork, fw, s)) return e;
+  factor_check_kernel<<<1, 32, 0, s>>>(p, fi.st, fi.minfo, fi.cond, fi.nfp64, h_retry);
+  {
+    cudaGraphNode_t node;
+    if (int e = begin_while(s, body_s, h_retry, node)) return e;
+    convert_shift_batched<<<dim3(L.maxslots, 1, (unsigned)r.batch), 256, 0, body_s>>>(dmats, p.l_fail, r.A, r.W, p.rs,
+                                                                                     r.NB);
+    if (int e = gbx::mixed::run_batch(r.batch, r.n, r.NB, r.W, r.prec, r.fp64_cond, p.fail, fwork, fw, body_s))
+      return e;
+    factor_check_kernel<<<1, 32, 0, body_s>>>(p, fi.st, fi.minfo, fi.cond, fi.nfp64, h_retry);
+    if (int e = end_while(s, body_s, node)) return e;
+  }
+  // 2. the preconditioner's diagonal inverses; ||A||_inf and ||b_j||_inf
+  diag_inverse_batched<<<dim3(L.maxNT, (r.NB + kBlk - 1) / kBlk, (unsigned)r.batch), kThreads,
+                         op_trsm_smem_elems<float>() * sizeof(float), s>>>(dmats, p.l_live, r.W, Inv, r.NB);
+  colstats_batched<<<dim3(1, 1, (unsigned)r.batch), 256, 0, s>>>(dmats, p.l_live, rowsum, nullptr, r.nrhs, 1, p.stats);
+  emit_stats(r, s, p.l_live, r.B, nullptr, p.stats_x);
+  norms_kernel<<<1, 256, 0, s>>>(p);
+  // 3. x0 = M^{-1} b ; r = b - A x0 ; z = M^{-1} r ; p = z
+  if (int e = emit_precond(r, s, p.live_flag, r.B, r.X)) return e;
+  emit_copy(r, s, p.l_live, R, r.B);
+  emit_symm(r, s, p.l_live, -1.0, r.X, R);
+  if (int e = emit_precond(r, s, p.live_flag, R, Z)) return e;
+  emit_copy(r, s, p.l_live, P, Z);
+  emit_stats(r, s, p.l_live, R, Z, p.stats);
+  emit_stats(r, s, p.l_live, r.X, nullptr, p.stats_x);
+  pcg_start_kernel<<<1, 32, 0, s>>>(p, h_cg);
+  // 4. preconditioned CG in FP64 (a WHILE node), each matrix until its own backward error meets
+  //    the loop's target or it runs out of iterations
+  {
+    cudaGraphNode_t node;
+    if (int e = begin_while(s, body_s, h_cg, node)) return e;
+    cudaStream_t b = body_s;
+    emit_axpy(r, b, p.l_act, Q, Q, p.coef, -1.0, 2);  // q = 0
+    emit_symm(r, b, p.l_act, 1.0, P, Q);              // q = A p
+    emit_stats(r, b, p.l_act, P, Q, p.stats);
+    pcg_alpha_kernel<<<1, 32, 0, b>>>(p);
+    emit_axpy(r, b, p.l_act, r.X, P, p.coef, 1.0, 0);
+    emit_axpy(r, b, p.l_act, R, Q, p.coef, -1.0, 0);
+    emit_copy(r, b, p.l_true, R, r.B);  // every 8th iteration: the true residual against drift
+    emit_symm(r, b, p.l_true, -1.0, r.X, R);
+    if (int e = emit_precond(r, b, p.act_flag, R, Z)) return e;
+    emit_stats(r, b, p.l_act, R, Z, p.stats);
+    emit_stats(r, b, p.l_act, r.X, nullptr, p.stats_x);
+    pcg_beta_kernel<<<1, 32, 0, b>>>(p);
+    emit_axpy(r, b, p.l_act, P, Z, p.coef_b, 1.0, 1);  // p = z + beta p
+    pcg_select_kernel<<<1, 32, 0, b>>>(p, h_cg);
+    if (int e = end_while(s, body_s, node)) return e;
+  }
+  // 5. final check on the true residual of every live matrix
+  emit_copy(r, s, p.l_live, R, r.B);
+  emit_symm(r, s, p.l_live, -1.0, r.X, R);
+  emit_stats(r, s, p.l_live, R, nullptr, p.stats);
+  emit_stats(r, s, p.l_live, r.X, nullptr, p.stats_x);
+  pcg_final_kernel<<<1, 256, 0, s>>>(p);
+  return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+int check_args(int batch, const int* n, int NB, int nrhs, int prec) {
+  if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > 512 || nrhs <= 0 || nrhs > kMaxRhs || prec < 0 || prec > 2)
+    return GBX_ERR_ARG;
+  for (int k = 0; k < batch; ++k)
+    if (n[k] <= 0) return GBX_ERR_ARG;
+  return GBX_OK;
+}
+
+int make_run(Run& r, int batch, const int* n, int NB, int nrhs, int prec, double fp64_cond, const double* A,
+             const double* B, double* X, double tol, int maxiter, float* W, void* work, size_t work_bytes) {
+  r.batch = batch;
+  r.n = n;
+  r.NB = NB;
+  r.nrhs = nrhs;
+  r.prec = prec;
+  r.A = A;
+  r.B = B;
+  r.X = X;
+  r.W = W;
+  r.base = (char*)work;
+  r.work_bytes = work_bytes;
+  r.fp64_cond = fp64_cond;
+  r.L = blayout(batch, n, NB, nrhs);
+  r.tmo = gbx_get_wait_timeout_ns();
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&r.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  const BLayout& L = r.L;
+  RunPtrs& p = r.p;
+  char* base = r.base;
+  p.rs = (RunState*)(base + L.rs);
+  p.rec = (DevRec*)(base + L.rec);
+  p.fail = (int*)(base + L.fail);
+  int* lists = (int*)(base + L.lists);
+  p.l_all = lists;
+  p.l_live = lists + (batch + 1);
+  p.l_act = lists + 2 * (batch + 1);
+  p.l_true = lists + 3 * (batch + 1);
+  p.l_fail = lists + 4 * (batch + 1);
+  p.live_flag = (int*)(base + L.flags);
+  p.act_flag = p.live_flag + batch;
+  p.rz = (double*)(base + L.rz);
+  p.anorm = (double*)(base + L.norms);
+  p.bnorm = p.anorm + batch;
+  p.be = p.bnorm + (size_t)batch * kMaxRhs;
+  p.stats = (double*)(base + L.stats);
+  p.stats_x = p.stats + (size_t)batch * kMaxRhs * 3;
+  p.coef = (double*)(base + L.coef);
+  p.coef_b = p.coef + (size_t)batch * kMaxRhs;
+  p.batch = batch;
+  p.nrhs = nrhs;
+  p.maxiter = maxiter;
+  p.prec = prec;
+  p.tol = tol;
+  p.sig = plan_signature(batch, n, NB, nrhs, prec);
+  return GBX_OK;
 }
 }  // namespace
 
@@ -1246,320 +1737,174 @@ extern "C" int gbx_split_f64(const double* a, float* hi, float* lo, long long n,
 }
 
 extern "C" int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes) {
-  if (batch <= 0 || !n || NB <= 0 || NB % 256 || NB > 512 || nrhs <= 0 || nrhs > kMaxRhs || !bytes) return GBX_ERR_ARG;
-  for (int k = 0; k < batch; ++k)
-    if (n[k] <= 0) return GBX_ERR_ARG;
+  if (!bytes || check_args(batch, n, NB, nrhs, 0)) return GBX_ERR_ARG;
   *bytes = blayout(batch, n, NB, nrhs).total;
   return GBX_OK;
 }
 
-extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
-                                       double* X, int prec, double tol, int maxiter, float* W, void* work,
-                                       size_t work_bytes, gbx_refine_info* info, void* stream) {
-  size_t need = 0;
-  if (int e = gbx_dposv_mixed_batched_bufferSize(batch, n, NB, nrhs, &need)) return e;
-  if (!A || !B || !X || !W || !work || maxiter < 0 || prec < 0 || prec > 2) return GBX_ERR_ARG;
-  if (work_bytes < need) return GBX_ERR_WORKSPACE;
-  if (int e = set_attrs()) return e;
-  cudaStream_t s = (cudaStream_t)stream;
+extern "C" int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, void* work,
+                                            size_t work_bytes, void* stream) {
+  if (check_args(batch, n, NB, nrhs, prec) || !work) return GBX_ERR_ARG;
   const BLayout L = blayout(batch, n, NB, nrhs);
+  if (work_bytes < L.total) return GBX_ERR_WORKSPACE;
+  if (int e = set_attrs()) return e;
+  DevStreams* ds = nullptr;
+  if (int e = run_streams(ds)) return e;
+  cudaStream_t s = (cudaStream_t)stream;
   char* base = (char*)work;
-  void* fwork = base;
-  float* Inv = (float*)(base + L.inv);
-  double* R = (double*)(base + L.R);
-  double* Z = (double*)(base + L.Z);
-  double* P = (double*)(base + L.P);
-  double* Q = (double*)(base + L.Q);
-  float* tmp = (float*)(base + L.tmp);
-  double* rowsum = (double*)(base + L.rowsum);
-  double* stats = (double*)(base + L.stats);
-  double* stats_x = stats + (size_t)batch * kMaxRhs * 3;
-  double* coef = (double*)(base + L.coef);
-  double* coef_b = coef + (size_t)batch * kMaxRhs;
-  RMat* dmats = (RMat*)(base + L.mats);
-  int* dlist = (int*)(base + L.list);
-  float* Ahi = (float*)(base + L.ahi);
-  float* Alo = (float*)(base + L.alo);
-
-  // matrix table (batch order) and the list of matrices by decreasing tile count
+  // matrix table (batch order), the list of all matrices by decreasing tile count
   std::vector<RMat> mats(batch);
   long long slot = 0, invt = 0, vecn = 0;
-  int maxNT = 0, maxN = 0;
   for (int k = 0; k < batch; ++k) {
     const int nt = (n[k] + NB - 1) / NB;
     mats[k] = RMat{slot, invt, vecn, n[k], nt};
     slot += (long long)nt * (nt + 1) / 2;
     invt += nt;
     vecn += (long long)n[k] * nrhs;
-    maxNT = std::max(maxNT, nt);
-    maxN = std::max(maxN, n[k]);
   }
-  const long long nvec = vecn;
-  auto by_nt = [&](std::vector<int>& l) {
-    std::stable_sort(l.begin(), l.end(), [&](int a, int b) { return mats[a].NT > mats[b].NT; });
+  std::vector<int> all(batch + 1);
+  all[0] = batch;
+  for (int k = 0; k < batch; ++k) all[1 + k] = k;
+  std::stable_sort(all.begin() + 1, all.end(), [&](int a, int b) { return mats[a].NT > mats[b].NT; });
+  // the sweeps' task lists over every matrix, interleaved step by step (largest first); the run
+  // skips the tasks of matrices that are not in a sweep
+  std::vector<SweepTask> tf, tb;
+  auto push = [](std::vector<SweepTask>& v, int q, int kind, int M, int K) {
+    const int subs = kind == 0 ? kDiagSubs : kUpdSubs;
+    for (int u = 0; u < subs; ++u) v.push_back(SweepTask{q, (short)kind, (short)u, M, K});
   };
-  std::vector<int> all(batch);
-  for (int k = 0; k < batch; ++k) all[k] = k;
-  by_nt(all);
-  std::vector<gbx_refine_info> inf(batch);
-  std::memset(inf.data(), 0, batch * sizeof(gbx_refine_info));
-
-  // 0. one pass over A: W = fl32(A) for the first factorisation, the split of A for the residual
-  //    products, and the row sums of |A|
-  {
-    int slots = 0;
-    for (int k = 0; k < batch; ++k) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
-    if (cudaMemcpyAsync(dmats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(dlist, all.data(), batch * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemsetAsync(rowsum, 0, (size_t)(nvec / nrhs) * 8, s) != cudaSuccess)
-      return GBX_ERR_CUDA;
-    prep_batched<<<dim3(slots, 1, (unsigned)batch), 256, 0, s>>>(dmats, dlist, A, W, Ahi, Alo, rowsum, NB, nrhs);
+  const int maxNT = L.maxNT;
+  for (int K = 0; K < maxNT; ++K) {
+    for (int i = 1; i <= batch; ++i)
+      if (mats[all[i]].NT > K) push(tf, all[i], 0, K, K);
+    for (int i = 1; i <= batch; ++i)  // the next step's own row first: it is on the critical path
+      if (K + 1 < mats[all[i]].NT) push(tf, all[i], 1, K + 1, K);
+    for (int i = 1; i <= batch; ++i)
+      for (int M = K + 2; M < mats[all[i]].NT; ++M) push(tf, all[i], 1, M, K);
   }
-  // 1. low-precision factorisation of every matrix; the ones that break down are factorised again,
-  //    alone, with a growing diagonal shift (from A again: W then holds the failed attempt)
-  std::vector<unsigned char> sel(batch, 1);
-  std::vector<int> finfo(batch, 0);
-  std::vector<float> cond(batch, 0.f), cnow(batch);
-  double shift = 0.0;
-  int first_bad = 0;
-  for (int attempt = 0; attempt < 8; ++attempt) {
-    if (int e = gbx::mixed::launch_batch(batch, n, NB, A, W, prec, shift, sel.data(), fwork, L.fwork_bytes, s,
-                                         attempt == 0))
-      return e;
-    if (int e = gbx_potrf_mixed_batched_info(fwork, batch, n, NB, finfo.data(), cnow.data(), stream)) return e;
-    bool any = false;
-    first_bad = 0;
-    for (int k = 0; k < batch; ++k) {
-      if (!sel[k]) continue;
-      cond[k] = cnow[k];
-      inf[k].shift = shift;
-      if (finfo[k] != 0) {
-        any = true;
-        if (!first_bad) first_bad = finfo[k];
-        ++inf[k].factor_retries;
-      } else {
-        sel[k] = 0;
-      }
+  for (int st = 0; st < maxNT; ++st) {  // steps counted from each matrix's last tile row
+    for (int i = 1; i <= batch; ++i)
+      if (mats[all[i]].NT > st) push(tb, all[i], 0, mats[all[i]].NT - 1 - st, mats[all[i]].NT - 1 - st);
+    for (int i = 1; i <= batch; ++i) {
+      const int K = mats[all[i]].NT - 1 - st;
+      if (K >= 1) push(tb, all[i], 1, K, K - 1);
     }
-    if (!any) break;
-    // first shift about the operands' unit roundoff: fp16 2^-11, bf16 2^-8, fp8 e4m3 2^-4
-    shift = shift == 0.0 ? (prec == 1 ? 1.0 / 2048 : prec == 2 ? 1.0 / 32 : 1.0 / 256) : shift * 4;
-  }
-  for (int k = 0; k < batch; ++k) inf[k].cond_estimate = cond[k];
-  bool factored = true;
-  for (int k = 0; k < batch; ++k)
-    if (sel[k]) {  // still broken after every shift
-      factored = false;
-      inf[k].backward_error = INFINITY;
+    for (int i = 1; i <= batch; ++i) {
+      const int K = mats[all[i]].NT - 1 - st;
+      for (int J = 0; J + 1 < K; ++J) push(tb, all[i], 1, K, J);
     }
-  if (!factored && batch == 1) {
-    if (info) info[0] = inf[0];
-    return first_bad;
   }
-  std::vector<int> live;  // matrices with a factor
-  for (int k : all)
-    if (!sel[k]) live.push_back(k);
-
-  auto upload_list = [&](const std::vector<int>& l) {
-    return cudaMemcpyAsync(dlist, l.data(), l.size() * sizeof(int), cudaMemcpyHostToDevice, s) == cudaSuccess;
-  };
-  const unsigned gx_vec = (unsigned)std::min<long long>(64, ((long long)maxN * nrhs + 255) / 256);
-  // z := M^{-1} r for the matrices of l (FP32 sweeps; vectors in FP64): two persistent launches
-  // over task lists that interleave the listed matrices step by step
-  DagState* sw_st = (DagState*)(base + L.sweep);
-  int* sw_cnt = (int*)(base + L.sweep + 2 * sizeof(DagState));
-  SweepTask* d_tasks = (SweepTask*)(base + L.tasks);
-  if (cudaMemsetAsync(sw_st, 0, 2 * sizeof(DagState), s) != cudaSuccess) return GBX_ERR_CUDA;
-  int sms = 0, dev = 0;
-  cudaGetDevice(&dev);
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
-  std::vector<int> swept;  // matrices of the uploaded task lists
-  int nf = 0, nb = 0;
-  const uint64_t tmo = gbx_get_wait_timeout_ns();
-  auto precond = [&](const std::vector<int>& l, const double* r, double* z) -> int {
-    float* xf = tmp;
-    float* yf = tmp + nvec;
-    d2s_kernel<<<512, 256, 0, s>>>(r, xf, nvec);
-    if (l != swept) {
-      std::vector<SweepTask> tf, tb;
-      auto push = [](std::vector<SweepTask>& v, int q, int kind, int M, int K) {
-        const int subs = kind == 0 ? kDiagSubs : kUpdSubs;
-        for (int u = 0; u < subs; ++u) v.push_back(SweepTask{q, (short)kind, (short)u, M, K});
-      };
-      for (int K = 0; K < maxNT; ++K) {
-        for (int q : l)
-          if (mats[q].NT > K) push(tf, q, 0, K, K);
-        for (int q : l)  // the next step's own row first: it is on the critical path
-          if (K + 1 < mats[q].NT) push(tf, q, 1, K + 1, K);
-        for (int q : l)
-          for (int M = K + 2; M < mats[q].NT; ++M) push(tf, q, 1, M, K);
-      }
-      for (int st = 0; st < maxNT; ++st) {  // steps counted from each matrix's last tile row
-        for (int q : l)
-          if (mats[q].NT > st) push(tb, q, 0, mats[q].NT - 1 - st, mats[q].NT - 1 - st);
-        for (int q : l) {
-          const int K = mats[q].NT - 1 - st;
-          if (K >= 1) push(tb, q, 1, K, K - 1);
-        }
-        for (int q : l) {
-          const int K = mats[q].NT - 1 - st;
-          for (int J = 0; J + 1 < K; ++J) push(tb, q, 1, K, J);
-        }
-      }
-      nf = (int)tf.size();
-      nb = (int)tb.size();
-      tf.insert(tf.end(), tb.begin(), tb.end());
-      if (cudaMemcpyAsync(d_tasks, tf.data(), tf.size() * sizeof(SweepTask), cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return GBX_ERR_CUDA;
-      swept = l;
-    }
-    // fresh queue heads and counters; status and abort stay, so a wait that ran out is reported
-    if (cudaMemsetAsync(&sw_st[0].head, 0, sizeof(unsigned long long), s) != cudaSuccess ||
-        cudaMemsetAsync(&sw_st[1].head, 0, sizeof(unsigned long long), s) != cudaSuccess ||
-        cudaMemsetAsync(sw_cnt, 0, (size_t)4 * invt * sizeof(int), s) != cudaSuccess)
-      return GBX_ERR_CUDA;
-    const int gf = std::max(1, std::min(2 * sms, nf)), gb = std::max(1, std::min(2 * sms, nb));
-    launch_sweep(0, gf, s, dmats, d_tasks, nf, W, Inv, xf, yf, NB, nrhs, sw_cnt, sw_cnt + invt, sw_st, tmo);
-    launch_sweep(1, gb, s, dmats, d_tasks + nf, nb, W, Inv, xf, yf, NB, nrhs, sw_cnt + 2 * invt, sw_cnt + 3 * invt,
-                 sw_st + 1, tmo);
-    s2d_kernel<<<512, 256, 0, s>>>(xf, z, nvec);
-    return GBX_OK;
-  };
-  // y := y + alpha A x for the matrices of l (double-float arithmetic on the split A)
-  auto symm = [&](const std::vector<int>& l, double alpha, const double* x, double* y) {
-    const int c = (int)l.size();
-    int slots = 0;
-    for (int k : l) slots = std::max(slots, mats[k].NT * (mats[k].NT + 1) / 2);
-    const size_t vs = (size_t)2 * nrhs * 512 * sizeof(float);
-    float* xh = tmp;  // the preconditioner's FP32 buffers are free between its calls
-    float* xl = tmp + nvec;
-    split_vec_kernel<<<512, 256, 0, s>>>(x, xh, xl, nvec);
-    symm_df(dim3(slots, (NB + 127) / 128, c), dim3(slots, std::max(1, NB / 64), c), vs, s, dmats, dlist, Ahi, Alo, xh,
-            xl, y, NB, nrhs, alpha);
-  };
-  auto stats_of = [&](const std::vector<int>& l, const double* a, const double* b, double* out) {
-    colstats_batched<<<dim3(nrhs, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, a, b, nrhs, nrhs, out);
-  };
-  std::vector<double> hs((size_t)2 * batch * kMaxRhs * 3), hc((size_t)2 * batch * kMaxRhs, 0.0);
-  auto fetch_stats = [&]() {
-    if (cudaMemcpyAsync(hs.data(), stats, hs.size() * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
-    return cudaStreamSynchronize(s) == cudaSuccess;
-  };
-  auto st_at = [&](const double* h, int k, int j, int q) { return h[((size_t)k * kMaxRhs + j) * 3 + q]; };
-  const double* hsx = hs.data() + (size_t)batch * kMaxRhs * 3;
-
-  if (live.empty()) {
-    if (info)
-      for (int k = 0; k < batch; ++k) info[k] = inf[k];
-    return GBX_ERR_NOCONV;
-  }
-  if (cudaMemcpyAsync(dmats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      !upload_list(live))
+  if ((long long)tf.size() != L.nf || (long long)tb.size() != L.nb) return GBX_ERR_ARG;
+  tf.insert(tf.end(), tb.begin(), tb.end());
+  RunState rs;
+  std::memset(&rs, 0, sizeof(rs));
+  rs.sig = plan_signature(batch, n, NB, nrhs, prec);
+  if (int e = gbx::mixed::plan_batch(batch, n, NB, work, L.fwork_bytes, s)) return e;
+  if (cudaMemcpyAsync(base + L.mats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(base + L.lists, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(base + L.tasks, tf.data(), tf.size() * sizeof(SweepTask), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(base + L.rs, &rs, sizeof(rs), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemsetAsync(base + L.sweep, 0, 2 * sizeof(DagState), s) != cudaSuccess)
     return GBX_ERR_CUDA;
-  diag_inverse_batched<<<dim3(maxNT, (NB + kBlk - 1) / kBlk, (unsigned)live.size()), kThreads,
-                         op_trsm_smem_elems<float>() * sizeof(float), s>>>(dmats, dlist, W, Inv, NB);
-  // ||A||_inf (row sums from the pass over A) and ||b_j||_inf per matrix
-  colstats_batched<<<dim3(1, 1, (unsigned)live.size()), 256, 0, s>>>(dmats, dlist, rowsum, nullptr, nrhs, 1, stats);
-  stats_of(live, B, nullptr, stats_x);
-  if (!fetch_stats()) return GBX_ERR_CUDA;
-  std::vector<double> anorm(batch, 0.0), bnorm((size_t)batch * kMaxRhs, 0.0), rz((size_t)batch * kMaxRhs, 0.0),
-      be(batch, INFINITY);
-  for (int k : live) {
-    anorm[k] = st_at(hs.data(), k, 0, 1);
-    for (int j = 0; j < nrhs; ++j) bnorm[(size_t)k * kMaxRhs + j] = st_at(hsx, k, j, 1);
-  }
-  auto backward = [&](int k) {  // from the residual stats (hs) and the solution stats (hsx)
-    double b = 0.0;
-    for (int j = 0; j < nrhs; ++j) {
-      const double den = anorm[k] * st_at(hsx, k, j, 1) + bnorm[(size_t)k * kMaxRhs + j];
-      b = std::max(b, den > 0 ? st_at(hs.data(), k, j, 1) / den : 0.0);
-    }
-    return b;
-  };
-  auto copy_vecs = [&](const std::vector<int>& l, double* y, const double* x) {
-    copy_vec_batched<<<dim3(gx_vec, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, y, x, nrhs);
-  };
-  auto zero_vecs = [&](const std::vector<int>& l, double* y) {
-    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)l.size()), 256, 0, s>>>(dmats, dlist, y, y, coef, -1.0, nrhs, 2);
-  };
+  return cudaStreamSynchronize(s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
 
-  // 2. x0 = M^{-1} b ; r = b - A x0 ; z = M^{-1} r ; p = z
-  if (int e = precond(live, B, X)) return e;
-  copy_vecs(live, R, B);
-  symm(live, -1.0, X, R);
-  if (int e = precond(live, R, Z)) return e;
-  copy_vecs(live, P, Z);
-  stats_of(live, R, Z, stats);
-  stats_of(live, X, nullptr, stats_x);
-  if (!fetch_stats()) return GBX_ERR_CUDA;
-  for (int k : live) {
-    for (int j = 0; j < nrhs; ++j) rz[(size_t)k * kMaxRhs + j] = st_at(hs.data(), k, j, 0);
-    be[k] = backward(k);
+extern "C" int gbx_dposv_mixed_batched_exec(int batch, const int* n, int NB, const double* A, int nrhs,
+                                            const double* B, double* X, int prec, double fp64_diag_cond, double tol,
+                                            int maxiter, float* W, void* work, size_t work_bytes, void* stream) {
+  if (check_args(batch, n, NB, nrhs, prec) || !A || !B || !X || !W || !work || maxiter < 0 || !(tol > 0.0) ||
+      !(fp64_diag_cond >= 0.0))
+    return GBX_ERR_ARG;
+  if (work_bytes < blayout(batch, n, NB, nrhs).total) return GBX_ERR_WORKSPACE;
+  if (int e = set_attrs()) return e;
+  DevStreams* ds = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_run_mtx);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return GBX_ERR_CUDA;
+    ds = &g_run[dev];
+    if (!ds->ready) return GBX_ERR_ARG;  // no plan was made in this process on this device
   }
-  // 3. preconditioned CG in FP64, each matrix until its own backward error meets the tolerance
-  // the loop's own estimate comes from the updated residual; it aims at half the tolerance so that
-  // the final check on the true residual meets the tolerance itself
-  const double target = 0.5 * tol;
-  std::vector<int> act;
-  for (int it = 0; it < maxiter; ++it) {
-    act.clear();
-    for (int k : live)
-      if (be[k] > target) act.push_back(k);
-    if (act.empty()) break;
-    if (!upload_list(act)) return GBX_ERR_CUDA;
-    zero_vecs(act, Q);
-    symm(act, 1.0, P, Q);  // q = A p
-    stats_of(act, P, Q, stats);
-    if (!fetch_stats()) return GBX_ERR_CUDA;
-    for (int k : act)
-      for (int j = 0; j < nrhs; ++j) {
-        const double pq = st_at(hs.data(), k, j, 0);
-        hc[(size_t)k * kMaxRhs + j] = pq != 0.0 ? rz[(size_t)k * kMaxRhs + j] / pq : 0.0;  // alpha
-      }
-    cudaMemcpyAsync(coef, hc.data(), (size_t)batch * kMaxRhs * 8, cudaMemcpyHostToDevice, s);
-    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)act.size()), 256, 0, s>>>(dmats, dlist, X, P, coef, 1.0, nrhs, 0);
-    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)act.size()), 256, 0, s>>>(dmats, dlist, R, Q, coef, -1.0, nrhs, 0);
-    if ((it + 1) % 8 == 0) {  // replace the recursive residual by the true one against drift
-      copy_vecs(act, R, B);
-      symm(act, -1.0, X, R);
+  Run r;
+  if (int e = make_run(r, batch, n, NB, nrhs, prec, fp64_diag_cond, A, B, X, tol, maxiter, W, work, work_bytes))
+    return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cs;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cs == cudaStreamCaptureStatusActive) return emit_run(r, s, ds->side);  // into the caller's graph
+  // not capturing: the run as a graph of its own, captured on a private stream and launched on `s`
+  std::lock_guard<std::mutex> lk(g_run_mtx);  // one capture at a time on the private streams
+  static cudaStream_t cap[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!cap[dev] && cudaStreamCreateWithFlags(&cap[dev], cudaStreamNonBlocking) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaStreamBeginCapture(cap[dev], cudaStreamCaptureModeRelaxed) != cudaSuccess) return GBX_ERR_CUDA;
+  const int e = emit_run(r, cap[dev], ds->side);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(cap[dev], &g);
+  if (e) {
+    if (g) cudaGraphDestroy(g);
+    return e;
+  }
+  if (ce != cudaSuccess || !g) return GBX_ERR_CUDA;
+  cudaGraphExec_t ge = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return GBX_ERR_CUDA;
+  const cudaError_t le = cudaGraphLaunch(ge, s);
+  cudaGraphExecDestroy(ge);  // released once the launch completes
+  return le == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
+}
+
+extern "C" int gbx_dposv_mixed_batched_result(int batch, const int* n, int NB, int nrhs, double tol, const void* work,
+                                              gbx_refine_info* info, void* stream) {
+  if (check_args(batch, n, NB, nrhs, 0) || !work) return GBX_ERR_ARG;
+  const BLayout L = blayout(batch, n, NB, nrhs);
+  cudaStream_t s = (cudaStream_t)stream;
+  const char* base = (const char*)work;
+  std::vector<DevRec> rec(batch);
+  RunState rs;
+  DagState sw[2];
+  if (cudaMemcpyAsync(rec.data(), base + L.rec, batch * sizeof(DevRec), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&rs, base + L.rs, sizeof(rs), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(sw, base + L.sweep, sizeof(sw), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  bool ok = true;
+  int first_bad = 0;
+  for (int k = 0; k < batch; ++k) {
+    const DevRec& d = rec[k];
+    if (info) {
+      info[k].iterations = d.iterations;
+      info[k].factor_retries = d.retries;
+      info[k].shift = d.shift;
+      info[k].backward_error = d.live ? d.backward_error : INFINITY;
+      info[k].anorm = d.anorm;
+      info[k].cond_estimate = d.cond;
+      info[k].fp64_diag_tiles = d.fp64_tiles;
     }
-    if (int e = precond(act, R, Z)) return e;
-    stats_of(act, R, Z, stats);
-    stats_of(act, X, nullptr, stats_x);
-    if (!fetch_stats()) return GBX_ERR_CUDA;
-    for (int k : act) {
-      ++inf[k].iterations;
-      be[k] = backward(k);
-      for (int j = 0; j < nrhs; ++j) {
-        const double rz_new = st_at(hs.data(), k, j, 0);
-        const double old = rz[(size_t)k * kMaxRhs + j];
-        hc[(size_t)(batch + k) * kMaxRhs + j] = old != 0.0 ? rz_new / old : 0.0;  // beta
-        rz[(size_t)k * kMaxRhs + j] = rz_new;
-      }
+    if (!d.live) {
+      ok = false;
+      if (!first_bad) first_bad = d.piv;
+    } else if (!(d.backward_error <= tol)) {
+      ok = false;
     }
-    cudaMemcpyAsync(coef_b, hc.data() + (size_t)batch * kMaxRhs, (size_t)batch * kMaxRhs * 8, cudaMemcpyHostToDevice, s);
-    axpy_cols_batched<<<dim3(gx_vec, 1, (unsigned)act.size()), 256, 0, s>>>(dmats, dlist, P, Z, coef_b, 1.0, nrhs, 1);
   }
-  // 4. final check on the true residual of every factorised matrix
-  if (!upload_list(live)) return GBX_ERR_CUDA;
-  copy_vecs(live, R, B);
-  symm(live, -1.0, X, R);
-  stats_of(live, R, nullptr, stats);
-  stats_of(live, X, nullptr, stats_x);
-  if (!fetch_stats()) return GBX_ERR_CUDA;
-  int sw_status[2 * sizeof(DagState) / sizeof(int)];
-  if (cudaMemcpy(sw_status, sw_st, 2 * sizeof(DagState), cudaMemcpyDeviceToHost) != cudaSuccess) return GBX_ERR_CUDA;
-  if (sw_status[0] || sw_status[sizeof(DagState) / sizeof(int)]) return GBX_ERR_TIMEOUT;  // a sweep's wait ran out
-  bool ok = factored;
-  for (int k : live) {
-    inf[k].backward_error = backward(k);
-    inf[k].anorm = anorm[k];
-    if (!(inf[k].backward_error <= tol)) ok = false;
-  }
-  if (cudaGetLastError() != cudaSuccess) return GBX_ERR_CUDA;
-  if (info)
-    for (int k = 0; k < batch; ++k) info[k] = inf[k];
+  if (rs.status) return rs.status;
+  if (sw[0].status || sw[1].status) return GBX_ERR_TIMEOUT;  // a sweep's wait ran out
+  if (batch == 1 && first_bad > 0) return first_bad;
   return ok ? GBX_OK : GBX_ERR_NOCONV;
+}
+
+extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
+                                       double* X, int prec, double fp64_diag_cond, double tol, int maxiter, float* W,
+                                       void* work, size_t work_bytes, gbx_refine_info* info, void* stream) {
+  if (int e = gbx_dposv_mixed_batched_plan(batch, n, NB, nrhs, prec, work, work_bytes, stream)) return e;
+  if (int e = gbx_dposv_mixed_batched_exec(batch, n, NB, A, nrhs, B, X, prec, fp64_diag_cond, tol, maxiter, W, work,
+                                           work_bytes, stream))
+    return e;
+  return gbx_dposv_mixed_batched_result(batch, n, NB, nrhs, tol, work, info, stream);
 }
 
 extern "C" int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes) {
@@ -1569,8 +1914,9 @@ extern "C" int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes
 
 // one matrix: the batch of one
 extern "C" int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec,
-                               double tol, int maxiter, float* W, void* work, size_t work_bytes, gbx_refine_info* info,
-                               void* stream) {
+                               double fp64_diag_cond, double tol, int maxiter, float* W, void* work, size_t work_bytes,
+                               gbx_refine_info* info, void* stream) {
   if (N <= 0) return GBX_ERR_ARG;
-  return gbx_dposv_mixed_batched(1, &N, NB, A, nrhs, B, X, prec, tol, maxiter, W, work, work_bytes, info, stream);
+  return gbx_dposv_mixed_batched(1, &N, NB, A, nrhs, B, X, prec, fp64_diag_cond, tol, maxiter, W, work, work_bytes,
+                                 info, stream);
 }
