@@ -367,7 +367,11 @@ def add_roofline_fractions(line, fp64_peak, bf16_peak):
         if not isinstance(part, dict):
             continue
         for key, res in part.items():
-            if key in peaks and isinstance(res, dict) and isinstance(res.get("tflops"), (int, float)):
+            if not isinstance(res, dict) or not isinstance(res.get("tflops"), (int, float)):
+                continue
+            if key == "tuned":  # the tuner's choice: the peak of its precision
+                key = res.get("prec", res.get("mode"))
+            if key in peaks:
                 res["frac_of_peak"] = res["tflops"] / peaks[key]
     line["peaks"] = {"fp64_tflops": fp64_peak, "bf16_tflops": bf16_peak,
                      "fp8_tflops": 2.0 * bf16_peak, "note": "fp8 = twice the bf16 rate (nominal ratio)"}
@@ -462,10 +466,12 @@ def run_mixed(gbx, dev, N=32768, NB=512, nrhs=8, kappa=1e6):
 
 def run_batched(gbx, dev, count=4096, reps=3, cpu=True):
     """4096 SPD systems, sizes uniform over 32*{1..16}, (M+M^T)/2 + n I, 1 right-hand side each:
-    one persistent launch per solve, captured in a CUDA graph; FP64 and FP32 + 2 FP64 refinement
-    steps."""
+    one persistent launch per solve, captured in a CUDA graph; FP64, FP32 + 2 FP64 refinement steps,
+    and the configuration the batched autotuner picks (precision split, queue order, CTA count)."""
     import numpy as np
     import torch
+
+    from ttg_gb300 import autotune
     rng = np.random.default_rng(42)
     sizes = 32 * rng.integers(1, 17, size=count)
     rhs = [rng.standard_normal((1, int(n))) for n in sizes]
@@ -473,13 +479,18 @@ def run_batched(gbx, dev, count=4096, reps=3, cpu=True):
     out = {"config": {"workload": "%d SPD systems, n uniform in 32*{1..16}, 1 rhs, one persistent launch in a CUDA graph"
                                   % count, "count": count, "flops": b.flops}}
     stream = torch.cuda.Stream()
-    for mode, refine in (("fp64", 0), ("fp32", 2)):
+    fp64_peak = measure_fp64_gemm_peak(dev)
+    fp32_peak = 2.0 * 128 * torch.cuda.get_device_properties(0).multi_processor_count * 2.07e9  # FFMA issue rate
+    hbm = measured_hbm_peak() * 1e9
+    n2 = float(np.sum(sizes.astype(np.float64) ** 2))
+
+    def measure(mode, refine, ctas):
         b.reset()
-        b.solve(mode=mode, refine=refine)
+        b.solve(mode=mode, refine=refine, ctas=ctas)
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=stream):
-            b.solve(mode=mode, refine=refine, stream=stream)
+            b.solve(mode=mode, refine=refine, stream=stream, ctas=ctas)
         times = []
         for _ in range(reps + 1):
             b.reset()
@@ -494,21 +505,33 @@ def run_batched(gbx, dev, count=4096, reps=3, cpu=True):
         ms = sum(times[1:]) / reps
         # solution quality on a sample of the systems (checked on the host)
         xs = b.solutions()
-        An = b.A0.cpu().numpy() if mode == "fp32" else None
+        An = b.A0.cpu().numpy()
         worst = 0.0
-        if An is not None:
-            o = 0
-            offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
-            for k in range(0, count, 97):
-                n = int(sizes[k])
-                Ak = An[offs[k]:offs[k] + n * n].reshape(n, n).T
-                r = rhs[k][0] - Ak @ xs[k][0]
-                worst = max(worst, np.abs(r).max() / (np.abs(Ak).sum(1).max() * np.abs(xs[k][0]).max()
-                                                      + np.abs(rhs[k][0]).max()))
-        out[mode] = {"ms": ms, "matrices_per_s": count / (ms * 1e-3), "tflops": b.flops / (ms * 1e-3) / 1e12,
-                     "refine_steps": refine, "info_nonzero": int((b.info != 0).sum().item())}
-        if An is not None:
-            out[mode]["backward_error_sampled"] = worst
+        offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+        for k in range(0, count, 97):
+            n = int(sizes[k])
+            Ak = An[offs[k]:offs[k] + n * n].reshape(n, n).T
+            r = rhs[k][0] - Ak @ xs[k][0]
+            worst = max(worst, np.abs(r).max() / (np.abs(Ak).sum(1).max() * np.abs(xs[k][0]).max()
+                                                  + np.abs(rhs[k][0]).max()))
+        # size-mix roofline: FP64 mode, the factorisation at the FP64 rate (compute-bound for every
+        # n >= 32) plus one read and one write of each matrix (16 n^2 B); FP32 mode, the factorisation
+        # at the FP32 FFMA rate plus the HBM bytes (A read 8 n^2, factor written 4 n^2, per refinement
+        # step A read again and the factor read twice: 16 n^2)
+        if mode == "fp64":
+            t_roof = b.flops / (fp64_peak * 1e12) + 16.0 * n2 / hbm
+        else:
+            t_roof = b.flops / fp32_peak + (12.0 + 16.0 * refine) * n2 / hbm
+        return {"ms": ms, "matrices_per_s": count / (ms * 1e-3), "tflops": b.flops / (ms * 1e-3) / 1e12,
+                "refine_steps": refine, "ctas": ctas, "info_nonzero": int((b.info != 0).sum().item()),
+                "backward_error_sampled": worst, "size_mix_roofline_ms": t_roof * 1e3,
+                "frac_of_size_mix_roofline": t_roof * 1e3 / ms}
+
+    out["fp64"] = measure("fp64", 0, 0)
+    out["fp32"] = measure("fp32", 2, 0)
+    best = autotune.tune_batched(b, rhs, tol=1e-14, use_cache=False)  # leaves its queue order set
+    out["tuned"] = measure(best["mode"], best["refine"], best["ctas"])
+    out["tuned"].update(mode=best["mode"], schedule=best["schedule"], candidates=len(best["candidates"]))
     if cpu:
         # CPU counterpart: LAPACK dpotrf + dpotrs per matrix (OpenBLAS, one thread per matrix), all
         # host cores over the matrices, largest first; the whole batch (not a sample)
@@ -573,40 +596,31 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
     out["plain_fp64_per_matrix"] = {"ms": plain_ms, "tflops": flops / (plain_ms * 1e-3) / 1e12}
     bf16_peak, _ = measured_bf16_peak()
     hbm = measured_hbm_peak()
-    for prec in ("fp16", "bf16", "fp8"):  # fp8: e4m3 operands on kind::f8f6f4
+    from ttg_gb300 import autotune
+    tiles = {NB: A}
+
+    def measure(prec, nb, sched):
         # the whole solve (factorisation with its retry loop, CG to 1e-14 with device-side
         # coefficients and convergence tests) captured once in a CUDA graph, replayed
-        W = torch.empty(total, dtype=torch.float32, device=dev)
-        X = torch.empty_like(B)
-        solver = gbx.MixedBatchedSolver(sizes, NB, nrhs, prec=prec, device=dev)
-        side = torch.cuda.Stream()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
-            solver.run(A, B, X, W, tol=1e-14, maxiter=300, stream=side)
-        times = []
-        for _ in range(3):  # the first replay is a warm-up
-            torch.cuda.synchronize()
-            with torch.cuda.stream(side):
-                e0, e1 = _events()
-                e0.record()
-                g.replay()
-                e1.record()
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-        ms = statistics.median(times[1:])
-        infos, st = solver.result()
-        del g, solver
+        if nb not in tiles:
+            tiles[nb] = autotune.retile(A, sizes, NB, nb)
+        At = tiles[nb]
+        W = torch.empty(At.numel(), dtype=torch.float32, device=dev)
+        solver = gbx.MixedBatchedSolver(sizes, nb, nrhs, prec=prec, device=dev, sched=sched)
+        ms, infos, st, X = autotune.time_mixed_graph(solver, At, B, W, 1e-14, 300, reps=2)
+        del solver, W
         it = [i["iterations"] for i in infos]
         be = [i["backward_error"] for i in infos]
         fe = ((X - X64).abs().max() / X64.abs().max()).item()
         # after the timed region: every matrix's residual again, from plain FP64 products
+        offs_nb, _ = gbx.batched_tile_offsets(sizes, nb)
         be64, vo = 0.0, 0
         for k, n in enumerate(sizes):
             n = int(n)
-            nt = (n + NB - 1) // NB
-            Ak = A[int(offs[k]):int(offs[k]) + nt * (nt + 1) // 2 * NB * NB]
+            nt = (n + nb - 1) // nb
+            Ak = At[int(offs_nb[k]):int(offs_nb[k]) + nt * (nt + 1) // 2 * nb * nb]
             Bk, Xk = B[vo:vo + n * nrhs].view(nrhs, n), X[vo:vo + n * nrhs].view(nrhs, n)
-            be64 = max(be64, max(gbx.backward_error_fp64(Ak, n, NB, Bk, Xk)))
+            be64 = max(be64, max(gbx.backward_error_fp64(Ak, n, nb, Bk, Xk)))
             vo += n * nrhs
         # size-mix roofline: per matrix, its factorisation at the tensor-core rate plus the HBM
         # bytes of the refinement (one pass over A writing W and the split: 10 n^2 B; the factor's
@@ -615,16 +629,24 @@ def run_batched_mixed(gbx, dev, cpu=True, count=256, nrhs=4, kappa=1e4, NB=512, 
         peak_tc = (2.0 if prec == "fp8" else 1.0) * bf16_peak * 1e12
         t_roof = sum((float(n) ** 3 / 3) / peak_tc + (30.0 + 8.0 * i["iterations"]) * float(n) ** 2 / (hbm * 1e9)
                      for n, i in zip(sizes, infos))
-        out[prec] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "matrices_per_s": count / (ms * 1e-3),
-                     "cuda_graph": True, "size_mix_roofline_ms": t_roof * 1e3,
-                     "frac_of_size_mix_roofline": t_roof * 1e3 / ms,
-                     "backward_error_fp64_check_max": be64,
-                     "speedup_vs_plain_fp64": plain_ms / ms, "status": st, "iterations_max": int(max(it)),
-                     "iterations_mean": float(np.mean(it)), "factor_retries": int(sum(i["factor_retries"] for i in infos)),
-                     "shift_max": float(max(i["shift"] for i in infos)),
-                     "backward_error_max": float(max(be)), "forward_error_vs_fp64": fe}
-        del W
-        torch.cuda.empty_cache()
+        return {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "matrices_per_s": count / (ms * 1e-3),
+                "NB": nb, "sched": sched, "cuda_graph": True, "size_mix_roofline_ms": t_roof * 1e3,
+                "frac_of_size_mix_roofline": t_roof * 1e3 / ms,
+                "speedup_vs_plain_fp64": plain_ms / ms, "status": st, "iterations_max": int(max(it)),
+                "iterations_mean": float(np.mean(it)), "factor_retries": int(sum(i["factor_retries"] for i in infos)),
+                "fp64_diag_tiles": int(sum(i["fp64_diag_tiles"] for i in infos)),
+                "shift_max": float(max(i["shift"] for i in infos)),
+                "backward_error_max": float(max(be)), "backward_error_fp64_check_max": be64,
+                "forward_error_vs_fp64": fe}
+
+    # the configuration the tuner picks (tile size, operand precision, CTA schedule of the queue),
+    # then each operand precision at the configuration's tile size (fp8 is the one the workload names)
+    best = autotune.tune_mixed_batched(A, sizes, NB, B, nrhs, tol=1e-14, use_cache=False)
+    out["tuned"] = measure(best["prec"], best["NB"], best["sched"])
+    out["tuned"].update(prec=best["prec"], tuner_candidates=[
+        {k: c[k] for k in ("prec", "NB", "sched", "ms", "ok")} for c in best["candidates"]])
+    for prec in ("fp8", "fp16", "bf16"):
+        out[prec] = measure(prec, NB, 0)
     if cpu:
         # CPU counterpart: LAPACK dpotrf + dpotrs per matrix (OpenBLAS, one matrix per thread) on a
         # bounded sample: the first `cpu_sample` matrices of the batch

@@ -257,6 +257,10 @@ int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, d
  * reference.
  *   _plan:   builds the task tables of a batch shape (batch, n, NB, nrhs, prec) and uploads them
  *            into `work`; synchronises `stream`. Not capturable. Once per shape and workspace.
+ *            sched: the factorisation queue's order within each panel step, 0 the trailing
+ *            updates before the panel's TRSMs (CTAs update while the diagonal POTRF runs), 1 the
+ *            TRSMs first (the next panel's chain starts earlier); gbx_dposv_mixed_batched uses 0
+ *            and ttg_gb300.autotune.tune_mixed_batched picks one per batch.
  *   _exec:   the solve itself, asynchronous on `stream`: no host synchronisation, no allocation, no
  *            host-to-device copy. When `stream` is capturing, the solve's nodes (with its two
  *            conditional nodes) are added to the caller's graph, which can then be replayed; else
@@ -269,8 +273,8 @@ int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, d
  *            matrix.
  * gbx_dposv_mixed_batched = _plan + _exec + _result. */
 int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int NB, int nrhs, size_t* bytes);
-int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, void* work, size_t work_bytes,
-                                 void* stream);
+int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, int sched, void* work,
+                                 size_t work_bytes, void* stream);
 int gbx_dposv_mixed_batched_exec(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
                                  double* X, int prec, double fp64_diag_cond, double tol, int maxiter, float* W,
                                  void* work, size_t work_bytes, void* stream);

@@ -43,19 +43,20 @@ def test_retile_matches_the_tile_layout(gbx, nb_from, nb_to):
 
 
 def test_select_mixed_takes_the_fastest_converged_candidate():
-    table = {("fp16", 512): (90.0, 0, 5e-15), ("bf16", 512): (80.0, 0, 2e-14),   # too inaccurate
-             ("fp8", 512): (70.0, -4, 5e-15),                                    # did not converge
-             ("fp16", 256): (85.0, 0, 9e-15), ("bf16", 256): (95.0, 0, 4e-15)}
+    table = {("fp16", 512, 0): (90.0, 0, 5e-15), ("bf16", 512, 0): (80.0, 0, 2e-14),   # too inaccurate
+             ("fp8", 512, 1): (70.0, -4, 5e-15),                                       # did not converge
+             ("fp16", 256, 0): (85.0, 0, 9e-15), ("fp16", 256, 1): (84.0, 0, 9e-15),
+             ("bf16", 256, 1): (95.0, 0, 4e-15)}
     calls = []
 
-    def run(prec, nb):
-        calls.append((prec, nb))
-        ms, st, be = table[(prec, nb)]
+    def run(prec, nb, sched):
+        calls.append((prec, nb, sched))
+        ms, st, be = table[(prec, nb, sched)]
         return {"ms": ms, "status": st, "backward_error_max": be}
 
     best = autotune.select_mixed(run, list(table), 1e-14)
-    assert (best["prec"], best["NB"], best["ms"]) == ("fp16", 256, 85.0)
+    assert (best["prec"], best["NB"], best["sched"], best["ms"]) == ("fp16", 256, 1, 84.0)
     assert calls == list(table) and len(best["candidates"]) == len(table)
-    assert [c["ok"] for c in best["candidates"]] == [True, False, False, True, True]
+    assert [c["ok"] for c in best["candidates"]] == [True, False, False, True, True, True]
     with pytest.raises(RuntimeError):
-        autotune.select_mixed(run, [("bf16", 512), ("fp8", 512)], 1e-14)
+        autotune.select_mixed(run, [("bf16", 512, 0), ("fp8", 512, 1)], 1e-14)

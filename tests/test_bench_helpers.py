@@ -14,9 +14,10 @@ def test_roofline_fractions_of_secondary_configurations():
         "mixed": {"config": {}, "plain_fp64": {"ms": 1.0, "tflops": 1.1}, "bf16": {"tflops": 19.0},
                   "fp16": {"tflops": 95.0}},
         "batched": {"config": {}, "fp64": {"tflops": 0.5}, "fp32": {"tflops": 3.3},
-                    "cpu_baseline": {"value": 1.0}},
+                    "tuned": {"tflops": 3.5, "mode": "fp32"}, "cpu_baseline": {"value": 1.0}},
         "batched_mixed": {"config": {}, "plain_fp64_per_matrix": {"tflops": 0.2}, "fp16": {"tflops": 18.7},
-                          "bf16": {"tflops": 15.9}, "fp8": {"tflops": 11.0}},
+                          "bf16": {"tflops": 15.9}, "fp8": {"tflops": 11.0},
+                          "tuned": {"tflops": 19.0, "prec": "fp16"}},
         "config_small": {"gpu": {"tflops": 0.17}, "cpu_baseline": {"value": 0.4}},
         "potri": {"gpu": {"tflops": 0.67}},
     }
@@ -25,7 +26,9 @@ def test_roofline_fractions_of_secondary_configurations():
     assert abs(line["mixed"]["fp16"]["frac_of_peak"] - 95.0 / 1928.0) < 1e-12
     assert abs(line["batched_mixed"]["fp8"]["frac_of_peak"] - 11.0 / 3856.0) < 1e-12
     assert abs(line["potri"]["gpu"]["frac_of_peak"] - 0.67 / 1.1) < 1e-12
+    assert abs(line["batched_mixed"]["tuned"]["frac_of_peak"] - 19.0 / 1928.0) < 1e-12
     assert "frac_of_peak" not in line["batched"]["fp32"]           # CUDA-core FP32: no tensor roofline
+    assert "frac_of_peak" not in line["batched"]["tuned"]
     assert "frac_of_peak" not in line["batched"]["cpu_baseline"]
     assert line["peaks"]["fp8_tflops"] == 3856.0
 

@@ -100,9 +100,10 @@ def test_batched_mixed_plan_exec_result_argument_checks(gbx):
     n = (ctypes.c_int * 2)(700, 300)
     dummy = ctypes.c_void_p(16)
     d = ctypes.c_double
-    assert L.gbx_dposv_mixed_batched_plan(2, n, 200, 2, 0, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG
-    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 3, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG
-    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 0, dummy, 16, None) == gbx.GBX_ERR_WORKSPACE
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 200, 2, 0, 0, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 3, 0, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 0, 2, dummy, 1 << 40, None) == gbx.GBX_ERR_ARG  # schedule
+    assert L.gbx_dposv_mixed_batched_plan(2, n, 256, 2, 0, 0, dummy, 16, None) == gbx.GBX_ERR_WORKSPACE
     ex = L.gbx_dposv_mixed_batched_exec
     assert ex(2, n, 256, dummy, 2, dummy, dummy, 0, d(1e4), d(0.0), 10, dummy, dummy, 1 << 40, None) == \
         gbx.GBX_ERR_ARG  # tolerance must be positive

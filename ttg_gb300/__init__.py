@@ -84,7 +84,7 @@ SIGNATURES = {
     "gbx_potrf_mixed_batched_info": (_i, [_vp, _i, _vp, _i, _vp, _vp, _vp, _vp]),
     "gbx_dposv_mixed_batched_bufferSize": (_i, [_i, _vp, _i, _i, _szp]),
     "gbx_dposv_mixed_batched": (_i, [_i, _vp, _i, _vp, _i, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _sz, _vp, _vp]),
-    "gbx_dposv_mixed_batched_plan": (_i, [_i, _vp, _i, _i, _i, _vp, _sz, _vp]),
+    "gbx_dposv_mixed_batched_plan": (_i, [_i, _vp, _i, _i, _i, _i, _vp, _sz, _vp]),
     "gbx_dposv_mixed_batched_exec": (_i, [_i, _vp, _i, _vp, _i, _vp, _vp, _i, _d, _d, _i, _vp, _vp, _sz, _vp]),
     "gbx_dposv_mixed_batched_result": (_i, [_i, _vp, _i, _i, _d, _vp, _vp, _vp]),
 }
@@ -363,7 +363,7 @@ class MixedBatchedSolver:
     CUDA graph, e.g. torch.cuda.graph) and the result (synchronises). A, B, X, W: CUDA float64
     tensors laid out as for dposv_mixed_batched; X receives the solutions."""
 
-    def __init__(self, sizes, NB, nrhs, prec="fp16", device=None, work=None):
+    def __init__(self, sizes, NB, nrhs, prec="fp16", device=None, work=None, sched=0):
         import numpy as np
         import torch
         self.n = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32))
@@ -374,8 +374,8 @@ class MixedBatchedSolver:
         if work is None or work.numel() < need.value:
             work = torch.empty(need.value, dtype=torch.uint8, device=device)
         self.work = work
-        call("gbx_dposv_mixed_batched_plan", self.batch, self._n(), NB, nrhs, PREC[prec], _ptr(work), need.value,
-             _stream(None))
+        call("gbx_dposv_mixed_batched_plan", self.batch, self._n(), NB, nrhs, PREC[prec], int(sched), _ptr(work),
+             need.value, _stream(None))
 
     def _n(self):
         return self.n.ctypes.data_as(ctypes.c_void_p)

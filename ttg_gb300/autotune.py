@@ -7,10 +7,12 @@ candidate of
     interleaved large/small; and the number of CTAs (1 or 2 per SM for FP32, 1 per SM for FP64),
 keeps the candidates whose sampled backward error meets the tolerance, and returns the fastest.
 
-tune_mixed_batched (tiled systems, gbx_dposv_mixed_batched): times every tile size (256, 512) and
-tensor-core operand precision (fp16, bf16, fp8-e4m3) of the mixed solve on the batch, keeps the
-candidates with which every matrix met the tolerance, and returns the fastest. The tiles of the
-other tile sizes are made on the device by `retile`.
+tune_mixed_batched (tiled systems, gbx_dposv_mixed_batched): times every tile size (256, 512),
+tensor-core operand precision (fp16, bf16, fp8-e4m3) and CTA schedule of the factorisation queue
+(0: trailing updates before each panel's TRSMs, 1: TRSMs first) of the mixed solve on the batch,
+each as the replay of a captured CUDA graph of the whole solve, keeps the candidates with which
+every matrix met the tolerance, and returns the fastest. The tiles of the other tile sizes are
+made on the device by `retile`.
 
 Choices are cached per (GPU, size histogram, nrhs, tolerance) in a JSON file next to this module.
 """
@@ -140,13 +142,13 @@ def retile(A, sizes, NB_from, NB_to):
 
 
 def select_mixed(run, candidates, tol):
-    """Runs `run(prec, NB)` for every candidate (it returns a dict with "ms", "status" and
+    """Runs `run(prec, NB, sched)` for every candidate (it returns a dict with "ms", "status" and
     "backward_error_max"), and returns the fastest candidate with status 0 and backward error
     within tol, with every result under "candidates". Raises if none qualifies."""
     results = []
-    for prec, nb in candidates:
-        r = dict(run(prec, nb))
-        r.update(prec=prec, NB=nb)
+    for prec, nb, sched in candidates:
+        r = dict(run(prec, nb, sched))
+        r.update(prec=prec, NB=nb, sched=sched)
         r["ok"] = bool(r["status"] == 0 and r["backward_error_max"] <= tol)
         results.append(r)
     ok = [r for r in results if r["ok"]]
@@ -157,13 +159,38 @@ def select_mixed(run, candidates, tol):
     return best
 
 
-def tune_mixed_batched(A, sizes, NB, B, nrhs, tol=1e-14, precs=("fp16", "bf16", "fp8"), NBs=(256, 512), maxiter=300,
-                       reps=1, use_cache=True):
-    """Tile size and operand precision for gbx_dposv_mixed_batched on this batch (A: its tiles at
-    tile size NB on the device, B: its right-hand sides). Returns {"prec", "NB", "ms", ...,
-    "candidates": [...]}; the solution of the chosen candidate is not kept."""
+def time_mixed_graph(solver, A, B, W, tol, maxiter, reps):
+    """Captures one solve of `solver` (a ttg_gb300.MixedBatchedSolver) in a CUDA graph, replays it
+    1 + reps times (the first is a warm-up) and returns (mean ms of the timed replays, infos,
+    status, X of the last replay)."""
     import torch
-    from . import dposv_mixed_batched
+    X = torch.empty_like(B)
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+        solver.run(A, B, X, W, tol=tol, maxiter=maxiter, stream=side)
+    times = []
+    for _ in range(1 + reps):
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            g.replay()
+            e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    infos, st = solver.result()
+    del g
+    return float(np.mean(times[1:])), infos, st, X
+
+
+def tune_mixed_batched(A, sizes, NB, B, nrhs, tol=1e-14, precs=("fp16", "bf16", "fp8"), NBs=(256, 512),
+                       scheds=(0, 1), maxiter=300, reps=1, use_cache=True):
+    """Tile size, operand precision and CTA schedule for the batched mixed solve on this batch (A:
+    its tiles at tile size NB on the device, B: its right-hand sides). Returns {"prec", "NB",
+    "sched", "ms", ..., "candidates": [...]}; the solution of the chosen candidate is not kept."""
+    import torch
+    from . import MixedBatchedSolver
     sizes = np.asarray(sizes)
     hist = np.bincount(sizes.astype(np.int64), minlength=1).tobytes()
     key = "mixed|%s|%s|%d|%g" % (torch.cuda.get_device_name(), hashlib.sha1(hist).hexdigest()[:16], nrhs, tol)
@@ -177,27 +204,19 @@ def tune_mixed_batched(A, sizes, NB, B, nrhs, tol=1e-14, precs=("fp16", "bf16", 
         return cache[key]
     tiles = {NB: A}
 
-    def run(prec, nb):
+    def run(prec, nb, sched):
         if nb not in tiles:
             tiles[nb] = retile(A, sizes, NB, nb)
         At = tiles[nb]
         W = torch.empty(At.numel(), dtype=torch.float32, device=At.device)
-        X, infos, st = dposv_mixed_batched(At, sizes, nb, B, nrhs, prec=prec, tol=tol, maxiter=maxiter, W=W)
-        times = []
-        for _ in range(reps):
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            X, infos, st = dposv_mixed_batched(At, sizes, nb, B, nrhs, prec=prec, tol=tol, maxiter=maxiter, W=W)
-            e1.record()
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-        return {"ms": float(np.mean(times)), "status": int(st),
+        solver = MixedBatchedSolver(sizes, nb, nrhs, prec=prec, device=At.device, sched=sched)
+        ms, infos, st, _ = time_mixed_graph(solver, At, B, W, tol, maxiter, reps)
+        return {"ms": ms, "status": int(st),
                 "backward_error_max": float(max(i["backward_error"] for i in infos)),
                 "iterations_max": int(max(i["iterations"] for i in infos)),
                 "factor_retries": int(sum(i["factor_retries"] for i in infos))}
 
-    best = select_mixed(run, [(p, nb) for nb in NBs for p in precs], tol)
+    best = select_mixed(run, [(p, nb, sc) for nb in NBs for p in precs for sc in scheds], tol)
     if use_cache:
         cache[key] = best
         try:

@@ -228,39 +228,109 @@ __device__ bool choose_fp64_route(const Params& P, const float* A, int n, float*
   return !(mn > 0.f) || mx > P.fp64_cond * mn;
 }
 
+// (the FP64 scratch is read through L2 only: other CTAs wrote it, and L1 is not coherent)
 __device__ void round_block_to_w(const double* D, float* A, int ld, int di, int dj, bool diag) {
   for (int idx = threadIdx.x; idx < kBlk * dj; idx += kThr) {
     const int i = idx & (kBlk - 1), j = idx >> 7;
-    if (i < di && (!diag || i >= j)) A[i + (long long)j * ld] = (float)D[i + (long long)j * ld];
+    if (i < di && (!diag || i >= j)) A[i + (long long)j * ld] = (float)__ldcg(D + i + (long long)j * ld);
   }
 }
 
+// FP64 route block operations: plain loops through L2 with few live registers. The route is for
+// the rare ill-conditioned diagonal tile; the register-blocked FP64 block ops of the FP64 executor
+// would raise the persistent kernel's register peak and make it spill in its FP32 and tensor paths.
+// Blocks are column-major with leading dimension ld; n, m <= 128.
+// Cholesky of the lower n x n block in shared memory (right-looking, column by column); returns 0
+// or the 1-based index of the first non-positive pivot. S: 128 x 128 doubles.
+__device__ int f64_block_potrf(double* A, int ld, int n, double* S) {
+  __shared__ int s_info;
+  if (threadIdx.x == 0) s_info = 0;
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < kBlk * n; idx += kThr) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    S[idx] = (i < n && i >= j) ? __ldcg(A + i + (long long)j * ld) : 0.0;
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int j = 0; j < n; ++j) {
+    if (threadIdx.x == 0) {
+      const double d = S[j + kBlk * j];
+      if (!(d > 0.0)) s_info = j + 1;
+      else S[j + kBlk * j] = sqrt(d);
+    }
+    __syncthreads();
+    if (s_info) break;
+    const double piv = S[j + kBlk * j];
+#pragma unroll 1
+    for (int i = j + 1 + threadIdx.x; i < n; i += kThr) S[i + kBlk * j] /= piv;
+    __syncthreads();
+    const int w = n - j - 1;
+#pragma unroll 1
+    for (int idx = threadIdx.x; idx < w * w; idx += kThr) {
+      const int i = j + 1 + idx % w, k = j + 1 + idx / w;
+      if (i >= k) S[i + kBlk * k] -= S[i + kBlk * j] * S[k + kBlk * j];
+    }
+    __syncthreads();
+  }
+  const int info = s_info;
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < kBlk * n; idx += kThr) {
+    const int i = idx & (kBlk - 1), j = idx >> 7;
+    if (i < n && i >= j) A[i + (long long)j * ld] = S[idx];
+  }
+  __syncthreads();
+  return info;
+}
+// B(m x n) := B L^{-T} (L lower n x n): one thread per row, forward substitution in place
+__device__ void f64_block_trsm(const double* L, int ld, double* B, int m, int n) {
+  const int r = threadIdx.x;
+  if (r < m) {
+#pragma unroll 1
+    for (int c = 0; c < n; ++c) {
+      double x = __ldcg(B + r + (long long)c * ld);
+#pragma unroll 1
+      for (int k = 0; k < c; ++k) x -= __ldcg(B + r + (long long)k * ld) * __ldcg(L + c + (long long)k * ld);
+      B[r + (long long)c * ld] = x / __ldcg(L + c + (long long)c * ld);
+    }
+  }
+  __syncthreads();
+}
+// C(m x n) -= A(m x k) B(n x k)^T, lower part only when `lower`
+__device__ void f64_block_gemm(const double* A, const double* B, double* C, int ld, int m, int n, int k, bool lower) {
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < m * n; idx += kThr) {
+    const int i = idx % m, j = idx / m;
+    if (lower && i < j) continue;
+    double acc = 0.0;
+#pragma unroll 4
+    for (int q = 0; q < k; ++q) acc = fma(__ldcg(A + i + (long long)q * ld), __ldcg(B + j + (long long)q * ld), acc);
+    C[i + (long long)j * ld] = __ldcg(C + i + (long long)j * ld) - acc;
+  }
+  __syncthreads();
+}
+
 // One mini-task of the FP64 route on the tile's FP64 scratch D (NB x NB, column-major); the final
-// writer of a block also rounds it into W (A). Kept out of line: the FP64 block ops need many
-// registers, and inlined they would make the compiler spill in the kernel's FP32 and tensor paths.
-__device__ __noinline__ int potrf_mini_fp64(double* D, float* A, int NB, int n, const Mini& mk, double* sm) {
+// writer of a block also rounds it into W (A).
+__device__ int potrf_mini_fp64(double* D, float* A, int NB, int n, const Mini& mk, double* sm) {
   auto blk = [&](int i, int j) { return A + kBlk * i + (long long)kBlk * j * NB; };
   auto dblk = [&](int i, int j) { return D + kBlk * i + (long long)kBlk * j * NB; };
   auto bdim = [&](int i) { return min(kBlk, n - kBlk * i); };
   const int dp = bdim(mk.p);
   if (dp <= 0) return 0;
   if (mk.kind == 0) {
-    const int info = op_potrf<double>(dblk(mk.p, mk.p), NB, dp, sm);
-    __syncthreads();
+    const int info = f64_block_potrf(dblk(mk.p, mk.p), NB, dp, sm);
     round_block_to_w(dblk(mk.p, mk.p), blk(mk.p, mk.p), NB, dp, dp, true);
     return info;
   }
   const int di = bdim(mk.i);
   if (di <= 0) return 0;
   if (mk.kind == 1) {
-    op_trsm<double>(dblk(mk.p, mk.p), NB, dblk(mk.i, mk.p), NB, di, dp, sm);
-    __syncthreads();
+    f64_block_trsm(dblk(mk.p, mk.p), NB, dblk(mk.i, mk.p), di, dp);
     round_block_to_w(dblk(mk.i, mk.p), blk(mk.i, mk.p), NB, di, dp, false);
     return 0;
   }
   const int dj = bdim(mk.j);
-  if (dj > 0) op_gemm_nt<double>(dblk(mk.i, mk.p), NB, dblk(mk.j, mk.p), NB, dblk(mk.i, mk.j), NB, di, dj, dp,
-                                 mk.i == mk.j, sm);
+  if (dj > 0) f64_block_gemm(dblk(mk.i, mk.p), dblk(mk.j, mk.p), dblk(mk.i, mk.j), NB, di, dj, dp, mk.i == mk.j);
   return 0;
 }
 
@@ -904,7 +974,7 @@ int set_kernel_attrs() {
   return GBX_OK;
 }
 
-int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, cudaStream_t s) {
+int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, cudaStream_t s, int sched) {
   const Ws w = layout_batch(batch, n, NB);
   if (work_bytes < w.total) return GBX_ERR_WORKSPACE;
   if (int e = set_kernel_attrs()) return e;
@@ -941,12 +1011,13 @@ int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, c
   }
   // queue: phase by phase (phase p of a matrix: the tasks between POTRF(p) and POTRF(p+1) in its
   // own order); within a phase, group by group: 1 the updates of column p by panel p-1, 2 POTRF(p),
-  // 4 the trailing updates of the columns right of p by panel p-1, 3 the TRSMs of column p; within
-  // a group the matrices largest first; the POTRF group goes mini-task by mini-task across the
-  // matrices. The trailing updates do not depend on POTRF(p), so CTAs work on them while the
-  // POTRF mini-flowgraph runs instead of waiting on its TRSMs. Every task's predecessors stay
-  // earlier in the queue (group 4 of phase p needs TRSMs of phase p-1 and updates of phase p-1;
-  // group 3 needs groups 1 and 2 of phase p), so in-order grabbing cannot deadlock.
+  // then (schedule 0) 4 the trailing updates of the columns right of p by panel p-1 and 3 the TRSMs
+  // of column p, or (schedule 1) 3 before 4; within a group the matrices largest first; the POTRF
+  // group goes mini-task by mini-task across the matrices. The trailing updates do not depend on
+  // POTRF(p): with schedule 0 CTAs work on them while the POTRF mini-flowgraph runs instead of
+  // waiting on its TRSMs; schedule 1 starts the next panel's critical chain earlier. Every task's
+  // predecessors stay earlier in the queue in both (group 4 of phase p needs TRSMs and updates of
+  // phase p-1; group 3 needs groups 1 and 2 of phase p), so in-order grabbing cannot deadlock.
   std::vector<MixSeg> segs;
   long long task0 = 0;
   auto group_range = [&](int nt, int p, int g, long long& first, long long& last) {
@@ -961,7 +1032,7 @@ int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, c
     first = base + lo[g];
     last = base + hi[g];
   };
-  const int group_order[4] = {1, 2, 4, 3};
+  const int group_order[4] = {1, 2, sched == 1 ? 3 : 4, sched == 1 ? 4 : 3};
   for (int p = 0; p < maxNT; ++p)
     for (int gi = 0; gi < 4; ++gi) {
       const int g = group_order[gi];
@@ -1128,7 +1199,7 @@ extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const do
   if (!A || !W || !work || prec < 0 || prec > 2 || !(fp64_diag_cond >= 0.0)) return GBX_ERR_ARG;
   if (work_bytes < need) return GBX_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  if (int e = plan_batch(batch, n, NB, work, work_bytes, s)) return e;
+  if (int e = plan_batch(batch, n, NB, work, work_bytes, s, 0)) return e;
   if (int e = convert_host_sel(batch, n, NB, A, W, shift, sel, s)) return e;
   const int* dsel = nullptr;
   if (sel) {

@@ -23,7 +23,7 @@
 
 namespace gbx {
 namespace mixed {
-int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, cudaStream_t s);
+int plan_batch(int batch, const int* n, int NB, void* work, size_t work_bytes, cudaStream_t s, int sched);
 int run_batch(int batch, const int* n, int NB, float* W, int prec, double fp64_cond, const int* dsel, void* work,
               size_t work_bytes, cudaStream_t s);
 // device addresses of a batched factorisation's results in its workspace
@@ -1292,10 +1292,44 @@ __device__ double backward_of(const RunPtrs& p, int k) {
   return b;
 }
 
+// Order-preserving compaction by one CTA of kRunThreads threads: to = {count, the entries k of from
+// (a list {count, entries}) with keep(k)}, in from's order. `to` may not alias `from`.
+constexpr int kRunThreads = 256;
+template <typename Keep>
+__device__ void block_compact(const int* from, int* to, Keep keep) {
+  __shared__ int s_warp[kRunThreads / 32];
+  __shared__ int s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = from[0];
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < n; c0 += kRunThreads) {
+    const int q = c0 + threadIdx.x;
+    const int k = q < n ? from[1 + q] : -1;
+    const bool f = q < n && keep(k);
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) s_warp[warp] = __popc(m);
+    __syncthreads();
+    int before = s_base;
+    for (int w = 0; w < warp; ++w) before += s_warp[w];
+    if (f) to[1 + before + __popc(m & ((1u << lane) - 1u))] = k;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int w = 0; w < kRunThreads / 32; ++w) t += s_warp[w];
+      s_base += t;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) to[0] = s_base;
+  __syncthreads();
+}
+
 // start of a run: checks the plan signature; selects every matrix for the first factorisation
 __global__ void run_init_kernel(RunPtrs p) {
+  const bool ok = p.rs->sig == p.sig;
+  __syncthreads();  // every thread has read the signature before thread 0 may change the state
   if (threadIdx.x == 0) {
-    const bool ok = p.rs->sig == p.sig;
     p.rs->status = ok ? 0 : GBX_ERR_ARG;
     p.rs->attempt = 0;
     p.rs->it = 0;
@@ -1305,7 +1339,7 @@ __global__ void run_init_kernel(RunPtrs p) {
   }
   for (int k = threadIdx.x; k < p.batch; k += blockDim.x) {
     p.rec[k] = DevRec{0.0, INFINITY, 0.0, 0.f, 0, 0, 0, 0, 0, 0};
-    p.fail[k] = p.rs->sig == p.sig ? 1 : 0;
+    p.fail[k] = ok ? 1 : 0;
     p.live_flag[k] = p.act_flag[k] = 0;
   }
 }
@@ -1315,40 +1349,44 @@ __global__ void run_init_kernel(RunPtrs p) {
 // the retry loop's condition; rebuilds the live list (matrices with a factor), largest first
 __global__ void factor_check_kernel(RunPtrs p, const DagState* fst, const int* finfo, const float* fcond,
                                     const int* fnf, cudaGraphConditionalHandle retry) {
-  if (threadIdx.x != 0) return;
+  __shared__ int s_any, s_status;
   RunState* rs = p.rs;
-  if (rs->status == 0 && fst->status < 0) rs->status = fst->status;  // a timed-out wait
-  int any = 0;
-  for (int k = 0; k < p.batch; ++k) {
+  if (threadIdx.x == 0) {
+    s_any = 0;
+    if (rs->status == 0 && fst->status < 0) rs->status = fst->status;  // a timed-out wait
+    s_status = rs->status;
+  }
+  __syncthreads();
+  const double shift = rs->shift;
+  for (int k = threadIdx.x; k < p.batch; k += blockDim.x) {
     if (!p.fail[k]) continue;
     DevRec& r = p.rec[k];
     r.cond = fcond[k];
     r.fp64_tiles = fnf[k];
-    r.shift = rs->shift;
+    r.shift = shift;
     if (finfo[k] != 0) {
       r.piv = finfo[k];
       ++r.retries;
-      ++any;
+      atomicAdd(&s_any, 1);
     } else {
       r.piv = 0;
       p.fail[k] = 0;
     }
   }
-  ++rs->attempt;
-  rs->shift = rs->shift == 0.0 ? (p.prec == 1 ? 1.0 / 2048 : p.prec == 2 ? 1.0 / 32 : 1.0 / 256) : rs->shift * 4;
-  int nl = 0, nf = 0;
-  const int nall = p.l_all[0];
-  for (int q = 0; q < nall; ++q) {
-    const int k = p.l_all[1 + q];
-    const bool live = rs->status == 0 && !p.fail[k];
+  __syncthreads();
+  const bool ok = s_status == 0;
+  for (int k = threadIdx.x; k < p.batch; k += blockDim.x) {
+    const int live = ok && !p.fail[k];
     p.live_flag[k] = live;
     p.rec[k].live = live;
-    if (live) p.l_live[1 + nl++] = k;
-    else if (p.fail[k]) p.l_fail[1 + nf++] = k;
   }
-  p.l_live[0] = nl;
-  p.l_fail[0] = nf;
-  cudaGraphSetConditional(retry, (rs->status == 0 && any > 0 && rs->attempt < 8) ? 1u : 0u);
+  block_compact(p.l_all, p.l_live, [&](int k) { return ok && !p.fail[k]; });
+  block_compact(p.l_all, p.l_fail, [&](int k) { return ok && p.fail[k] != 0; });
+  if (threadIdx.x == 0) {
+    ++rs->attempt;
+    rs->shift = shift == 0.0 ? (p.prec == 1 ? 1.0 / 2048 : p.prec == 2 ? 1.0 / 32 : 1.0 / 256) : shift * 4;
+    cudaGraphSetConditional(retry, (ok && s_any > 0 && rs->attempt < 8) ? 1u : 0u);
+  }
 }
 
 // W = fl32(A) for the matrices of the refactorisation list, the diagonal scaled by (1 + shift)
@@ -1377,53 +1415,47 @@ __global__ void norms_kernel(RunPtrs p) {
 
 // the active list: the matrices of `from` whose backward error is above the loop's target (half the
 // tolerance, so that the final check on the true residual meets the tolerance itself) and which have
-// iterations left; sets the CG loop's condition
+// iterations left; sets the CG loop's condition. Called by every thread of the CTA.
 __device__ void select_active(const RunPtrs& p, const int* from, cudaGraphConditionalHandle loop) {
-  int na = 0;
-  const int nfrom = from[0];
-  for (int q = 0; q < nfrom; ++q) {
+  auto go = [&](int k) { return p.be[k] > 0.5 * p.tol && p.rec[k].iterations < p.maxiter; };
+  for (int q = threadIdx.x; q < from[0]; q += blockDim.x) {
     const int k = from[1 + q];
-    const bool go = p.be[k] > 0.5 * p.tol && p.rec[k].iterations < p.maxiter;
-    p.act_flag[k] = go;
-    if (go) p.l_act[1 + na++] = k;
+    p.act_flag[k] = go(k);
   }
-  p.l_act[0] = na;
-  p.l_true[0] = 0;
-  cudaGraphSetConditional(loop, na > 0 ? 1u : 0u);
+  block_compact(from, p.l_act, go);
+  if (threadIdx.x == 0) cudaGraphSetConditional(loop, p.l_act[0] > 0 ? 1u : 0u);
 }
 
 // start of CG: rz = r.z, the backward error of x0, the first active list
 __global__ void pcg_start_kernel(RunPtrs p, cudaGraphConditionalHandle loop) {
-  if (threadIdx.x != 0) return;
-  for (int q = 0; q < p.l_live[0]; ++q) {
+  for (int q = threadIdx.x; q < p.l_live[0]; q += blockDim.x) {
     const int k = p.l_live[1 + q];
     for (int j = 0; j < p.nrhs; ++j) p.rz[(size_t)k * kMaxRhs + j] = st_at(p.stats, k, j, 0);
     p.be[k] = backward_of(p, k);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) p.l_true[0] = 0;
   select_active(p, p.l_live, loop);
 }
 
 // alpha = (r.z) / (p.q); every 8th iteration the true residual replaces the recursive one
 __global__ void pcg_alpha_kernel(RunPtrs p) {
-  if (threadIdx.x != 0) return;
   const int na = p.l_act[0];
-  for (int q = 0; q < na; ++q) {
+  const bool due = (p.rs->it + 1) % 8 == 0;
+  for (int q = threadIdx.x; q < na; q += blockDim.x) {
     const int k = p.l_act[1 + q];
     for (int j = 0; j < p.nrhs; ++j) {
       const double pq = st_at(p.stats, k, j, 0);
       p.coef[(size_t)k * kMaxRhs + j] = pq != 0.0 ? p.rz[(size_t)k * kMaxRhs + j] / pq : 0.0;
     }
+    if (due) p.l_true[1 + q] = k;
   }
-  const bool due = (p.rs->it + 1) % 8 == 0;
-  p.l_true[0] = due ? na : 0;
-  if (due)
-    for (int q = 0; q < na; ++q) p.l_true[1 + q] = p.l_act[1 + q];
+  if (threadIdx.x == 0) p.l_true[0] = due ? na : 0;
 }
 
 // after the preconditioner: the backward error, beta = (r.z)_new / (r.z)_old
 __global__ void pcg_beta_kernel(RunPtrs p) {
-  if (threadIdx.x != 0) return;
-  for (int q = 0; q < p.l_act[0]; ++q) {
+  for (int q = threadIdx.x; q < p.l_act[0]; q += blockDim.x) {
     const int k = p.l_act[1 + q];
     ++p.rec[k].iterations;
     p.be[k] = backward_of(p, k);
@@ -1437,14 +1469,13 @@ __global__ void pcg_beta_kernel(RunPtrs p) {
 
 // end of a CG iteration: the next active list (a subset of the current one) and the loop condition
 __global__ void pcg_select_kernel(RunPtrs p, cudaGraphConditionalHandle loop) {
-  if (threadIdx.x != 0) return;
-  ++p.rs->it;
-  // select_active writes l_act while reading it: entries only move forward, so copy it first
-  int* from = p.l_true;  // free at this point of the iteration (rebuilt by the next alpha kernel)
-  const int na = p.l_act[0];
-  from[0] = na;
-  for (int q = 0; q < na; ++q) from[1 + q] = p.l_act[1 + q];
-  select_active(p, from, loop);
+  // the current list moves to l_true (free at this point of the iteration; the next alpha kernel
+  // rebuilds it), and the next active list is compacted from there
+  for (int q = threadIdx.x; q <= p.l_act[0]; q += blockDim.x) p.l_true[q] = p.l_act[q];
+  if (threadIdx.x == 0) ++p.rs->it;
+  __syncthreads();
+  select_active(p, p.l_true, loop);
+  if (threadIdx.x == 0) p.l_true[0] = 0;
 }
 
 // final check on the true residual of every live matrix
@@ -1600,7 +1631,7 @@ int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
   const size_t fw = L.fwork_bytes;
   const gbx::mixed::InfoPtrs fi = gbx::mixed::info_ptrs(r.batch, r.n, r.NB, fwork);
 
-  run_init_kernel<<<1, 256, 0, s>>>(p);
+  run_init_kernel<<<1, kRunThreads, 0, s>>>(p);
   // 0. one pass over A: W = fl32(A) for the first factorisation, the split of A for the residual
   //    products, and the row sums of |A|
   if (cudaMemsetAsync(rowsum, 0, (size_t)L.sumN * 8, s) != cudaSuccess) return GBX_ERR_CUDA;
@@ -1612,7 +1643,7 @@ int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
   if (int e = conditional_handle(s, h_retry)) return e;
   if (int e = conditional_handle(s, h_cg)) return e;
   if (int e = gbx::mixed::run_batch(r.batch, r.n, r.NB, r.W, r.prec, r.fp64_cond, p.fail, fwork, fw, s)) return e;
-  factor_check_kernel<<<1, 32, 0, s>>>(p, fi.st, fi.minfo, fi.cond, fi.nfp64, h_retry);
+  factor_check_kernel<<<1, kRunThreads, 0, s>>>(p, fi.st, fi.minfo, fi.cond, fi.nfp64, h_retry);
   {
     cudaGraphNode_t node;
     if (int e = begin_while(s, body_s, h_retry, node)) return e;
@@ -1620,7 +1651,7 @@ int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
                                                                                      r.NB);
     if (int e = gbx::mixed::run_batch(r.batch, r.n, r.NB, r.W, r.prec, r.fp64_cond, p.fail, fwork, fw, body_s))
       return e;
-    factor_check_kernel<<<1, 32, 0, body_s>>>(p, fi.st, fi.minfo, fi.cond, fi.nfp64, h_retry);
+    factor_check_kernel<<<1, kRunThreads, 0, body_s>>>(p, fi.st, fi.minfo, fi.cond, fi.nfp64, h_retry);
     if (int e = end_while(s, body_s, node)) return e;
   }
   // 2. the preconditioner's diagonal inverses; ||A||_inf and ||b_j||_inf
@@ -1637,7 +1668,7 @@ int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
   emit_copy(r, s, p.l_live, P, Z);
   emit_stats(r, s, p.l_live, R, Z, p.stats);
   emit_stats(r, s, p.l_live, r.X, nullptr, p.stats_x);
-  pcg_start_kernel<<<1, 32, 0, s>>>(p, h_cg);
+  pcg_start_kernel<<<1, kRunThreads, 0, s>>>(p, h_cg);
   // 4. preconditioned CG in FP64 (a WHILE node), each matrix until its own backward error meets
   //    the loop's target or it runs out of iterations
   {
@@ -1647,7 +1678,7 @@ int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
     emit_axpy(r, b, p.l_act, Q, Q, p.coef, -1.0, 2);  // q = 0
     emit_symm(r, b, p.l_act, 1.0, P, Q);              // q = A p
     emit_stats(r, b, p.l_act, P, Q, p.stats);
-    pcg_alpha_kernel<<<1, 32, 0, b>>>(p);
+    pcg_alpha_kernel<<<1, kRunThreads, 0, b>>>(p);
     emit_axpy(r, b, p.l_act, r.X, P, p.coef, 1.0, 0);
     emit_axpy(r, b, p.l_act, R, Q, p.coef, -1.0, 0);
     emit_copy(r, b, p.l_true, R, r.B);  // every 8th iteration: the true residual against drift
@@ -1655,9 +1686,9 @@ int emit_run(Run& r, cudaStream_t s, cudaStream_t body_s) {
     if (int e = emit_precond(r, b, p.act_flag, R, Z)) return e;
     emit_stats(r, b, p.l_act, R, Z, p.stats);
     emit_stats(r, b, p.l_act, r.X, nullptr, p.stats_x);
-    pcg_beta_kernel<<<1, 32, 0, b>>>(p);
+    pcg_beta_kernel<<<1, kRunThreads, 0, b>>>(p);
     emit_axpy(r, b, p.l_act, P, Z, p.coef_b, 1.0, 1);  // p = z + beta p
-    pcg_select_kernel<<<1, 32, 0, b>>>(p, h_cg);
+    pcg_select_kernel<<<1, kRunThreads, 0, b>>>(p, h_cg);
     if (int e = end_while(s, body_s, node)) return e;
   }
   // 5. final check on the true residual of every live matrix
@@ -1742,9 +1773,9 @@ extern "C" int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int N
   return GBX_OK;
 }
 
-extern "C" int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, void* work,
+extern "C" int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, int sched, void* work,
                                             size_t work_bytes, void* stream) {
-  if (check_args(batch, n, NB, nrhs, prec) || !work) return GBX_ERR_ARG;
+  if (check_args(batch, n, NB, nrhs, prec) || !work || sched < 0 || sched > 1) return GBX_ERR_ARG;
   const BLayout L = blayout(batch, n, NB, nrhs);
   if (work_bytes < L.total) return GBX_ERR_WORKSPACE;
   if (int e = set_attrs()) return e;
@@ -1799,7 +1830,7 @@ extern "C" int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int
   RunState rs;
   std::memset(&rs, 0, sizeof(rs));
   rs.sig = plan_signature(batch, n, NB, nrhs, prec);
-  if (int e = gbx::mixed::plan_batch(batch, n, NB, work, L.fwork_bytes, s)) return e;
+  if (int e = gbx::mixed::plan_batch(batch, n, NB, work, L.fwork_bytes, s, sched)) return e;
   if (cudaMemcpyAsync(base + L.mats, mats.data(), batch * sizeof(RMat), cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemcpyAsync(base + L.lists, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
       cudaMemcpyAsync(base + L.tasks, tf.data(), tf.size() * sizeof(SweepTask), cudaMemcpyHostToDevice, s) !=
@@ -1900,7 +1931,7 @@ extern "C" int gbx_dposv_mixed_batched_result(int batch, const int* n, int NB, i
 extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
                                        double* X, int prec, double fp64_diag_cond, double tol, int maxiter, float* W,
                                        void* work, size_t work_bytes, gbx_refine_info* info, void* stream) {
-  if (int e = gbx_dposv_mixed_batched_plan(batch, n, NB, nrhs, prec, work, work_bytes, stream)) return e;
+  if (int e = gbx_dposv_mixed_batched_plan(batch, n, NB, nrhs, prec, 0, work, work_bytes, stream)) return e;
   if (int e = gbx_dposv_mixed_batched_exec(batch, n, NB, A, nrhs, B, X, prec, fp64_diag_cond, tol, maxiter, W, work,
                                            work_bytes, stream))
     return e;
