@@ -321,6 +321,7 @@ def run_ours(args, ws, rank, local):
         torch.cuda.empty_cache()
         line["batched_mixed"] = run_batched_mixed(gbx, dev, cpu=rank == 0 and not args.no_cpu)
     line["config_small"] = run_config1(gbx, dev, cpu=rank == 0 and not args.no_cpu)
+    line["ttg_flowgraph"] = run_ttg_flowgraph(gbx, dev)
     line["potri"] = run_potri(gbx, dev, cpu=rank == 0 and not args.no_cpu)
 
     if rank == 0 and not args.no_cpu:
@@ -780,6 +781,54 @@ def run_config1(gbx, dev, cpu=True, reps=5):
         # the CPU and GPU factors of the same matrix agree
         L = torch.from_numpy(base.reshape(-1)).to(dev)
         out["max_abs_diff_gpu_vs_cpu"] = (L - T).abs().max().item()
+    return out
+
+
+def run_ttg_flowgraph(gbx, dev, N=16384, NB=512, iters=2, chain_tasks=20000):
+    """The drop-in path: the potrf flowgraph on the TTG API (make_tt device tasks calling the tile
+    kernels, ttg_gb300/potrf/testing_dpotrf, the reference driver's timed region: generation on the
+    device, factorisation, write-back of the factor) at N=16384 NB=512 and its GF/s as the driver
+    prints them; beside it the whole-flowgraph executor (gbx_dpotrf_tiled) on the same matrix, and
+    the per-device-task overhead of the runtime (ttg_gb300/potrf/chain_dev, a chain of device tasks
+    as in the reference's task benchmark)."""
+    import re
+
+    import torch
+
+    from ttg_gb300 import build as gb
+    out = {"config": {"workload": "potrf FP64 N=%d NB=%d through the TTG flowgraph (device tasks), PLASMA "
+                                  "generator seed 3872" % (N, NB), "N": N, "NB": NB}}
+    drv = gb.build_driver()
+    r = subprocess.run([drv, "-N", str(N), "-t", str(NB), "-n", str(iters), "-x"], capture_output=True, text=True,
+                       timeout=1200)
+    gfs = [float(x) for x in re.findall(r"([0-9.eE+-]+) GF/s", r.stdout)]
+    ms = [float(x) for x in re.findall(r"Execution Time \(milliseconds\) : ([0-9.eE+-]+)", r.stdout)]
+    out["flowgraph"] = {"rc": r.returncode, "gflops_per_iter": gfs, "ms_per_iter": ms,
+                        "tflops": max(gfs) / 1e3 if gfs else None}
+    # the same factorisation by the persistent executor, device time
+    t = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
+    gbx.plgsy(t, N, NB, N, 3872)
+    work = gbx.potrf_tiled(t.clone(), N, NB)
+    T = t.clone()
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    gbx.potrf_tiled(T, N, NB, workspace=work, check=False)
+    e1.record()
+    e1.synchronize()
+    exe_ms = e0.elapsed_time(e1)
+    out["executor"] = {"ms": exe_ms, "tflops": flops_factor(N) / (exe_ms * 1e-3) / 1e12}
+    if gfs:
+        out["flowgraph_vs_executor"] = out["flowgraph"]["tflops"] / out["executor"]["tflops"]
+    del t, T, work
+    chain = gb.build_chain()
+    out["chain"] = {}
+    for flows in (0, 1):
+        r = subprocess.run([chain, "-f", str(flows), "-n", str(chain_tasks)], capture_output=True, text=True,
+                           timeout=600)
+        m = re.search(r"avg ([0-9.eE+-]+)", r.stdout)
+        out["chain"]["flows_%d" % flows] = {"rc": r.returncode, "tasks": chain_tasks + 1,
+                                            "us_per_task": float(m.group(1)) if m else None}
     return out
 
 

@@ -95,6 +95,15 @@ int gbx_dsyrk_ln_tile(int n, int k, const double* A, int lda, double* C, int ldc
 int gbx_dgemm_nt_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                       double* C, int ldc, void* stream);
 
+/* Tile kernels of the backward sweep of the tiled solve flowgraph (ttg_gb300/potrf/potrs.h). The
+ * reference has no solve; these are the non-transposed forms of its TRSM and GEMM calls
+ * (examples/potrf/potrf.h:292-297 and 547-553), for right-hand-side tiles stored as nrhs x NB:
+ *   gbx_dtrsm_rln_tile: B := B * L^{-1}, B m x n, L n x n lower non-unit (n <= 3200);
+ *   gbx_dgemm_nn_tile:  C := C - A * B, A m x k, B k x n. */
+int gbx_dtrsm_rln_tile(int m, int n, const double* L, int ldl, double* B, int ldb, void* stream);
+int gbx_dgemm_nn_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb, double* C, int ldc,
+                      void* stream);
+
 /* ============================================================================================
  * Whole-flowgraph device executor. One persistent launch runs every POTRF/TRSM/SYRK/GEMM task
  * of the potrf flowgraph (examples/potrf/potrf.h:670-764) over a tile-major lower matrix: CTAs

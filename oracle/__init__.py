@@ -40,6 +40,9 @@ def lib():
         L.orc_syrk_ln_tile.argtypes = [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int]
         L.orc_gemm_nt_tile.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp,
                                        ctypes.c_int, _dp, ctypes.c_int]
+        L.orc_trsm_rln_tile.argtypes = [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp, ctypes.c_int]
+        L.orc_gemm_nn_tile.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp,
+                                       ctypes.c_int, _dp, ctypes.c_int]
         L.orc_blas_load.restype = ctypes.c_int
         L.orc_blas_load.argtypes = [ctypes.c_char_p]
         L.orc_blas_loaded.restype = ctypes.c_int

@@ -232,6 +232,34 @@ extern "C" void orc_gemm_nt_tile(int m, int n, int k, const double* A, int lda, 
     }
 }
 
+// The backward sweep's tile operations of the tiled solve on nrhs x NB right-hand-side tiles (the
+// reference has no solve; these are the non-transposed forms of its TRSM and GEMM).
+// B := B * L^{-1} (Right, Lower, NoTrans, NonUnit) — column by column, right to left.
+extern "C" void orc_trsm_rln_tile(int m, int n, const double* L, int ldl, double* B, int ldb) {
+  for (int j = n - 1; j >= 0; --j) {
+    double* bj = B + (int64_t)j * ldb;
+    for (int k = j + 1; k < n; ++k) {
+      const double l = L[k + (int64_t)j * ldl];
+      const double* bk = B + (int64_t)k * ldb;
+      for (int i = 0; i < m; ++i) bj[i] -= bk[i] * l;
+    }
+    const double d = L[j + (int64_t)j * ldl];
+    for (int i = 0; i < m; ++i) bj[i] = bj[i] / d;
+  }
+}
+
+// C := C - A B, A m x k, B k x n.
+extern "C" void orc_gemm_nn_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                                 double* C, int ldc) {
+  for (int j = 0; j < n; ++j)
+    for (int l = 0; l < k; ++l) {
+      const double b = B[l + (int64_t)j * ldb];
+      const double* al = A + (int64_t)l * lda;
+      double* cj = C + (int64_t)j * ldc;
+      for (int i = 0; i < m; ++i) cj[i] -= al[i] * b;
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // OpenBLAS tile kernels (Fortran ABI, hidden string lengths appended)
 // ------------------------------------------------------------------------------------------------

@@ -56,6 +56,9 @@ void orc_trsm_rlt_tile(int m, int n, const double* L, int ldl, double* B, int ld
 void orc_syrk_ln_tile(int n, int k, const double* A, int lda, double* C, int ldc);
 void orc_gemm_nt_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
                       double* C, int ldc);
+void orc_trsm_rln_tile(int m, int n, const double* L, int ldl, double* B, int ldb);
+void orc_gemm_nn_tile(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                      double* C, int ldc);
 
 /* ---- OpenBLAS tile kernels (optional, for timing the CPU baseline) ---- */
 /* loads the given shared library; returns 0 on success */

@@ -123,6 +123,36 @@ def test_tile_dtrsm_rlt(gbx, cuda, m, n):
     assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("m,n", [(1, 512), (8, 512), (3, 100), (16, 129), (40, 33)])
+def test_tile_dtrsm_rln(gbx, cuda, m, n):
+    """B := B L^{-1} (the backward sweep of the solve flowgraph) against the oracle."""
+    L = np.linalg.cholesky(spd(n, 7))
+    rng = np.random.default_rng(m * 3 + n)
+    B = rng.uniform(-1, 1, (m, n))
+    dL, dB = colmajor_dev(L, n + 3, cuda), colmajor_dev(B, m + 1, cuda)
+    gbx.call("gbx_dtrsm_rln_tile", m, n, _vp(dL), n + 3, _vp(dB), m + 1, _s())
+    got = from_colmajor(dB, m)
+    ref = np.asfortranarray(B.copy())
+    oracle.lib().orc_trsm_rln_tile(m, n, oracle._p(np.asfortranarray(L)), n, oracle._p(ref), m)
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+    assert np.all(np.isnan(dB.cpu().numpy()[:, m:m + 1]))  # padding rows untouched
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 512, 512), (8, 512, 300), (5, 37, 129), (16, 16, 16)])
+def test_tile_dgemm_nn(gbx, cuda, m, n, k):
+    """C := C - A B against the oracle, within the standard GEMM bound."""
+    rng = np.random.default_rng(m + 5 * n + k)
+    A, B, C = rng.uniform(-1, 1, (m, k)), rng.uniform(-1, 1, (k, n)), rng.uniform(-1, 1, (m, n))
+    dA, dB, dC = colmajor_dev(A, m + 2, cuda), colmajor_dev(B, k + 1, cuda), colmajor_dev(C, m + 3, cuda)
+    gbx.call("gbx_dgemm_nn_tile", m, n, k, _vp(dA), m + 2, _vp(dB), k + 1, _vp(dC), m + 3, _s())
+    got = from_colmajor(dC, m)
+    ref = np.asfortranarray(C.copy())
+    oracle.lib().orc_gemm_nn_tile(m, n, k, oracle._p(np.asfortranarray(A)), m, oracle._p(np.asfortranarray(B)), k,
+                                  oracle._p(ref), m)
+    bound = 4 * k * EPS * (np.abs(C) + np.abs(A) @ np.abs(B))
+    assert np.all(np.abs(got - ref) <= bound)
+
+
 @pytest.mark.parametrize("n", [1, 31, 128, 129, 512, 1000])
 def test_tile_dpotrf(gbx, cuda, n):
     import torch

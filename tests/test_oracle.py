@@ -172,3 +172,20 @@ def test_potri_oracle_inverse(N, NB):
     Ainv = np.tril(oracle.tiles_to_lower(t, N, NB))
     ref = np.tril(np.linalg.inv(A))
     assert np.abs(Ainv - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_backward_sweep_tile_ops_against_numpy():
+    """The oracle's restatements of the solve flowgraph's backward-sweep tile operations:
+    B L^{-1} (right, lower, non-transposed TRSM) and C - A B (non-transposed GEMM)."""
+    rng = np.random.default_rng(3)
+    n, m, k = 45, 4, 17
+    L = np.linalg.cholesky(oracle.uniform_sym_full(n, 5))
+    B = rng.standard_normal((m, n))
+    X = np.asfortranarray(B.copy())
+    oracle.lib().orc_trsm_rln_tile(m, n, oracle._p(np.asfortranarray(L)), n, oracle._p(X), m)
+    assert np.abs(X @ L - B).max() <= 1e-13
+    A2, B2, C = rng.standard_normal((m, k)), rng.standard_normal((k, n)), rng.standard_normal((m, n))
+    Cf = np.asfortranarray(C.copy())
+    oracle.lib().orc_gemm_nn_tile(m, n, k, oracle._p(np.asfortranarray(A2)), m, oracle._p(np.asfortranarray(B2)), k,
+                                  oracle._p(Cf), m)
+    assert np.abs(Cf - (C - A2 @ B2)).max() <= 1e-13

@@ -118,3 +118,22 @@ def test_gb300_potrf_flowgraph_timed_iterations(gbx, cuda):
     rc, log = _run([drv, "-N", "4096", "-t", "512", "-n", "2", "-x"], timeout=600)
     assert rc == 0, log
     assert log.count("TTG Execution Time") == 2, log
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N,NB,nrhs", [(1000, 128, 3), (2500, 512, 1), (160, 32, 16)])
+def test_gb300_potrs_flowgraph_matches_oracle(gbx, cuda, tmp_path, N, NB, nrhs):
+    """The solve as a TTG flowgraph (forward and backward TRSM/GEMM device tasks over right-hand-side
+    tiles, ttg_gb300/potrf/potrs.h) after the factorisation flowgraph: the driver's backward-error
+    check passes and X equals the oracle's solve with the same factor."""
+    drv = _driver(gbx)
+    lf, xf = str(tmp_path / "L.bin"), str(tmp_path / "X.bin")
+    rc, log = _run([drv, "-N", str(N), "-t", str(NB), "-s", str(nrhs), "-o", lf, "-p", xf], timeout=600)
+    assert rc == 0 and "Factorization is CORRECT" in log and "Solve is CORRECT" in log, log
+    L = np.fromfile(lf)
+    X = np.fromfile(xf).reshape(nrhs, N)
+    i = np.arange(N)[:, None]
+    r = np.arange(nrhs)[None, :]
+    B = ((7919 * i + 104729 * r) % 1000) / 500.0 - 1.0  # the driver's right-hand sides, N x nrhs
+    Xref = oracle.potrs_tiled(L, N, NB, B)
+    assert np.max(np.abs(X.T - Xref)) <= 1e-12 * np.max(np.abs(Xref))

@@ -49,6 +49,8 @@ SIGNATURES = {
     "gbx_dtrsm_rlt_tile": (_i, [_i, _i, _vp, _i, _vp, _i, _vp]),
     "gbx_dsyrk_ln_tile": (_i, [_i, _i, _vp, _i, _vp, _i, _vp]),
     "gbx_dgemm_nt_tile": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp]),
+    "gbx_dtrsm_rln_tile": (_i, [_i, _i, _vp, _i, _vp, _i, _vp]),
+    "gbx_dgemm_nn_tile": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp]),
     "gbx_dpotrf_tiled_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dpotrf_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
     "gbx_dpotrf_tiled_status": (_i, [_vp, _vp]),

@@ -69,7 +69,8 @@ DRIVER = os.path.join(HERE, "potrf", "testing_dpotrf")
 def build_driver(force=False):
     """The potrf flowgraph driver on the TTG API (C++ host code linked to libgbx_potrf.so)."""
     lib = build()
-    deps = [DRIVER_SRC, lib, os.path.join(HERE, "potrf", "potrf.h"), os.path.join(HERE, "potrf", "matrix.h")]
+    deps = [DRIVER_SRC, lib, os.path.join(HERE, "potrf", "potrf.h"), os.path.join(HERE, "potrf", "potrs.h"),
+            os.path.join(HERE, "potrf", "matrix.h")]
     deps += glob.glob(os.path.join(INCLUDE, "ttg", "*.h")) + glob.glob(os.path.join(INCLUDE, "ttg", "*", "*.h"))
     if force or _stale(DRIVER, deps):
         cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))) if os.path.isabs(nvcc()) else "/usr/local/cuda"
@@ -82,6 +83,24 @@ def build_driver(force=False):
     return DRIVER
 
 
+CHAIN_SRC = os.path.join(HERE, "potrf", "chain_dev.cc")
+CHAIN = os.path.join(HERE, "potrf", "chain_dev")
+
+
+def build_chain(force=False):
+    """The device-task chain benchmark on the TTG API (per-task runtime overhead)."""
+    deps = [CHAIN_SRC] + glob.glob(os.path.join(INCLUDE, "ttg", "*.h")) + glob.glob(os.path.join(INCLUDE, "ttg", "*", "*.h"))
+    if force or _stale(CHAIN, deps):
+        cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))) if os.path.isabs(nvcc()) else "/usr/local/cuda"
+        cmd = ["g++", "-std=c++20", "-O2", "-pthread", "-I", INCLUDE, "-I", os.path.join(cuda, "include"), CHAIN_SRC,
+               "-o", CHAIN, "-L", os.path.join(cuda, "lib64"), "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("chain benchmark build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return CHAIN
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose=True))
     print(build_driver(force=True))
+    print(build_chain(force=True))

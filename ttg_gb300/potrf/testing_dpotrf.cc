@@ -1,7 +1,9 @@
 // Driver of the GB300 potrf flowgraph, with the command line of the reference's
 // examples/potrf/testing_dpotrf.cc:41-87: -N order, -t tile size, -c worker threads, -n timed
 // iterations, -x skip the check. Extra: -o FILE writes the factor tiles (tile-major lower
-// storage) after the checked run.
+// storage) after the checked run; -s NRHS then solves A X = B through the solve flowgraph
+// (potrs.h) for NRHS right-hand sides B(i, r) = ((7919 i + 104729 r) mod 1000) / 500 - 1, checks
+// the normwise backward error and, with -p FILE, writes X (NRHS rows of N, row r = column r of X).
 //
 // Each iteration generates the PLASMA test matrix (seed 3872, bump N) with one device task per
 // tile, factorises it through the flowgraph and writes the factor back to the host matrix, all
@@ -18,6 +20,7 @@
 #include <vector>
 
 #include "potrf.h"
+#include "potrs.h"
 
 using namespace gbx_potrf;
 
@@ -96,6 +99,59 @@ static void run_once(TiledMatrix<double>& A, int N, bool defer) {
   ttg::fence(ttg::default_execution_context());
 }
 
+// the solve flowgraph on the factor in L; returns the normwise backward error against A0
+static double run_solve(TiledMatrix<double>& L, const TiledMatrix<double>& A0, int N, int NB, int nrhs,
+                        std::vector<double>& X) {
+  std::vector<double> rhs(potrs::TiledRhs<double>::num_elements(N, NB, nrhs), 0.0);
+  potrs::TiledRhs<double> B(rhs.data(), N, NB, nrhs);
+  auto b_at = [](long i, int r) { return (double)((7919L * i + 104729L * r) % 1000) / 500.0 - 1.0; };
+  for (long i = 0; i < N; ++i)
+    for (int r = 0; r < nrhs; ++r) B.tile_ptr((int)(i / NB))[r + (i % NB) * nrhs] = b_at(i, r);
+  ttg::Edge<Key2, potrs::Tile> lin("L tiles");
+  ttg::Edge<Key1, potrs::Tile> bin("B tiles"), xout("X tiles");
+  auto feed = ttg::make_tt<void>([&](std::tuple<ttg::Out<Key2, potrs::Tile>, ttg::Out<Key1, potrs::Tile>>& out) {
+    for (int m = 0; m < (int)L.rows(); ++m)
+      for (int k = 0; k <= m; ++k) ttg::send<0>(Key2{m, k}, L(m, k), out);
+    for (int k = 0; k < B.tiles(); ++k) ttg::send<1>(Key1{k}, B(k), out);
+  }, ttg::edges(), ttg::edges(lin, bin), "Solve inputs", {}, {"L", "B"});
+  auto ops = potrs::make_potrs_ttg(L, nrhs, lin, bin, xout);
+  auto result = ttg::make_tt([&B](const Key1& key, const potrs::Tile& x, std::tuple<>&) {
+    double* dst = B.tile_ptr(key[0]);
+    if (dst != x.data()) std::copy_n(x.data(), x.rows() * x.cols(), dst);
+  }, ttg::edges(xout), ttg::edges(), "Solution", {"X"}, {});
+  if (!ttg::make_graph_executable(feed.get())) throw std::runtime_error("solve graph not connected");
+  feed->invoke();
+  ttg::execute(ttg::default_execution_context());
+  ttg::fence(ttg::default_execution_context());
+  // X (row-major by right-hand side) and the backward error max_r ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)
+  X.assign((size_t)nrhs * N, 0.0);
+  for (long i = 0; i < N; ++i)
+    for (int r = 0; r < nrhs; ++r) X[(size_t)r * N + i] = B.tile_ptr((int)(i / NB))[r + (i % NB) * nrhs];
+  auto a_at = [&](long i, long j) {
+    if (i < j) std::swap(i, j);
+    return A0.tile_ptr((int)(i / NB), (int)(j / NB))[(i % NB) + (j % NB) * (long)NB];
+  };
+  double anorm = 0.0, worst = 0.0;
+  for (long i = 0; i < N; ++i) {
+    double s = 0.0;
+    for (long j = 0; j < N; ++j) s += std::fabs(a_at(i, j));
+    anorm = std::max(anorm, s);
+  }
+  for (int r = 0; r < nrhs; ++r) {
+    const double* x = X.data() + (size_t)r * N;
+    double rmax = 0.0, xmax = 0.0, bmax = 0.0;
+    for (long i = 0; i < N; ++i) {
+      double s = b_at(i, r);
+      for (long j = 0; j < N; ++j) s -= a_at(i, j) * x[j];
+      rmax = std::max(rmax, std::fabs(s));
+      xmax = std::max(xmax, std::fabs(x[i]));
+      bmax = std::max(bmax, std::fabs(b_at(i, r)));
+    }
+    worst = std::max(worst, rmax / (anorm * xmax + bmax));
+  }
+  return worst;
+}
+
 int main(int argc, char** argv) {
   int NB = 32, N = 5 * NB, nthreads = -1, niter = 3;
   if (auto o = opt(argv + 1, argv + argc, "-N")) N = std::atoi(o);
@@ -103,6 +159,9 @@ int main(int argc, char** argv) {
   if (auto o = opt(argv + 1, argv + argc, "-c")) nthreads = std::atoi(o);
   if (auto o = opt(argv + 1, argv + argc, "-n")) niter = std::atoi(o);
   const char* outfile = opt(argv + 1, argv + argc, "-o");
+  const char* xfile = opt(argv + 1, argv + argc, "-p");
+  int nrhs = 0;
+  if (auto o = opt(argv + 1, argv + argc, "-s")) nrhs = std::atoi(o);
   const bool check = !has(argv + 1, argv + argc, "-x");
   const bool defer = !has(argv + 1, argv + argc, "-w");
   ttg::initialize(argc, argv, nthreads);
@@ -140,6 +199,26 @@ int main(int argc, char** argv) {
         FILE* f = std::fopen(outfile, "wb");
         std::fwrite(store.data(), sizeof(double), store.size(), f);
         std::fclose(f);
+      }
+      if (nrhs > 0) {
+        std::vector<double> X;
+        auto beg = std::chrono::high_resolution_clock::now();
+        const double be = run_solve(A, A0, N, NB, nrhs, X);
+        auto end = std::chrono::high_resolution_clock::now();
+        std::printf("TTG solve (%d right-hand sides) incl. check: %g ms\n", nrhs,
+                    std::chrono::duration_cast<std::chrono::microseconds>(end - beg).count() / 1e3);
+        std::printf("-- max_r ||b - A x||_oo / (||A||_oo ||x||_oo + ||b||_oo) = %g\n", be);
+        if (!(be <= 1e-14)) {
+          std::printf("-- Solve is suspicious !\n");
+          ret = 1;
+        } else {
+          std::printf("-- Solve is CORRECT !\n");
+        }
+        if (xfile) {
+          FILE* f = std::fopen(xfile, "wb");
+          std::fwrite(X.data(), sizeof(double), X.size(), f);
+          std::fclose(f);
+        }
       }
     }
   } catch (const std::exception& e) {
