@@ -352,6 +352,36 @@ int gbx_dposv_batched_ex(int batch, const int* n, const long long* offA, const l
                          double* A, double* B, int nrhs, int mode, int refine, float* L32, int* info, int ctas,
                          void* work, size_t work_bytes, void* stream);
 
+/* ============================================================================================
+ * Device task queue: the persistent device-side ready queue behind the TTG API's device tasks
+ * (include/ttg/device/gbx_queue.h). Replaces the reference's per-task hand-off of device tasks to
+ * PaRSEC's GPU manager (parsec/ttg.h:1521-1672, 2678-2727).
+ * ========================================================================================== */
+
+/* Creates / destroys a queue (at most 64 live queues). */
+int gbx_taskq_create(void** q);
+int gbx_taskq_destroy(void* q);
+
+/* The queue's recording stream handle. Passed as the `stream` of gbx_dpotrf_tile,
+ * gbx_dtrsm_rlt_tile, gbx_dsyrk_ln_tile, gbx_dgemm_nt_tile, gbx_dtrsm_rln_tile or
+ * gbx_dgemm_nn_tile, it makes the call append its tile operation to the queue instead of launching
+ * a kernel (nothing runs, nothing is read). The handle is not a CUDA stream: give it to no other
+ * call. An operation waits for the last writer of every tile it reads or writes and for the
+ * readers of every tile it writes (tiles are identified by their base device pointers). The
+ * operands must stay allocated until the run that executes the operation has completed. */
+void* gbx_taskq_stream(void* q);
+
+/* Operations recorded and not yet run. */
+long long gbx_taskq_pending(void* q);
+
+/* Runs every operation recorded since the previous run, in one persistent launch on `stream`
+ * (asynchronous; operations of earlier runs are complete once their run is). A POTRF operation
+ * writes 0 or its first bad pivot to its devInfo. */
+int gbx_taskq_run(void* q, void* stream);
+
+/* Synchronises `stream` and returns the status of the last run: 0 or GBX_ERR_TIMEOUT. */
+int gbx_taskq_status(void* q, void* stream);
+
 /* Test hook for the failure path: launches the executor on a 2 x 2 block problem whose first
  * task is skipped, so the dependency wait of the second task can never be satisfied and must
  * run out after `timeout_ns`. Returns the status the kernel reported (GBX_ERR_TIMEOUT when the

@@ -33,7 +33,7 @@ struct BufferState {
   cudaEvent_t dev_ready = nullptr;  // completes when the device copy is valid
 
   ~BufferState() {
-    if (dev) rt::Runtime::get().pool().release(dev, bytes);
+    if (dev) rt::Runtime::get().release_device(dev, bytes);  // deferred while a device queue may read it
     if (dev_ready) cudaEventDestroy(dev_ready);
   }
 
@@ -69,15 +69,20 @@ struct BufferState {
       host_version = dev_version;
     }
   }
-  // Synchronous version for host tasks.
+  bool device_newer() {
+    std::lock_guard<std::mutex> lk(m);
+    return dev && dev_version > host_version && host;
+  }
+  // Synchronous version for host tasks. With a device queue, the operations recorded so far (which
+  // may write this buffer) run first, unless the calling host job already waited for a batch.
   void to_host_sync() {
-    bool need;
-    {
-      std::lock_guard<std::mutex> lk(m);
-      need = dev && dev_version > host_version && host;
+    if (!device_newer()) return;
+    auto& R = rt::Runtime::get();
+    cudaStream_t s = R.copy_stream();
+    if (R.device_queue() && !device::detail::tl_after_flush()) {
+      s = R.flush();
+      rt::cuda_check(cudaStreamSynchronize(s), "device queue sync");
     }
-    if (!need) return;
-    cudaStream_t s = rt::Runtime::get().copy_stream();
     to_host_async(s);
     rt::cuda_check(cudaStreamSynchronize(s), "D2H sync");
   }
@@ -317,6 +322,18 @@ template <typename T>
 inline constexpr bool has_buffer_apply_v =
     meta::is_buffer_v<T> || has_serialize1<T, BufferVisitor<buffer_apply_dummy_fn>>::value ||
     has_serialize2<T, BufferVisitor<buffer_apply_dummy_fn>>::value;
+
+/// True when some buffer of `value` has a newer device copy than host copy.
+template <typename T>
+bool value_on_device(T& value) {
+  bool any = false;
+  if constexpr (has_buffer_apply_v<std::remove_const_t<T>>) {
+    buffer_apply(value, [&any](auto& b) {
+      if (auto* s = b.state()) any = any || s->device_newer();
+    });
+  }
+  return any;
+}
 
 /// Brings every buffer of `value` up to date on the host (before a host task reads it).
 template <typename T>

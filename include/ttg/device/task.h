@@ -227,7 +227,8 @@ struct DeviceDriver {
   typename TTT::key_store key{};  // the body holds `const Key&` across suspensions: keep it alive here
   std::function<void()> release;  // releases the task's inputs and its runtime count
   device::Task task;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // stage-in copies (and the kernels, without a device queue)
+  cudaStream_t rec_stream = nullptr;  // with a device queue: its recording stream, what the body sees
   int64_t prio = 0;
   std::vector<device::detail::BufRef> touched;  // every buffer selected by the task
 
@@ -235,7 +236,7 @@ struct DeviceDriver {
 
   void set_current() {
     device::detail::tl_device() = device::Device(0);
-    device::detail::tl_stream() = stream;
+    device::detail::tl_stream() = rec_stream ? rec_stream : stream;
     ttg::detail::tl_outputs() = &tt->out_ptrs_;
   }
   static void clear_current() {
@@ -256,6 +257,8 @@ struct DeviceDriver {
       }
       switch (pr.state) {
         case device::detail::State::WaitTransfer: {
+          std::shared_lock<std::shared_mutex> staging;  // with a device queue: copies, then recording
+          if (rec_stream) staging = std::shared_lock<std::shared_mutex>(rt::Runtime::get().stage_mutex());
           set_current();
           for (auto& r : pr.select_refs) {
             const bool sync_in = r.st->sc != ttg::scope::Allocate;
@@ -269,6 +272,9 @@ struct DeviceDriver {
           continue;
         }
         case device::detail::State::WaitKernel: {
+          // with a device queue, what was recorded so far (this task's operations included) runs
+          // now, and the copies back follow the run on its stream
+          cudaStream_t ws = rec_stream ? rt::Runtime::get().flush() : stream;
           for (auto& r : pr.wait_refs) {
             // a buffer this task holds mutably may have been changed by any kernel since select
             for (auto& t : touched)
@@ -276,10 +282,10 @@ struct DeviceDriver {
                 r.st->mark_device_written();
                 break;
               }
-            r.st->to_host_async(stream);
+            r.st->to_host_async(ws);
           }
           pr.wait_refs.clear();
-          rt::Runtime::get().when_stream_done(stream, prio, [self]() {
+          rt::Runtime::get().when_stream_done(ws, prio, [self]() {
             self->set_current();
             self->task.h.resume();
             clear_current();
@@ -289,6 +295,18 @@ struct DeviceDriver {
         }
         case device::detail::State::SendOut:
         case device::detail::State::Complete: {
+          if (rec_stream) {  // device queue: the successors' operations are ordered by their operands
+            ttg::detail::tl_outputs() = &tt->out_ptrs_;
+            try {
+              for (auto& s : pr.sends) s.fn();
+            } catch (...) {
+              rt::Runtime::get().record_error(std::current_exception());
+            }
+            ttg::detail::tl_outputs() = nullptr;
+            pr.sends.clear();
+            finish();
+            return;
+          }
           rt::Runtime::get().when_stream_done(stream, prio, [self]() {
             auto& p = self->task.h.promise();
             ttg::detail::tl_outputs() = &self->tt->out_ptrs_;
@@ -324,6 +342,16 @@ template <ExecutionSpace Space, typename Key, typename Func, typename OutTerms, 
 void TT<Space, Key, Func, OutTerms, Values...>::run_task(const key_store& k, std::shared_ptr<Pending> sp) {
   auto& R = rt::Runtime::get();
   if constexpr (Space == ExecutionSpace::Host) {
+    // with a device queue, a host task that reads device data waits for the next batch to complete
+    if (R.device_queue() && !device::detail::tl_after_flush() &&
+        inputs_on_device(*sp, std::make_index_sequence<numins>{})) {
+      R.defer_host(priority(k), [this, k, sp]() {
+        device::detail::tl_after_flush() = true;
+        run_task(k, sp);
+        device::detail::tl_after_flush() = false;
+      });
+      return;
+    }
     std::vector<detail::InputRef> refs;
     try {
       sync_inputs_to_host(*sp, std::make_index_sequence<numins>{});
@@ -348,7 +376,12 @@ void TT<Space, Key, Func, OutTerms, Values...>::run_task(const key_store& k, std
     drv->prio = priority(k);
     int hint = -1;
     if (devicemap_) hint = -1;  // one GPU: the device map cannot move work elsewhere
-    drv->stream = R.pick_stream(hint);
+    if (auto* dq = R.device_queue()) {  // stage-in on the copy stream; kernels recorded into the queue
+      drv->stream = R.copy_stream();
+      drv->rec_stream = dq->record_stream();
+    } else {
+      drv->stream = R.pick_stream(hint);
+    }
     drv->release = [this, sp]() {
       release_inputs(*sp);
       rt::Runtime::get().done();

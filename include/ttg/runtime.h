@@ -20,6 +20,7 @@
 #include <memory>
 #include <mutex>
 #include <queue>
+#include <shared_mutex>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -89,6 +90,12 @@ namespace detail {
 inline Device& tl_device() {
   thread_local Device d;
   return d;
+}
+/// Set while a host job that waited for a device-queue batch brings its inputs to the host: the
+/// batch has completed, so no further run is needed before the copies.
+inline bool& tl_after_flush() {
+  thread_local bool f = false;
+  return f;
 }
 inline cudaStream_t& tl_stream() {
   thread_local cudaStream_t s = nullptr;
@@ -169,6 +176,20 @@ class DevicePool {
   }
 };
 
+/// A device task queue behind the device tasks (include/ttg/device/gbx_queue.h wires in the GB300
+/// library's): while a queue is set, device task bodies see its recording stream as their current
+/// stream, so the kernels they call append tile operations to it instead of launching, and the
+/// runtime runs what was recorded in batches, one persistent launch per batch, on a stream of its
+/// own. A batch runs when a device task waits for its buffers (`co_await wait(...)`), when the
+/// workers fall idle with host tasks waiting for device data, and at `fence`.
+struct DeviceQueue {
+  virtual ~DeviceQueue() = default;
+  virtual cudaStream_t record_stream() = 0;  // what device task bodies see as current_stream()
+  virtual long long pending() = 0;           // operations recorded and not yet run
+  virtual void run(cudaStream_t s) = 0;      // runs them on s (asynchronous)
+  virtual void check(cudaStream_t s) = 0;    // synchronises s; throws if a run failed on the device
+};
+
 class Runtime {
  public:
   static Runtime& get() {
@@ -201,9 +222,16 @@ class Runtime {
       executing_ = false;  // a re-initialised runtime waits for execute() again
       stop_ = false;
     }
+    if (dq_) {  // the device queue's last runs finish before the memory goes
+      flush();
+      reclaim(true);
+      dq_.reset();
+    }
     if (dev_ready_) {
       for (auto s : streams_) cudaStreamDestroy(s);
       streams_.clear();
+      if (exec_stream_) cudaStreamDestroy(exec_stream_);
+      exec_stream_ = nullptr;
       pool_.trim();
       dev_ready_ = false;
     }
@@ -218,10 +246,23 @@ class Runtime {
   }
 
   /// Waits until no task is ready, running or in flight on the GPU; rethrows the first task error.
+  /// With a device queue, the operations still recorded are run and waited for.
   void fence() {
     execute();
-    std::unique_lock<std::mutex> lk(m_);
-    idle_cv_.wait(lk, [this] { return active_ == 0 && q_.empty(); });
+    {
+      std::unique_lock<std::mutex> lk(m_);
+      idle_cv_.wait(lk, [this] { return active_ == 0 && q_.empty(); });
+    }
+    if (dq_) {
+      flush();
+      try {
+        dq_->check(exec_stream_);
+      } catch (...) {
+        record_error(std::current_exception());
+      }
+      reclaim(true);
+    }
+    std::lock_guard<std::mutex> lk(m_);
     if (error_) {
       auto e = error_;
       error_ = nullptr;
@@ -291,6 +332,81 @@ class Runtime {
   }
   DevicePool& pool() { return pool_; }
 
+  // ---- device queue ----
+  /// Sets (or, with nullptr, clears) the device task queue. Call between executions, not while
+  /// tasks run.
+  void set_device_queue(std::shared_ptr<DeviceQueue> q) {
+    ensure_device();
+    if (q && !exec_stream_) cuda_check(cudaStreamCreateWithFlags(&exec_stream_, cudaStreamNonBlocking), "stream");
+    if (!q && dq_) {
+      flush();
+      reclaim(true);
+    }
+    dq_ = std::move(q);
+  }
+  DeviceQueue* device_queue() { return dq_.get(); }
+
+  /// Device memory a buffer gives back: with a device queue, kept until the runs that may still
+  /// read it (everything recorded so far) have completed.
+  void release_device(void* p, size_t bytes) {
+    if (!p) return;
+    if (!dq_) {
+      pool_.release(p, bytes);
+      return;
+    }
+    std::lock_guard<std::mutex> lk(frees_m_);
+    pending_frees_.emplace_back(p, bytes);
+  }
+
+  /// Runs everything recorded so far (after the stage-in copies issued so far) on the queue's
+  /// stream; the host tasks waiting for device data run once it has completed. Returns the stream.
+  cudaStream_t flush() {
+    std::lock_guard<std::mutex> lk(flush_m_);
+    reclaim(false);
+    // Taken BEFORE the queue's snapshot of its operations: a buffer freed, or a host job deferred,
+    // before this point was read or produced by operations recorded before it, so by this run or
+    // an earlier one; anything later belongs to a later run.
+    std::vector<std::pair<void*, size_t>> frees;
+    std::vector<Job> later;
+    {
+      std::lock_guard<std::mutex> fl(frees_m_);
+      frees.swap(pending_frees_);
+    }
+    {
+      std::lock_guard<std::mutex> ql(m_);
+      later.swap(deferred_host_);
+    }
+    {
+      // no task is between its stage-in copies and the recording of its operations here, so every
+      // recorded operation's copies are before this event
+      std::unique_lock<std::shared_mutex> st(stage_m_);
+      cudaEvent_t staged;
+      cuda_check(cudaEventCreateWithFlags(&staged, cudaEventDisableTiming), "event");
+      cuda_check(cudaEventRecord(staged, copy_stream()), "event record");
+      cuda_check(cudaStreamWaitEvent(exec_stream_, staged, 0), "stream wait");
+      cuda_check(cudaEventDestroy(staged), "event destroy");
+      dq_->run(exec_stream_);
+    }
+    cudaEvent_t done;
+    cuda_check(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "event");
+    cuda_check(cudaEventRecord(done, exec_stream_), "event record");
+    {
+      std::lock_guard<std::mutex> fl(frees_m_);
+      inflight_frees_.emplace_back(done, std::move(frees));
+    }
+    for (auto& j : later) when_stream_done(exec_stream_, j.prio, std::move(j.fn));
+    return exec_stream_;
+  }
+  cudaStream_t exec_stream() { return exec_stream_; }
+  /// Held (shared) by a device task from its stage-in copies through the recording of its operations.
+  std::shared_mutex& stage_mutex() { return stage_m_; }
+
+  /// A counted host job that reads device data: runs after the next batch has completed.
+  void defer_host(int64_t prio, std::function<void()> fn) {
+    std::lock_guard<std::mutex> lk(m_);
+    deferred_host_.push_back(Job{prio, seq_++, std::move(fn)});
+  }
+
   /// Runs `fn` on a worker (priority `prio`) once all work queued so far on `s` has finished.
   void when_stream_done(cudaStream_t s, int64_t prio, std::function<void()> fn) {
     auto* payload = new std::pair<int64_t, std::function<void()>>(prio, std::move(fn));
@@ -323,6 +439,7 @@ class Runtime {
         if (stop_ && (q_.empty() || !executing_)) return;
         j = std::move(const_cast<Job&>(q_.top()));
         q_.pop();
+        ++busy_;
       }
       try {
         j.fn();
@@ -330,6 +447,38 @@ class Runtime {
         // task wrappers settle their own accounting; anything escaping here is recorded
         record_error(std::current_exception());
       }
+      bool flush_now = false;
+      {
+        std::lock_guard<std::mutex> lk(m_);
+        --busy_;
+        // every worker idle, nothing ready, host tasks waiting for device data: run the batch
+        flush_now = dq_ && busy_ == 0 && q_.empty() && !deferred_host_.empty();
+      }
+      if (flush_now) {
+        try {
+          flush();
+        } catch (...) {
+          record_error(std::current_exception());
+        }
+      }
+    }
+  }
+
+  // gives the memory of completed runs back to the pool (all runs when `wait`)
+  void reclaim(bool wait) {
+    std::lock_guard<std::mutex> lk(frees_m_);
+    size_t i = 0;
+    for (; i < inflight_frees_.size(); ++i) {
+      auto& f = inflight_frees_[i];
+      if (wait) cuda_check(cudaEventSynchronize(f.first), "event sync");
+      else if (cudaEventQuery(f.first) != cudaSuccess) break;
+      for (auto& p : f.second) pool_.release(p.first, p.second);
+      cudaEventDestroy(f.first);
+    }
+    inflight_frees_.erase(inflight_frees_.begin(), inflight_frees_.begin() + i);
+    if (wait) {
+      for (auto& p : pending_frees_) pool_.release(p.first, p.second);
+      pending_frees_.clear();
     }
   }
 
@@ -339,6 +488,8 @@ class Runtime {
   std::vector<std::thread> workers_;
   uint64_t seq_ = 0;
   int64_t active_ = 0;
+  int busy_ = 0;                    // workers running a job
+  std::vector<Job> deferred_host_;  // host jobs waiting for the next device-queue batch
   bool stop_ = false, executing_ = false;
   std::exception_ptr error_;
 
@@ -348,6 +499,13 @@ class Runtime {
   cudaStream_t copy_stream_ = nullptr;
   std::atomic<uint64_t> next_stream_{0};
   DevicePool pool_;
+
+  std::shared_ptr<DeviceQueue> dq_;
+  cudaStream_t exec_stream_ = nullptr;  // the device queue's runs and the copies that follow them
+  std::mutex flush_m_, frees_m_;
+  std::shared_mutex stage_m_;
+  std::vector<std::pair<void*, size_t>> pending_frees_;
+  std::vector<std::pair<cudaEvent_t, std::vector<std::pair<void*, size_t>>>> inflight_frees_;
 };
 
 }  // namespace rt

@@ -682,6 +682,19 @@ class TT : public TTBase {
   void sync_inputs_to_host(Pending& p, std::index_sequence<I...>) {
     (sync_one<I>(p), ...);
   }
+  template <size_t... I>
+  bool inputs_on_device(Pending& p, std::index_sequence<I...>) {
+    return (on_device_one<I>(p) || ... || false);
+  }
+  template <size_t I>
+  bool on_device_one(Pending& p) {
+    if constexpr (!std::is_void_v<value_t<I>>) {
+      using V = std::decay_t<value_t<I>>;
+      return detail::value_on_device(static_cast<detail::Holder<V>*>(p.h[I].get())->value);
+    } else {
+      return false;
+    }
+  }
   template <size_t I>
   void sync_one(Pending& p) {
     if constexpr (!std::is_void_v<value_t<I>>) {

@@ -99,11 +99,14 @@ def _driver(gbx):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("queue", [False, True], ids=["per-task-launch", "device-queue"])
 @pytest.mark.parametrize("N,NB", [(1000, 128), (2048, 512), (160, 32)])
-def test_gb300_potrf_flowgraph_matches_oracle(gbx, cuda, tmp_path, N, NB):
+def test_gb300_potrf_flowgraph_matches_oracle(gbx, cuda, tmp_path, N, NB, queue):
+    """The potrf flowgraph's device tasks, launched one by one or recorded into the device task queue
+    (one persistent launch per batch), give the oracle's factor."""
     drv = _driver(gbx)
     out = str(tmp_path / "L.bin")
-    rc, log = _run([drv, "-N", str(N), "-t", str(NB), "-o", out], timeout=600)
+    rc, log = _run([drv, "-N", str(N), "-t", str(NB), "-o", out] + (["-q"] if queue else []), timeout=600)
     assert rc == 0 and "Factorization is CORRECT" in log, log
     got = np.fromfile(out)
     ref = oracle.plgsy_tiles(N, NB, N, 3872)
@@ -121,14 +124,16 @@ def test_gb300_potrf_flowgraph_timed_iterations(gbx, cuda):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("N,NB,nrhs", [(1000, 128, 3), (2500, 512, 1), (160, 32, 16)])
-def test_gb300_potrs_flowgraph_matches_oracle(gbx, cuda, tmp_path, N, NB, nrhs):
+@pytest.mark.parametrize("N,NB,nrhs,queue", [(1000, 128, 3, False), (2500, 512, 1, False), (160, 32, 16, False),
+                                            (1000, 128, 3, True), (2500, 512, 2, True)])
+def test_gb300_potrs_flowgraph_matches_oracle(gbx, cuda, tmp_path, N, NB, nrhs, queue):
     """The solve as a TTG flowgraph (forward and backward TRSM/GEMM device tasks over right-hand-side
     tiles, ttg_gb300/potrf/potrs.h) after the factorisation flowgraph: the driver's backward-error
     check passes and X equals the oracle's solve with the same factor."""
     drv = _driver(gbx)
     lf, xf = str(tmp_path / "L.bin"), str(tmp_path / "X.bin")
-    rc, log = _run([drv, "-N", str(N), "-t", str(NB), "-s", str(nrhs), "-o", lf, "-p", xf], timeout=600)
+    rc, log = _run([drv, "-N", str(N), "-t", str(NB), "-s", str(nrhs), "-o", lf, "-p", xf] + (["-q"] if queue else []),
+                   timeout=600)
     assert rc == 0 and "Factorization is CORRECT" in log and "Solve is CORRECT" in log, log
     L = np.fromfile(lf)
     X = np.fromfile(xf).reshape(nrhs, N)
@@ -137,3 +142,15 @@ def test_gb300_potrs_flowgraph_matches_oracle(gbx, cuda, tmp_path, N, NB, nrhs):
     B = ((7919 * i + 104729 * r) % 1000) / 500.0 - 1.0  # the driver's right-hand sides, N x nrhs
     Xref = oracle.potrs_tiled(L, N, NB, B)
     assert np.max(np.abs(X.T - Xref)) <= 1e-12 * np.max(np.abs(Xref))
+
+
+@pytest.mark.gpu
+def test_chain_of_device_tasks_through_the_device_queue(gbx, cuda):
+    """A chain of device tasks (keys only, and one device buffer travelling the chain) completes with
+    the device task queue: each task's sends run right after its recording, and the runtime's idle
+    and fence triggers run what was recorded."""
+    from ttg_gb300 import build as gb
+    chain = gb.build_chain()
+    for flows in ("0", "1"):
+        rc, log = _run([chain, "-f", flows, "-n", "2000", "-q"], timeout=300)
+        assert rc == 0 and "avg" in log, log

@@ -51,6 +51,12 @@ SIGNATURES = {
     "gbx_dgemm_nt_tile": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp]),
     "gbx_dtrsm_rln_tile": (_i, [_i, _i, _vp, _i, _vp, _i, _vp]),
     "gbx_dgemm_nn_tile": (_i, [_i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp]),
+    "gbx_taskq_create": (_i, [ctypes.POINTER(_vp)]),
+    "gbx_taskq_destroy": (_i, [_vp]),
+    "gbx_taskq_stream": (_vp, [_vp]),
+    "gbx_taskq_pending": (ctypes.c_longlong, [_vp]),
+    "gbx_taskq_run": (_i, [_vp, _vp]),
+    "gbx_taskq_status": (_i, [_vp, _vp]),
     "gbx_dpotrf_tiled_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dpotrf_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
     "gbx_dpotrf_tiled_status": (_i, [_vp, _vp]),

@@ -89,11 +89,14 @@ CHAIN = os.path.join(HERE, "potrf", "chain_dev")
 
 def build_chain(force=False):
     """The device-task chain benchmark on the TTG API (per-task runtime overhead)."""
-    deps = [CHAIN_SRC] + glob.glob(os.path.join(INCLUDE, "ttg", "*.h")) + glob.glob(os.path.join(INCLUDE, "ttg", "*", "*.h"))
+    lib = build()
+    deps = [CHAIN_SRC, lib] + glob.glob(os.path.join(INCLUDE, "ttg", "*.h")) + \
+        glob.glob(os.path.join(INCLUDE, "ttg", "*", "*.h"))
     if force or _stale(CHAIN, deps):
         cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))) if os.path.isabs(nvcc()) else "/usr/local/cuda"
         cmd = ["g++", "-std=c++20", "-O2", "-pthread", "-I", INCLUDE, "-I", os.path.join(cuda, "include"), CHAIN_SRC,
-               "-o", CHAIN, "-L", os.path.join(cuda, "lib64"), "-lcudart"]
+               "-o", CHAIN, "-L", HERE, "-lgbx_potrf", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+               "-Wl,-rpath," + HERE]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("chain benchmark build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

@@ -17,6 +17,7 @@
 #include "block_ops.cuh"
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
+#include "taskq.h"
 
 namespace gbx {
 
@@ -645,6 +646,8 @@ int gbx_dpotrf_tile_bufferSize(int n, int lda, size_t* bytes) {
 
 int gbx_dpotrf_tile(int n, double* A, int lda, void* work, size_t work_bytes, int* devInfo, void* stream) {
   if (n < 0 || lda < std::max(1, n) || (n > 0 && A == nullptr) || devInfo == nullptr) return GBX_ERR_ARG;
+  if (auto* q = taskq::recorder(stream))  // a device task queue's stream: record, do not launch
+    return taskq::record(q, taskq::Op{taskq::OP_POTRF, n, n, 0, nullptr, nullptr, A, 0, 0, lda, 0, devInfo});
   cudaStream_t s = (cudaStream_t)stream;
   if (n == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
   const BlockView V = plain_view(n, A, lda);
@@ -658,6 +661,8 @@ int gbx_dtrsm_rlt_tile(int m, int n, const double* L, int ldl, double* B, int ld
   if (m < 0 || n < 0 || ldl < std::max(1, n) || ldb < std::max(1, m)) return GBX_ERR_ARG;
   if (m == 0 || n == 0) return GBX_OK;
   if (!L || !B) return GBX_ERR_ARG;
+  if (auto* q = taskq::recorder(stream))
+    return taskq::record(q, taskq::Op{taskq::OP_TRSM_RLT, m, n, 0, L, nullptr, B, ldl, 0, ldb, 0, nullptr});
   DevInfo di;
   if (int e = device_info(di)) return e;
   const size_t smem = op_trsm_smem_elems<double>() * sizeof(double);
@@ -669,6 +674,8 @@ int gbx_dsyrk_ln_tile(int n, int k, const double* A, int lda, double* C, int ldc
   if (n < 0 || k < 0 || lda < std::max(1, n) || ldc < std::max(1, n)) return GBX_ERR_ARG;
   if (n == 0 || k == 0) return GBX_OK;
   if (!A || !C) return GBX_ERR_ARG;
+  if (auto* q = taskq::recorder(stream))
+    return taskq::record(q, taskq::Op{taskq::OP_SYRK_LN, n, n, k, A, nullptr, C, lda, 0, ldc, 0, nullptr});
   DevInfo di;
   if (int e = device_info(di)) return e;
   const int nb = (n + kBlk - 1) / kBlk;
@@ -684,6 +691,8 @@ int gbx_dgemm_nt_tile(int m, int n, int k, const double* A, int lda, const doubl
     return GBX_ERR_ARG;
   if (m == 0 || n == 0 || k == 0) return GBX_OK;
   if (!A || !B || !C) return GBX_ERR_ARG;
+  if (auto* q = taskq::recorder(stream))
+    return taskq::record(q, taskq::Op{taskq::OP_GEMM_NT, m, n, k, A, B, C, lda, ldb, ldc, 0, nullptr});
   DevInfo di;
   if (int e = device_info(di)) return e;
   const size_t smem = 4 * kKC * kBlk * sizeof(double);

@@ -9,6 +9,7 @@
 
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
+#include "taskq.h"
 
 namespace gbx {
 namespace solve {
@@ -39,8 +40,8 @@ __global__ void __launch_bounds__(32 * kRowsPerCta) trsm_rln_kernel(int m, int n
   for (int c = lane; c < n; c += 32) B[r + (long long)c * ldb] = x[c];
 }
 
-// C(m x n) -= A(m x k) B(k x n): one thread per element of C, k staged through shared memory in
-// chunks of 32 columns of A and rows of B
+// C(m x n) -= A(m x k) B(k x n): one thread per element of C in 16 x 16 blocks, k staged through
+// shared memory in chunks of 16 columns of A and rows of B
 constexpr int kTile = 16;
 __global__ void __launch_bounds__(kTile * kTile) gemm_nn_kernel(int m, int n, int k, const double* __restrict__ A, int lda,
                                                                 const double* __restrict__ B, int ldb, double* C, int ldc) {
@@ -68,6 +69,10 @@ extern "C" int gbx_dtrsm_rln_tile(int m, int n, const double* L, int ldl, double
   if (m < 0 || n < 0 || ldl < (n > 1 ? n : 1) || ldb < (m > 1 ? m : 1)) return GBX_ERR_ARG;
   if (m == 0 || n == 0) return GBX_OK;
   if (!L || !B) return GBX_ERR_ARG;
+  if (auto* q = gbx::taskq::recorder(stream)) {  // a device task queue's stream: record, do not launch
+    if (n > 2048) return GBX_ERR_ARG;
+    return gbx::taskq::record(q, gbx::taskq::Op{gbx::taskq::OP_TRSM_RLN, m, n, 0, L, nullptr, B, ldl, 0, ldb, 0, nullptr});
+  }
   const size_t smem = (size_t)gbx::solve::kRowsPerCta * n * sizeof(double);
   if (smem > 48 * 1024) {
     if (smem > 200 * 1024) return GBX_ERR_ARG;  // n <= 3200
@@ -86,6 +91,8 @@ extern "C" int gbx_dgemm_nn_tile(int m, int n, int k, const double* A, int lda, 
     return GBX_ERR_ARG;
   if (m == 0 || n == 0 || k == 0) return GBX_OK;
   if (!A || !B || !C) return GBX_ERR_ARG;
+  if (auto* q = gbx::taskq::recorder(stream))
+    return gbx::taskq::record(q, gbx::taskq::Op{gbx::taskq::OP_GEMM_NN, m, n, k, A, B, C, lda, ldb, ldc, 0, nullptr});
   using gbx::solve::kTile;
   dim3 grid((m + kTile - 1) / kTile, (n + kTile - 1) / kTile);
   gbx::solve::gemm_nn_kernel<<<grid, kTile * kTile, 0, (cudaStream_t)stream>>>(m, n, k, A, lda, B, ldb, C, ldc);

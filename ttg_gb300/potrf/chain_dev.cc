@@ -3,8 +3,10 @@
 // examples/task-benchmarks/chain-ttg-dev.cc:191-192). Flows:
 //   0  the chain is carried by keys only (no data; the task selects nothing)
 //   1  one value with a one-int device buffer travels the chain (selected by every task)
-// Usage: chain_dev [-f FLOWS] [-n TASKS]. Prints the time per task in microseconds.
+// Usage: chain_dev [-f FLOWS] [-n TASKS] [-q]. Prints the time per task in microseconds. -q runs the
+// device tasks through the device task queue (ttg/device/gbx_queue.h).
 #include <ttg.h>
+#include <ttg/device/gbx_queue.h>
 
 #include <chrono>
 #include <cstdio>
@@ -66,11 +68,15 @@ static double run_value() {
 
 int main(int argc, char** argv) {
   int flows = 0;
-  for (int i = 1; i + 1 < argc; ++i) {
+  bool queue = false;
+  for (int i = 1; i < argc; ++i) {
+    if (std::string(argv[i]) == "-q") queue = true;
+    if (i + 1 >= argc) continue;
     if (std::string(argv[i]) == "-f") flows = std::atoi(argv[i + 1]);
     if (std::string(argv[i]) == "-n") g_tasks = std::atoi(argv[i + 1]);
   }
   ttg::initialize(argc, argv, -1);
+  if (queue) ttg::device::use_gbx_queue();
   const double us = flows == 0 ? run_keys() : run_value();
   std::printf("# of tasks = %d\n", g_tasks + 1);
   std::printf("time elapsed (microseconds) = %g, avg %g\n", us, us / (g_tasks + 1));

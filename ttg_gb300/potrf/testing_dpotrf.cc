@@ -4,12 +4,15 @@
 // storage) after the checked run; -s NRHS then solves A X = B through the solve flowgraph
 // (potrs.h) for NRHS right-hand sides B(i, r) = ((7919 i + 104729 r) mod 1000) / 500 - 1, checks
 // the normwise backward error and, with -p FILE, writes X (NRHS rows of N, row r = column r of X).
+// -q runs the device tasks through the device task queue (ttg/device/gbx_queue.h): their tile
+// kernels are recorded and each batch runs as one persistent launch.
 //
 // Each iteration generates the PLASMA test matrix (seed 3872, bump N) with one device task per
 // tile, factorises it through the flowgraph and writes the factor back to the host matrix, all
 // inside the timed region as the reference does. The check uses the reference's criterion
 // ||L L^T - A||_inf / (||A||_inf N eps) < 60 (testing_dpotrf.cc:277-335).
 #include <ttg.h>
+#include <ttg/device/gbx_queue.h>
 
 #include <chrono>
 #include <cmath>
@@ -165,6 +168,7 @@ int main(int argc, char** argv) {
   const bool check = !has(argv + 1, argv + argc, "-x");
   const bool defer = !has(argv + 1, argv + argc, "-w");
   ttg::initialize(argc, argv, nthreads);
+  if (has(argv + 1, argv + argc, "-q")) ttg::device::use_gbx_queue();
   std::printf("Creating 2D block cyclic matrix with NB %d N %d M %d P 1 Q 1\n", NB, N, N);
   std::vector<double> store(TiledMatrix<double>::num_elements(N, NB), 0.0);
   TiledMatrix<double> A(store.data(), N, NB);
