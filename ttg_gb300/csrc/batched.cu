@@ -172,6 +172,7 @@ using namespace gbx::batched;
 
 extern "C" int gbx_dgen_uniform_sym_batched(int batch, const int* n, const long long* offA, unsigned long long seed,
                                             double* A, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (batch < 0 || (batch > 0 && (!n || !offA || !A))) return GBX_ERR_ARG;
   if (batch == 0) return GBX_OK;
   gen_batch_kernel<<<std::min(batch, 4096), 256, 0, (cudaStream_t)stream>>>(batch, n, offA, seed, A);
@@ -190,6 +191,7 @@ extern "C" int gbx_batched_order(int batch, const int* n_host, int* order_host) 
 extern "C" int gbx_dposv_batched(int batch, const int* n, const long long* offA, const long long* offB,
                                  const int* order, double* A, double* B, int nrhs, int mode, int refine, float* L32,
                                  int* info, void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   return gbx_dposv_batched_ex(batch, n, offA, offB, order, A, B, nrhs, mode, refine, L32, info, 0, work, work_bytes,
                               stream);
 }
@@ -197,6 +199,7 @@ extern "C" int gbx_dposv_batched(int batch, const int* n, const long long* offA,
 extern "C" int gbx_dposv_batched_ex(int batch, const int* n, const long long* offA, const long long* offB,
                                     const int* order, double* A, double* B, int nrhs, int mode, int refine, float* L32,
                                     int* info, int ctas, void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (batch < 0 || nrhs < 1 || (mode != 0 && mode != 1) || refine < 0 || ctas < 0) return GBX_ERR_ARG;
   if (batch == 0) return GBX_OK;
   if (!n || !offA || !offB || !order || !A || !B || !info || (mode == 1 && !L32)) return GBX_ERR_ARG;

@@ -7,6 +7,14 @@
 
 namespace gbx {
 
+namespace taskq {
+struct Queue;
+Queue* recorder(const void* stream);  // taskq.cu: the device task queue a stream handle records into
+}
+/// True for the recording stream handle of a device task queue: entry points that cannot record
+/// reject it (it is not a CUDA stream).
+inline bool recording_stream(const void* stream) { return taskq::recorder(stream) != nullptr; }
+
 // ---- memory-model helpers -------------------------------------------------------------------
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
   int v;

@@ -182,6 +182,7 @@ using namespace gbx::tc;
 
 extern "C" int gbx_gemm_bf16_nt_f32(int M, int N, int K, const void* A, int lda, const void* B, int ldb, float* D,
                                     int ldd, int* status, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (M < 0 || N < 0 || K < 0 || lda < K || ldb < K || ldd < M || (lda % 8) || (ldb % 8)) return GBX_ERR_ARG;
   if (M == 0 || N == 0) return GBX_OK;
   if (!A || !B || !D) return GBX_ERR_ARG;

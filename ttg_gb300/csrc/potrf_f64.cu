@@ -17,6 +17,7 @@
 #include "block_ops.cuh"
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
+#include "plgsy.cuh"
 #include "taskq.h"
 
 namespace gbx {
@@ -367,24 +368,6 @@ __global__ void __launch_bounds__(kThreads) solve_sweep_kernel(BlockView V, int 
 }
 
 // ---- device generators ----------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long lcg_jump_dev(unsigned long long n, unsigned long long seed) {
-  unsigned long long a = 6364136223846793005ULL, c = 1ULL, x = seed;
-  while (n) {
-    if (n & 1ULL) x = a * x + c;
-    c *= (a + 1);
-    a *= a;
-    n >>= 1;
-  }
-  return x;
-}
-
-__device__ __forceinline__ double plgsy_entry(unsigned long long ran) {
-  // `0.5f - ran * RndF_Mul` evaluated in float, as the reference generator does
-  const float r = __ull2float_rn(ran);
-  const float p = __fmul_rn(r, 5.4210108624275222e-20f);
-  return (double)__fsub_rn(0.5f, p);
-}
-
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   z += 0x9e3779b97f4a7c15ULL;
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
@@ -647,7 +630,7 @@ int gbx_dpotrf_tile_bufferSize(int n, int lda, size_t* bytes) {
 int gbx_dpotrf_tile(int n, double* A, int lda, void* work, size_t work_bytes, int* devInfo, void* stream) {
   if (n < 0 || lda < std::max(1, n) || (n > 0 && A == nullptr) || devInfo == nullptr) return GBX_ERR_ARG;
   if (auto* q = taskq::recorder(stream))  // a device task queue's stream: record, do not launch
-    return taskq::record(q, taskq::Op{taskq::OP_POTRF, n, n, 0, nullptr, nullptr, A, 0, 0, lda, 0, devInfo});
+    return taskq::record(q, taskq::make_op(taskq::OP_POTRF, n, n, 0, nullptr, nullptr, A, 0, 0, lda, devInfo));
   cudaStream_t s = (cudaStream_t)stream;
   if (n == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
   const BlockView V = plain_view(n, A, lda);
@@ -662,7 +645,7 @@ int gbx_dtrsm_rlt_tile(int m, int n, const double* L, int ldl, double* B, int ld
   if (m == 0 || n == 0) return GBX_OK;
   if (!L || !B) return GBX_ERR_ARG;
   if (auto* q = taskq::recorder(stream))
-    return taskq::record(q, taskq::Op{taskq::OP_TRSM_RLT, m, n, 0, L, nullptr, B, ldl, 0, ldb, 0, nullptr});
+    return taskq::record(q, taskq::make_op(taskq::OP_TRSM_RLT, m, n, 0, L, nullptr, B, ldl, 0, ldb));
   DevInfo di;
   if (int e = device_info(di)) return e;
   const size_t smem = op_trsm_smem_elems<double>() * sizeof(double);
@@ -675,7 +658,7 @@ int gbx_dsyrk_ln_tile(int n, int k, const double* A, int lda, double* C, int ldc
   if (n == 0 || k == 0) return GBX_OK;
   if (!A || !C) return GBX_ERR_ARG;
   if (auto* q = taskq::recorder(stream))
-    return taskq::record(q, taskq::Op{taskq::OP_SYRK_LN, n, n, k, A, nullptr, C, lda, 0, ldc, 0, nullptr});
+    return taskq::record(q, taskq::make_op(taskq::OP_SYRK_LN, n, n, k, A, nullptr, C, lda, 0, ldc));
   DevInfo di;
   if (int e = device_info(di)) return e;
   const int nb = (n + kBlk - 1) / kBlk;
@@ -692,7 +675,7 @@ int gbx_dgemm_nt_tile(int m, int n, int k, const double* A, int lda, const doubl
   if (m == 0 || n == 0 || k == 0) return GBX_OK;
   if (!A || !B || !C) return GBX_ERR_ARG;
   if (auto* q = taskq::recorder(stream))
-    return taskq::record(q, taskq::Op{taskq::OP_GEMM_NT, m, n, k, A, B, C, lda, ldb, ldc, 0, nullptr});
+    return taskq::record(q, taskq::make_op(taskq::OP_GEMM_NT, m, n, k, A, B, C, lda, ldb, ldc));
   DevInfo di;
   if (int e = device_info(di)) return e;
   const size_t smem = 4 * kKC * kBlk * sizeof(double);
@@ -711,6 +694,7 @@ int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes) {
 }
 
 int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N < 0 || NB <= 0 || block_edge(NB) == 0) return GBX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   if (N == 0) {
@@ -724,6 +708,7 @@ int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes
 }
 
 int gbx_dpotrf_tiled_status(const void* work, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (!work) return GBX_ERR_ARG;
   int st = 0;
   cudaStream_t s = (cudaStream_t)stream;
@@ -733,6 +718,7 @@ int gbx_dpotrf_tiled_status(const void* work, void* stream) {
 }
 
 int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, int ldb, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N < 0 || NB <= 0 || block_edge(NB) == 0 || nrhs < 0 || ldb < std::max(1, N)) return GBX_ERR_ARG;
   if (N == 0 || nrhs == 0) return GBX_OK;
   if (!tiles || !B) return GBX_ERR_ARG;
@@ -823,6 +809,7 @@ int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes) {
 
 int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, int nrhs, const double* B_host,
                          double* X_host, double* tiles, double* X, void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   size_t need = 0;
   if (int e = gbx_dposv_tiled_host_bufferSize(N, NB, &need)) return e;
   if (nrhs < 0 || !A_host || !L_host || !tiles || (nrhs > 0 && (!B_host || !X_host || !X))) return GBX_ERR_ARG;
@@ -890,6 +877,7 @@ int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, in
 }
 
 static int gen_tiles(int N, int NB, int kind, double v, unsigned long long seed, double* tiles, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N < 0 || NB <= 0) return GBX_ERR_ARG;
   if (N == 0) return GBX_OK;
   if (!tiles) return GBX_ERR_ARG;
@@ -902,10 +890,12 @@ static int gen_tiles(int N, int NB, int kind, double v, unsigned long long seed,
 }
 
 int gbx_dplgsy_tiled(int N, int NB, double bump, unsigned long long seed, double* tiles, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   return gen_tiles(N, NB, 0, bump, seed, tiles, stream);
 }
 
 int gbx_dgen_uniform_sym_tiled(int N, int NB, unsigned long long seed, double shift, double* tiles, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   return gen_tiles(N, NB, 1, shift, seed, tiles, stream);
 }
 
@@ -914,6 +904,15 @@ int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m
   if (m < 0 || n < 0 || lda < std::max(1, m) || m0 < 0 || n0 < 0 || gM < 0) return GBX_ERR_ARG;
   if (m == 0 || n == 0) return GBX_OK;
   if (!A) return GBX_ERR_ARG;
+  if (auto* q = taskq::recorder(stream)) {  // a device task queue's stream: record, do not launch
+    taskq::Op o = taskq::make_op(taskq::OP_PLGSY, m, n, 0, nullptr, nullptr, A, 0, 0, lda);
+    o.gM = gM;
+    o.g0 = m0;
+    o.g1 = n0;
+    o.bump = bump;
+    o.seed = seed;
+    return taskq::record(q, o);
+  }
   const long long total = (long long)m * n;
   plgsy_tile_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(bump, m, n, A, lda, gM, m0, n0,
                                                                                        seed);
@@ -922,6 +921,7 @@ int gbx_dplgsy_tile(double bump, int m, int n, double* A, int lda, int gM, int m
 
 int gbx_dgen_lowrank_sym_tiled(int N, int NB, const double* lam, const double* U, const double* V, const double* G,
                                int r, double* tiles, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N <= 0 || NB <= 0 || r < 0 || r > 8 || !lam || (r > 0 && (!U || !V || !G)) || !tiles) return GBX_ERR_ARG;
   const int NT = (N + NB - 1) / NB;
   if (NT > 65535) return GBX_ERR_ARG;
@@ -968,6 +968,7 @@ int noalloc_scratch(void** out) {
 extern "C" {
 
 int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N < 0 || NB <= 0 || block_edge(NB) == 0 || !devInfo || (N > 0 && !tiles)) return GBX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   if (N == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
@@ -984,6 +985,7 @@ int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* s
 
 int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_bytes, uint64_t timeout_ns,
                              void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (NB <= 0 || NB > kBlk || !tiles) return GBX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const BlockView V = tiled_view(2 * NB, NB, tiles);

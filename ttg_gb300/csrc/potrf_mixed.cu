@@ -1179,6 +1179,7 @@ extern "C" int gbx_potrf_mixed_bufferSize(int N, int NB, size_t* bytes) {
 
 extern "C" int gbx_potrf_mixed(int N, int NB, const double* A, float* W, int prec, double shift, double fp64_diag_cond,
                                void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N <= 0) return GBX_ERR_ARG;
   return gbx_potrf_mixed_batched(1, &N, NB, A, W, prec, shift, fp64_diag_cond, nullptr, work, work_bytes, stream);
 }
@@ -1194,6 +1195,7 @@ extern "C" int gbx_potrf_mixed_batched_bufferSize(int batch, const int* n, int N
 extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const double* A, float* W, int prec,
                                        double shift, double fp64_diag_cond, const unsigned char* sel, void* work,
                                        size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   size_t need = 0;
   if (int e = gbx_potrf_mixed_batched_bufferSize(batch, n, NB, &need)) return e;
   if (!A || !W || !work || prec < 0 || prec > 2 || !(fp64_diag_cond >= 0.0)) return GBX_ERR_ARG;
@@ -1215,6 +1217,7 @@ extern "C" int gbx_potrf_mixed_batched(int batch, const int* n, int NB, const do
 
 extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const int* n, int NB, int* info,
                                             float* cond_est, int* fp64_tiles, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (!work || batch <= 0 || !n || NB <= 0) return GBX_ERR_ARG;
   const Ws w = layout_batch(batch, n, NB);
   cudaStream_t s = (cudaStream_t)stream;
@@ -1234,6 +1237,7 @@ extern "C" int gbx_potrf_mixed_batched_info(const void* work, int batch, const i
 }
 
 extern "C" int gbx_potrf_mixed_info(const void* work, int N, int NB, float* cond_est, int* fp64_tiles, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (!work || N <= 0 || NB <= 0) return GBX_ERR_ARG;
   const Ws w = layout(N, NB);
   int st = 0, nf = 0;

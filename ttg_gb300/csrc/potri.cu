@@ -262,6 +262,7 @@ extern "C" int gbx_dpotri_tiled_bufferSize(int N, int NB, size_t* bytes) {
 }
 
 extern "C" int gbx_dpotri_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   size_t need = 0;
   if (int e = gbx_dpotri_tiled_bufferSize(N, NB, &need)) return e;
   if (!tiles) return GBX_ERR_ARG;

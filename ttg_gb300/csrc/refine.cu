@@ -1095,6 +1095,7 @@ int set_attrs() {
 }  // namespace
 
 extern "C" int gbx_spotri_diag(int N, int NB, const float* W, float* Inv, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N <= 0 || NB <= 0 || NB > 1024 || !W || !Inv) return GBX_ERR_ARG;
   if (int e = set_attrs()) return e;
   const int NT = (N + NB - 1) / NB;
@@ -1106,6 +1107,7 @@ extern "C" int gbx_spotri_diag(int N, int NB, const float* W, float* Inv, void* 
 
 extern "C" int gbx_sprecond(int N, int NB, const float* W, const float* Inv, int nrhs, const double* R, double* Z,
                             float* tmp, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N <= 0 || NB <= 0 || NB > 1024 || nrhs <= 0 || nrhs > kMaxRhs || !W || !Inv || !R || !Z || !tmp)
     return GBX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1140,6 +1142,7 @@ extern "C" int gbx_sprecond(int N, int NB, const float* W, const float* Inv, int
 
 extern "C" int gbx_dsymm_tiled(int N, int NB, const double* A, int nrhs, double alpha, const double* X, double beta,
                                double* Y, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N <= 0 || NB <= 0 || nrhs <= 0 || nrhs > kMaxRhs || !A || !X || !Y) return GBX_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   if (int e = set_attrs()) return e;
@@ -1761,6 +1764,7 @@ int make_run(Run& r, int batch, const int* n, int NB, int nrhs, int prec, double
 }  // namespace
 
 extern "C" int gbx_split_f64(const double* a, float* hi, float* lo, long long n, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (n < 0 || (n > 0 && (!a || !hi || !lo))) return GBX_ERR_ARG;
   if (n == 0) return GBX_OK;
   split_f64_kernel<<<(unsigned)std::min<long long>(4096, (n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, hi, lo, n);
@@ -1775,6 +1779,7 @@ extern "C" int gbx_dposv_mixed_batched_bufferSize(int batch, const int* n, int N
 
 extern "C" int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int nrhs, int prec, int sched, void* work,
                                             size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (check_args(batch, n, NB, nrhs, prec) || !work || sched < 0 || sched > 1) return GBX_ERR_ARG;
   const BLayout L = blayout(batch, n, NB, nrhs);
   if (work_bytes < L.total) return GBX_ERR_WORKSPACE;
@@ -1844,6 +1849,7 @@ extern "C" int gbx_dposv_mixed_batched_plan(int batch, const int* n, int NB, int
 extern "C" int gbx_dposv_mixed_batched_exec(int batch, const int* n, int NB, const double* A, int nrhs,
                                             const double* B, double* X, int prec, double fp64_diag_cond, double tol,
                                             int maxiter, float* W, void* work, size_t work_bytes, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (check_args(batch, n, NB, nrhs, prec) || !A || !B || !X || !W || !work || maxiter < 0 || !(tol > 0.0) ||
       !(fp64_diag_cond >= 0.0))
     return GBX_ERR_ARG;
@@ -1890,6 +1896,7 @@ extern "C" int gbx_dposv_mixed_batched_exec(int batch, const int* n, int NB, con
 
 extern "C" int gbx_dposv_mixed_batched_result(int batch, const int* n, int NB, int nrhs, double tol, const void* work,
                                               gbx_refine_info* info, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (check_args(batch, n, NB, nrhs, 0) || !work) return GBX_ERR_ARG;
   const BLayout L = blayout(batch, n, NB, nrhs);
   cudaStream_t s = (cudaStream_t)stream;
@@ -1931,6 +1938,7 @@ extern "C" int gbx_dposv_mixed_batched_result(int batch, const int* n, int NB, i
 extern "C" int gbx_dposv_mixed_batched(int batch, const int* n, int NB, const double* A, int nrhs, const double* B,
                                        double* X, int prec, double fp64_diag_cond, double tol, int maxiter, float* W,
                                        void* work, size_t work_bytes, gbx_refine_info* info, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (int e = gbx_dposv_mixed_batched_plan(batch, n, NB, nrhs, prec, 0, work, work_bytes, stream)) return e;
   if (int e = gbx_dposv_mixed_batched_exec(batch, n, NB, A, nrhs, B, X, prec, fp64_diag_cond, tol, maxiter, W, work,
                                            work_bytes, stream))
@@ -1947,6 +1955,7 @@ extern "C" int gbx_dposv_mixed_bufferSize(int N, int NB, int nrhs, size_t* bytes
 extern "C" int gbx_dposv_mixed(int N, int NB, const double* A, int nrhs, const double* B, double* X, int prec,
                                double fp64_diag_cond, double tol, int maxiter, float* W, void* work, size_t work_bytes,
                                gbx_refine_info* info, void* stream) {
+  if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
   if (N <= 0) return GBX_ERR_ARG;
   return gbx_dposv_mixed_batched(1, &N, NB, A, nrhs, B, X, prec, fp64_diag_cond, tol, maxiter, W, work, work_bytes,
                                  info, stream);

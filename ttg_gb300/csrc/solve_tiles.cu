@@ -71,7 +71,7 @@ extern "C" int gbx_dtrsm_rln_tile(int m, int n, const double* L, int ldl, double
   if (!L || !B) return GBX_ERR_ARG;
   if (auto* q = gbx::taskq::recorder(stream)) {  // a device task queue's stream: record, do not launch
     if (n > 2048) return GBX_ERR_ARG;
-    return gbx::taskq::record(q, gbx::taskq::Op{gbx::taskq::OP_TRSM_RLN, m, n, 0, L, nullptr, B, ldl, 0, ldb, 0, nullptr});
+    return gbx::taskq::record(q, gbx::taskq::make_op(gbx::taskq::OP_TRSM_RLN, m, n, 0, L, nullptr, B, ldl, 0, ldb));
   }
   const size_t smem = (size_t)gbx::solve::kRowsPerCta * n * sizeof(double);
   if (smem > 48 * 1024) {
@@ -92,7 +92,7 @@ extern "C" int gbx_dgemm_nn_tile(int m, int n, int k, const double* A, int lda, 
   if (m == 0 || n == 0 || k == 0) return GBX_OK;
   if (!A || !B || !C) return GBX_ERR_ARG;
   if (auto* q = gbx::taskq::recorder(stream))
-    return gbx::taskq::record(q, gbx::taskq::Op{gbx::taskq::OP_GEMM_NN, m, n, k, A, B, C, lda, ldb, ldc, 0, nullptr});
+    return gbx::taskq::record(q, gbx::taskq::make_op(gbx::taskq::OP_GEMM_NN, m, n, k, A, B, C, lda, ldb, ldc));
   using gbx::solve::kTile;
   dim3 grid((m + kTile - 1) / kTile, (n + kTile - 1) / kTile);
   gbx::solve::gemm_nn_kernel<<<grid, kTile * kTile, 0, (cudaStream_t)stream>>>(m, n, k, A, lda, B, ldb, C, ldc);

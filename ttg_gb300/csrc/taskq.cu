@@ -22,6 +22,7 @@
 #include "block_ops.cuh"
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
+#include "plgsy.cuh"
 #include "taskq.h"
 
 namespace gbx {
@@ -66,7 +67,7 @@ int nsub_of(const Op& o) {
     case OP_SYRK_LN: return nb(o.n) * (nb(o.n) + 1) / 2;
     case OP_GEMM_NT: return nb(o.m) * nb(o.n);
     case OP_TRSM_RLN: return (o.m + kRlnRows - 1) / kRlnRows;
-    default: return nb(o.n);  // OP_GEMM_NN: column blocks of C
+    default: return nb(o.n);  // OP_GEMM_NN, OP_PLGSY: column blocks of C
   }
 }
 
@@ -148,6 +149,20 @@ __device__ void gemm_nn_cols(const Op& o, int c0) {
   __syncthreads();
 }
 
+// columns [c0, c0 + 128) of a tile of the PLASMA test matrix (gbx_dplgsy_tile's entries)
+__device__ void plgsy_cols(const Op& o, int c0) {
+  const int nc = min(kBlk, o.n - c0);
+  for (int idx = threadIdx.x; idx < o.m * nc; idx += kThreads) {
+    const int i = idx % o.m, j = c0 + idx / o.m;
+    const long long gi = (long long)o.g0 + i, gj = (long long)o.g1 + j;
+    const long long hi = gi >= gj ? gi : gj, lo = gi >= gj ? gj : gi;
+    double v = plgsy_entry(lcg_jump_dev((unsigned long long)hi + (unsigned long long)lo * (unsigned long long)o.gM, o.seed));
+    if (gi == gj) v = __dadd_rn(v, o.bump);
+    o.C[i + (long long)j * o.ldc] = v;
+  }
+  __syncthreads();
+}
+
 // Cholesky of the whole tile on one CTA: right-looking over 128-block panels
 __device__ void potrf_tile(const Op& o, double* sm) {
   const int n = o.n, nb = (n + kBlk - 1) / kBlk;
@@ -209,6 +224,9 @@ __device__ void run_sub(const Op& o, int s, double* sm) {
     }
     case OP_TRSM_RLN:
       rln_rows(o, s * kRlnRows, sm);
+      return;
+    case OP_PLGSY:
+      plgsy_cols(o, s * kBlk);
       return;
     default:
       gemm_nn_cols(o, s * kBlk);
