@@ -799,12 +799,21 @@ def run_ttg_flowgraph(gbx, dev, N=16384, NB=512, iters=2, chain_tasks=20000):
     out = {"config": {"workload": "potrf FP64 N=%d NB=%d through the TTG flowgraph (device tasks), PLASMA "
                                   "generator seed 3872" % (N, NB), "N": N, "NB": NB}}
     drv = gb.build_driver()
-    r = subprocess.run([drv, "-N", str(N), "-t", str(NB), "-n", str(iters), "-x"], capture_output=True, text=True,
-                       timeout=1200)
-    gfs = [float(x) for x in re.findall(r"([0-9.eE+-]+) GF/s", r.stdout)]
-    ms = [float(x) for x in re.findall(r"Execution Time \(milliseconds\) : ([0-9.eE+-]+)", r.stdout)]
-    out["flowgraph"] = {"rc": r.returncode, "gflops_per_iter": gfs, "ms_per_iter": ms,
-                        "tflops": max(gfs) / 1e3 if gfs else None}
+
+    def flowgraph(n, extra):
+        r = subprocess.run([drv, "-N", str(n), "-t", str(NB), "-n", str(iters), "-x"] + extra, capture_output=True,
+                           text=True, timeout=1200)
+        g = [float(x) for x in re.findall(r"([0-9.eE+-]+) GF/s", r.stdout)]
+        t = [float(x) for x in re.findall(r"Execution Time \(milliseconds\) : ([0-9.eE+-]+)", r.stdout)]
+        return {"rc": r.returncode, "N": n, "gflops_per_iter": g, "ms_per_iter": t, "tflops": max(g) / 1e3 if g else None}
+
+    # one launch per device task (grid kernels, host continuations), and the device task queue
+    # (the tasks' tile kernels recorded, one persistent launch per batch)
+    out["flowgraph"] = flowgraph(N, [])
+    out["flowgraph_device_queue"] = flowgraph(N, ["-q"])
+    out["flowgraph_N4096"] = flowgraph(4096, [])
+    out["flowgraph_N4096_device_queue"] = flowgraph(4096, ["-q"])
+    gfs = out["flowgraph"]["gflops_per_iter"]
     # the same factorisation by the persistent executor, device time
     t = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
     gbx.plgsy(t, N, NB, N, 3872)
@@ -824,11 +833,12 @@ def run_ttg_flowgraph(gbx, dev, N=16384, NB=512, iters=2, chain_tasks=20000):
     chain = gb.build_chain()
     out["chain"] = {}
     for flows in (0, 1):
-        r = subprocess.run([chain, "-f", str(flows), "-n", str(chain_tasks)], capture_output=True, text=True,
-                           timeout=600)
-        m = re.search(r"avg ([0-9.eE+-]+)", r.stdout)
-        out["chain"]["flows_%d" % flows] = {"rc": r.returncode, "tasks": chain_tasks + 1,
-                                            "us_per_task": float(m.group(1)) if m else None}
+        for mode, extra in (("", []), ("_device_queue", ["-q"])):
+            r = subprocess.run([chain, "-f", str(flows), "-n", str(chain_tasks)] + extra, capture_output=True,
+                               text=True, timeout=600)
+            m = re.search(r"avg ([0-9.eE+-]+)", r.stdout)
+            out["chain"]["flows_%d%s" % (flows, mode)] = {"rc": r.returncode, "tasks": chain_tasks + 1,
+                                                          "us_per_task": float(m.group(1)) if m else None}
     return out
 
 
