@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision configuration")
     p.add_argument("--no-batched", action="store_true", help="skip the batched configuration")
+    p.add_argument("--only-main", action="store_true",
+                   help="the headline step alone (no e2e, secondary configurations or CPU baseline), e.g. for a "
+                        "launch-list capture")
     p.add_argument("--profile-case", choices=["dag", "mixed", "batched", "refine", "batched_mixed"], default=None,
                    help="run one small case of one kernel (N=8192) for an ncu capture; prints no JSON")
     p.add_argument("--profile-N", type=int, default=8192, help="matrix order of --profile-case dag/mixed")
@@ -320,9 +323,10 @@ def run_ours(args, ws, rank, local):
     if not args.no_batched:
         torch.cuda.empty_cache()
         line["batched_mixed"] = run_batched_mixed(gbx, dev, cpu=rank == 0 and not args.no_cpu)
-    line["config_small"] = run_config1(gbx, dev, cpu=rank == 0 and not args.no_cpu)
-    line["ttg_flowgraph"] = run_ttg_flowgraph(gbx, dev)
-    line["potri"] = run_potri(gbx, dev, cpu=rank == 0 and not args.no_cpu)
+    if not args.only_main:
+        line["config_small"] = run_config1(gbx, dev, cpu=rank == 0 and not args.no_cpu)
+        line["ttg_flowgraph"] = run_ttg_flowgraph(gbx, dev)
+        line["potri"] = run_potri(gbx, dev, cpu=rank == 0 and not args.no_cpu)
 
     if rank == 0 and not args.no_cpu:
         times, blas = cpu_run(args.cpu_N, NB, 2)
@@ -925,6 +929,8 @@ def profile_case(case, N=8192):
 
 def main():
     args = parse()
+    if args.only_main:
+        args.no_e2e = args.no_mixed = args.no_batched = args.no_cpu = True
     if args.profile_case:
         profile_case(args.profile_case, args.profile_N)
         return
