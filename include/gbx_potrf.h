@@ -117,6 +117,13 @@ int gbx_dgemm_nn_tile(int m, int n, int k, const double* A, int lda, const doubl
 /* Bytes of device workspace gbx_dpotrf_tiled needs. */
 int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes);
 
+/* Block edge of the executor (the reference's tile tasks run as tasks on blocks inside the tiles):
+ * 0 (default) = automatic, 64-blocks for N <= 4096 (a small matrix is bound by its chain of block
+ * steps) and 128 above; 32, 64 or 128 forces that edge where it divides the tile (else the
+ * automatic edge). Applies to later gbx_dpotrf_tiled / gbx_dpotrs_tiled / bufferSize calls, which
+ * must agree: size the workspace after setting it. Returns 0 or GBX_ERR_ARG. */
+int gbx_set_dag_block_edge(int b);
+
 /* Factorises the tile-major lower matrix in place (asynchronous). The status is kept in the
  * workspace; read it with gbx_dpotrf_tiled_status. */
 int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream);

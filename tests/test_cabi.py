@@ -69,6 +69,23 @@ def test_argument_validation_without_gpu(gbx):
     assert L.gbx_potrf_mixed_bufferSize(1000, 1024, ctypes.byref(sz)) == gbx.GBX_ERR_ARG
 
 
+def test_dag_block_edge_setting(gbx):
+    """The executor's block edge: 0 (automatic), 32, 64 or 128; anything else is refused. The
+    workspace follows the edge (64-blocks for N <= 4096 by default: four times the counters)."""
+    L = gbx.lib()
+    for bad in (-1, 16, 96, 256):
+        assert L.gbx_set_dag_block_edge(bad) == gbx.GBX_ERR_ARG
+    a, b = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    try:
+        assert L.gbx_set_dag_block_edge(128) == 0
+        assert L.gbx_dpotrf_tiled_bufferSize(2048, 128, ctypes.byref(a)) == 0
+        assert L.gbx_set_dag_block_edge(64) == 0
+        assert L.gbx_dpotrf_tiled_bufferSize(2048, 128, ctypes.byref(b)) == 0
+        assert b.value > a.value
+    finally:
+        assert L.gbx_set_dag_block_edge(0) == 0
+
+
 def test_wait_timeout_setting(gbx):
     L = gbx.lib()
     old = L.gbx_get_wait_timeout_ns()

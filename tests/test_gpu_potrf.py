@@ -218,6 +218,22 @@ def test_dag_potrf_matches_oracle(gbx, cuda, gen, N, NB):
         assert oracle.frob_residual(L, A0) <= 1e-15
 
 
+@pytest.mark.parametrize("edge", [128, 64, 32])
+def test_dag_block_edges_match_oracle(gbx, cuda, edge):
+    """The executor's block edge (automatic: 64 up to N=4096, 128 above; forced here) changes only
+    the order of the FP64 operations: the factor stays within the parity bar of the oracle."""
+    N, NB = 2048, 128
+    t0 = oracle.uniform_sym_tiles(N, NB, 42)
+    assert gbx.lib().gbx_set_dag_block_edge(edge) == 0
+    try:
+        got = run_dag(gbx, cuda, N, NB, t0)
+    finally:
+        gbx.lib().gbx_set_dag_block_edge(0)
+    ref = t0.copy()
+    assert oracle.potrf_tiled(ref, N, NB, nthreads=0, use_blas=oracle.load_openblas())[0] == 0
+    assert_factor_close(oracle.tiles_to_lower(got, N, NB), oracle.tiles_to_lower(ref, N, NB))
+
+
 def test_dag_potrf_8192_vs_cpu_oracle(gbx, cuda):
     # the checked size of the N=32768 configuration
     N, NB = 8192, 512
@@ -328,21 +344,24 @@ def test_full_size_solve_backward_error(gbx, cuda):
     assert berr <= 1e-14
 
 
-def test_task_timeline_trace(gbx, cuda, tmp_path):
-    """The per-task timeline records every executed task of the persistent executor."""
+@pytest.mark.parametrize("edge,ntb", [(128, 8), (0, 16)])
+def test_task_timeline_trace(gbx, cuda, tmp_path, edge, ntb):
+    """The per-task timeline records every executed task of the persistent executor (N=1024:
+    eight 128-blocks when forced, sixteen 64-blocks by the automatic choice for small matrices)."""
     import json
     import torch
-    N, NB = 1024, 256  # 128-blocks: NTb = 8
+    N, NB = 1024, 256
     A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=cuda)
     gbx.gen_uniform_sym(A, N, NB, seed=1)
     buf = torch.zeros(2 + 4 * 1000, dtype=torch.int64, device=cuda)
     gbx.lib().gbx_set_trace_buffer(_vp(buf), 1000)
+    assert gbx.lib().gbx_set_dag_block_edge(edge) == 0
     try:
         gbx.potrf_tiled(A, N, NB)
     finally:
         gbx.lib().gbx_set_trace_buffer(None, 0)
+        gbx.lib().gbx_set_dag_block_edge(0)
     recs = gbx.trace_records(buf)
-    ntb = 8
     assert len(recs) == ntb + ntb * (ntb - 1) + ntb * (ntb - 1) * (ntb - 2) // 6
     assert all(r["end_ns"] >= r["start_ns"] for r in recs)
     pot = {r["a"]: r for r in recs if r["type"] == "POTRF"}

@@ -45,20 +45,23 @@ __device__ __forceinline__ void chol_pivot(double d, double& l, double& inv) {
 // 256 threads, each owning an 8 x 8 micro-tile (rows 4tx..4tx+3 and 64+4tx..64+4tx+3, the same
 // pattern of columns from ty), read from shared memory with 16-byte vector loads; k staged through
 // double-buffered chunks of 16 with a register prefetch of the next chunk.
+// kSmall (m, n <= 64): each thread owns only the first 4 x 4 quarter of that pattern, so a 64 x 64
+// block keeps every thread's FMAs useful (the 8 x 8 form would spend three quarters on zeros).
 // smem: 2 * 2 * 16 * 128 elements (64 KB in FP64)
 // ------------------------------------------------------------------------------------------------
-template <typename T>
+template <typename T, bool kSmall = false>
 __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb, T* C,
                                            int ldc, int m, int n, int k, bool lower, T* sm) {
+  constexpr int R = kSmall ? 4 : 8;  // micro-tile edge
   T* As = sm;                       // [2][kKC][kBlk]
   T* Bs = sm + 2 * kKC * kBlk;      // [2][kKC][kBlk]
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int lrow = tid & 127, lk0 = tid >> 7;
-  T acc[8][8];
+  T acc[R][R];
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < R; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+    for (int j = 0; j < R; ++j) acc[i][j] = T(0);
 
   const int nchunks = (k + kKC - 1) / kKC;
   T ra[8], rb[8];
@@ -90,13 +93,15 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
       for (int kk = 0; kk < kKC; ++kk) {
         T a0[4], a1[4], b0[4], b1[4];
         lds4(as + kk * kBlk + 4 * tx, a0);
-        lds4(as + kk * kBlk + 64 + 4 * tx, a1);
         lds4(bs + kk * kBlk + 4 * ty, b0);
-        lds4(bs + kk * kBlk + 64 + 4 * ty, b1);
+        if (!kSmall) {
+          lds4(as + kk * kBlk + 64 + 4 * tx, a1);
+          lds4(bs + kk * kBlk + 64 + 4 * ty, b1);
+        }
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < R; ++i)
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+          for (int j = 0; j < R; ++j) {
             const T ai = i < 4 ? a0[i & 3] : a1[i & 3], bj = j < 4 ? b0[j & 3] : b1[j & 3];
             acc[i][j] = fma(ai, bj, acc[i][j]);
           }
@@ -106,10 +111,10 @@ __device__ __forceinline__ void op_gemm_nt(const T* __restrict__ A, int lda, con
     }
   }
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
+  for (int j = 0; j < R; ++j) {
     const int col = (j < 4 ? 0 : 60) + 4 * ty + j;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < R; ++i) {
       const int row = (i < 4 ? 0 : 60) + 4 * tx + i;
       if (row < m && col < n && (!lower || row >= col)) {
         T* p = C + row + (long long)col * ldc;

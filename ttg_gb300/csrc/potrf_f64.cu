@@ -184,14 +184,19 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
       case T_SYRK: {
         const int K = tk.a, M = tk.b;
         const double* a = V.ptr(M, K);
-        op_gemm_nt<double>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
+        if (V.b <= 64) op_gemm_nt<double, true>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
+        else op_gemm_nt<double>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
         target = P.cnt + tri_index(M, M, NTb);
         break;
       }
       default: {
         const int M = tk.a, Nn = tk.b, K = tk.c;
-        op_gemm_nt<double>(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn), V.dim(K), false,
-                   smem);
+        if (V.b <= 64)
+          op_gemm_nt<double, true>(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn),
+                                   V.dim(K), false, smem);
+        else
+          op_gemm_nt<double>(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn), V.dim(K),
+                             false, smem);
         target = P.cnt + tri_index(M, Nn, NTb);
         break;
       }
@@ -519,6 +524,19 @@ int block_edge(int NB) {
   return 0;
 }
 
+// Block edge of the executor for an N x N matrix of NB tiles. A small matrix is bound by its chain
+// of block steps (each a single-CTA FP64 POTRF, TRSM and update of one block), so up to
+// g_small_n it takes 64-blocks: twice the steps, each about a quarter as long; larger matrices are
+// bound by the total work and keep 128-blocks, whose block GEMM runs the FP64 pipe best.
+int g_small_n = 4096;
+int g_forced_edge = 0;  // gbx_set_dag_block_edge
+int dag_block_edge(int N, int NB) {
+  const int b = block_edge(NB);
+  if (b == 0) return 0;
+  if (g_forced_edge > 0) return (NB % g_forced_edge == 0 && g_forced_edge <= b) ? g_forced_edge : b;
+  return (b == kBlk && N <= g_small_n) ? 64 : b;
+}
+
 size_t dag_workspace_bytes(int NTb) {
   const size_t counters = (size_t)NTb * (NTb + 1) / 2 * sizeof(int);
   return sizeof(DagState) + ((counters + 255) / 256) * 256;
@@ -556,7 +574,7 @@ BlockView tiled_view(int N, int NB, double* tiles) {
   BlockView V;
   V.base = tiles;
   V.N = N;
-  V.b = block_edge(NB);
+  V.b = dag_block_edge(N, NB);
   V.ld = NB;
   V.r = NB / V.b;
   V.NT = (N + NB - 1) / NB;
@@ -684,9 +702,15 @@ int gbx_dgemm_nt_tile(int m, int n, int k, const double* A, int lda, const doubl
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
+int gbx_set_dag_block_edge(int b) {
+  if (b != 0 && b != 32 && b != 64 && b != kBlk) return GBX_ERR_ARG;
+  g_forced_edge = b;
+  return GBX_OK;
+}
+
 int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes) {
   if (N < 0 || NB <= 0 || bytes == nullptr) return GBX_ERR_ARG;
-  const int b = block_edge(NB);
+  const int b = dag_block_edge(N, NB);
   if (b == 0) return GBX_ERR_ARG;
   const int NTb = std::max(1, (N + b - 1) / b);
   *bytes = dag_workspace_bytes(NTb);
