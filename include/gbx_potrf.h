@@ -124,6 +124,23 @@ int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes);
  * must agree: size the workspace after setting it. Returns 0 or GBX_ERR_ARG. */
 int gbx_set_dag_block_edge(int b);
 
+/* FP64 update mode of the tiled executor (gbx_dpotrf_tiled, gbx_dposv_tiled_host and their
+ * bufferSize calls; replaces the cublasDsyrk / cublasDgemm tile calls at examples/potrf/potrf.h:422-427
+ * and 547-553 inside it):
+ *   0 (default)  FP64 FMA block GEMMs;
+ *   1            the same products on the bf16 tensor cores, exactly: each finished block of L is
+ *                split into seven 8-bit digit planes with a power-of-two scale per row, the 28 plane
+ *                products of the seven leading digit groups accumulate exactly in FP32, and each
+ *                element is composed from the exact integer sum with one rounding to FP64 and
+ *                subtracted from C with one FP64 add (product error ~2^-55 of the rows' largest
+ *                entries, the FP64 dot product's is ~k 2^-53). POTRF and TRSM tasks stay FP64.
+ *                Needs 128-blocks (the tile edge a multiple of 128 and N above the small-matrix
+ *                threshold, or gbx_set_dag_block_edge(128)); other block edges run mode 0. The
+ *                workspace grows by 7 x 32 KB + 512 B per lower 128-block (7.6 GB at N = 32768).
+ * Size the workspace after setting it. Returns 0 or GBX_ERR_ARG. */
+int gbx_set_fp64_update(int mode);
+int gbx_get_fp64_update(void);
+
 /* Factorises the tile-major lower matrix in place (asynchronous). The status is kept in the
  * workspace; read it with gbx_dpotrf_tiled_status. */
 int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream);

@@ -59,6 +59,8 @@ SIGNATURES = {
     "gbx_taskq_status": (_i, [_vp, _vp]),
     "gbx_dpotrf_tiled_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_set_dag_block_edge": (_i, [_i]),
+    "gbx_set_fp64_update": (_i, [_i]),
+    "gbx_get_fp64_update": (_i, []),
     "gbx_dpotrf_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
     "gbx_dpotrf_tiled_status": (_i, [_vp, _vp]),
     "gbx_dpotrs_tiled": (_i, [_i, _i, _vp, _i, _vp, _i, _vp]),

@@ -10,6 +10,14 @@ constexpr int kBlk = 128;      // largest block edge handled by one CTA
 constexpr int kKC = 16;        // k-chunk of the GEMM staging
 constexpr int kPW = 32;        // panel width of the TRSM
 
+// CTA barrier of the block operations: every thread of the CTA, or (kNamed) the first 256 threads
+// only, with named barrier 1, so that a larger CTA can run an operation on 256 of its threads
+template <bool kNamed>
+__device__ __forceinline__ void ops_sync() {
+  if (kNamed) asm volatile("bar.sync 1, 256;" ::: "memory");
+  else __syncthreads();
+}
+
 // four consecutive elements from shared memory in 16-byte loads (p 16-byte aligned)
 __device__ __forceinline__ void lds4(const float* p, float (&v)[4]) {
   const float4 f = *(const float4*)p;
@@ -179,7 +187,7 @@ __device__ __forceinline__ void col_solve32(float (&x)[32], const float* Lp, int
   }
 }
 
-template <typename T>
+template <typename T, bool kNamed = false>
 __device__ int op_potrf(T* A, int lda, int n, T* sm) {
   T* S = sm;                              // col-major, ld 128
   int* flag = (int*)(sm + kBlk * kBlk);
@@ -189,7 +197,7 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
     const int i = idx & (kBlk - 1), j = idx >> 7;
     if (i < n && i >= j) S[i + kBlk * j] = __ldcg(A + i + (long long)j * lda);
   }
-  __syncthreads();
+  ops_sync<kNamed>();
   int info = 0;
   for (int p0 = 0; p0 < n; p0 += 32) {
     const int pw = min(32, n - p0);
@@ -226,7 +234,7 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
         for (int c = 0; c < 32; ++c)
           if (c <= lane) S[(p0 + lane) + kBlk * (p0 + c)] = x[c];
     }
-    __syncthreads();
+    ops_sync<kNamed>();
     info = *flag;
     if (info) break;
     // rows below the block: each thread solves one row in registers
@@ -239,7 +247,7 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
       for (int c = 0; c < 32; ++c)
         if (c < pw) S[r + kBlk * (p0 + c)] = x[c];
     }
-    __syncthreads();
+    ops_sync<kNamed>();
     // trailing update S(i, c) -= sum_k S(i, k) S(c, k), p0+pw <= c <= i < n, in 4 x 4 register blocks
     const int t0 = p0 + pw, t = n - t0;
     if (t > 0) {
@@ -278,13 +286,13 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
           }
       }
     }
-    __syncthreads();
+    ops_sync<kNamed>();
   }
   for (int idx = tid; idx < kBlk * n; idx += kThreads) {
     const int i = idx & (kBlk - 1), j = idx >> 7;
     if (i < n && i >= j) __stcg(A + i + (long long)j * lda, S[i + kBlk * j]);
   }
-  __syncthreads();
+  ops_sync<kNamed>();
   return info;
 }
 
@@ -307,7 +315,7 @@ constexpr size_t op_trsm_smem_elems() {
 
 // kColSolve (FP32 only): the panel solve in the column-wise form with the branch-free reciprocal,
 // for kernels with registers to spare; the default keeps the row-wise form and IEEE division.
-template <typename T, bool kColSolve = false>
+template <typename T, bool kColSolve = false, bool kNamed = false>
 __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, int n, T* sm) {
   constexpr int KC = TrsmChunk<T>::value;
   T* P = sm;                    // [kPW][128]  panel, P[c*128 + r]
@@ -325,7 +333,7 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
       const int c = idx & 31, c2 = idx >> 5;
       Ld[idx] = (c < pw && c2 <= c) ? __ldcg(L + (p0 + c) + (long long)(p0 + c2) * ldl) : T(0);
     }
-    __syncthreads();
+    ops_sync<kNamed>();
     if (p0 > 0) {
       // P -= X(:, 0:p0) L(p0:p0+pw, 0:p0)^T, k in chunks of KC; the next chunk is prefetched into
       // registers while the current one is multiplied (hides the L2 latency)
@@ -359,7 +367,7 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
       gload(0);
       for (int k0 = 0; k0 < p0; k0 += KC) {
         sstore();
-        __syncthreads();
+        ops_sync<kNamed>();
         if (k0 + KC < p0) gload(k0 + KC);
 #pragma unroll
         for (int kk = 0; kk < KC; ++kk) {  // rows 4tx..4tx+3 x columns 4ty..4ty+3, vector loads
@@ -371,13 +379,13 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
         }
-        __syncthreads();
+        ops_sync<kNamed>();
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + 4 * tx + i] -= acc[i][j];
-      __syncthreads();
+      ops_sync<kNamed>();
     }
     // each thread solves its row of the panel in registers; the column-wise solve synchronises its
     // warp, so it runs on whole warps (rows past m are zero in P and are never stored back)
@@ -396,12 +404,12 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
 #pragma unroll
       for (int c = 0; c < kPW; ++c) P[c * kBlk + r] = x[c];
     }
-    __syncthreads();
+    ops_sync<kNamed>();
     for (int idx = tid; idx < kPW * kBlk; idx += kThreads) {
       const int r = idx & (kBlk - 1), c = idx >> 7;
       if (r < m && c < pw) __stcg(B + r + (long long)(p0 + c) * ldb, P[idx]);
     }
-    __syncthreads();
+    ops_sync<kNamed>();
   }
 }
 

@@ -1,0 +1,140 @@
+// FP64 block products on the bf16 tensor cores (Ozaki-style splitting, Ozaki, Ogita, Oishi and Rump
+// 2012): the building blocks the executor's emulated GEMM/SYRK tasks use.
+//
+// Splitting. Every row r of an FP64 block L (128 x 128) is scaled by its own power of two 2^e_r,
+// with |L(r,k)| < 2^e_r for every k, and rounded to the fixed-point integer
+//     F(r,k) = round(L(r,k) 2^(55 - e_r)),  |F| <= 2^55,
+// which is then written as seven balanced base-256 digits,
+//     F = sum_{i=0..6} d_i 256^(6-i),   d_i in [-128, 127] for i >= 1, |d_0| <= 128,
+// each digit stored as a bf16 "slice" (an integer of at most 8 significant bits: exact). So
+// L(r,k) = 2^(e_r - 55) sum_i d_i(r,k) 2^(8(6-i)) up to 2^-56 |2^e_r|.
+//
+// Products. For C(r,c) -= sum_k A(r,k) B(c,k), with digit planes a_i of A and b_j of B:
+//     sum_k A B = 2^(eA_r + eB_c - 110) sum_g 2^(8(12-g)) acc_g,   acc_g = sum_{i+j=g} sum_k a_i b_j.
+// The groups g = 0..6 are kept (the dropped ones are below 2^-56 of the leading term). Each acc_g is
+// a sum of at most 7 * 128 products of magnitude <= 2^14: below 2^24 in magnitude, so the tensor
+// cores' FP32 accumulation of these integers is exact. Then
+//     sum_k A B = X 2^(eA_r + eB_c - 62),   X = sum_{g=0..6} acc_g 2^(8(6-g))   (an integer < 2^73),
+// rounded once to FP64 from the exact 128-bit X with integer instructions, and subtracted from C
+// with one FP64 add: two roundings in all, against k of them for the FP64 dot product.
+//
+// Costs on GB300 (measured per SM per clock): FP64 add/FMA and every conversion to or from FP64
+// ~1.6-1.9, float->int ~15, integer ~60, FP32 ~113. Hence integer-only splitting and composing, and
+// a single FP64 operation per element of C per task.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbx {
+namespace emu {
+
+constexpr int kSlices = 7;                                  // digit planes per block
+constexpr int kEdge = 128;                                  // block edge of the emulated executor
+constexpr long long kPlaneElems = (long long)kEdge * kEdge; // bf16 elements per plane
+constexpr long long kBlockElems = kSlices * kPlaneElems;    // bf16 elements per block
+constexpr int kEmptyRow = -4000;                            // exponent of an all-zero row
+
+// float holding an integer of magnitude <= 2^22 -> its bf16 bit pattern (exact for |d| <= 256)
+__device__ __forceinline__ uint32_t digit_bf16(int d) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;  // exact for |d| < 2^22
+  return __float_as_uint(f) >> 16;
+}
+
+// Splits the FP64 block L (m x n valid of a 128 x 128 block, column-major, leading dimension ld)
+// into kSlices bf16 digit planes S[i][r][k] (row-major, k contiguous, zero outside m x n) and the
+// row exponents rexp[r]. Threads 0..255 of the CTA (synchronised with named barrier 1);
+// s_exp: 256 ints of shared memory.
+__device__ __forceinline__ void slice_block(const double* __restrict__ L, int ld, int m, int n,
+                                            uint16_t* __restrict__ S, int* __restrict__ rexp, int* s_exp) {
+  const int r = threadIdx.x & (kEdge - 1), h = threadIdx.x >> 7;  // row, column half
+  const int k0 = h * (kEdge / 2);
+  // 1. largest biased exponent in the row (integer compare of the exponent fields)
+  int mex = 0;
+  if (r < m)
+    for (int k = k0; k < min(k0 + kEdge / 2, n); ++k) mex = max(mex, (__double2hiint(__ldcg(L + r + (long long)k * ld)) >> 20) & 0x7ff);
+  s_exp[h * kEdge + r] = mex;
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+  mex = max(s_exp[r], s_exp[kEdge + r]);
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+  // every |L(r,k)| < 2^e (frexp exponent of the largest); rows of zeros and subnormals give no digits
+  const int e = mex - 1022;
+  if (h == 0) rexp[r] = (mex > 0) ? e : kEmptyRow;
+  // 2. fixed point and digits, eight consecutive k per 16-byte store of each plane
+  for (int kc = 0; kc < kEdge / 2; kc += 8) {
+    uint32_t pk[kSlices][4];
+#pragma unroll
+    for (int i = 0; i < kSlices; ++i)
+#pragma unroll
+      for (int w = 0; w < 4; ++w) pk[i][w] = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = k0 + kc + j;
+      long long F = 0;
+      if (mex > 0 && r < m && k < n) {
+        const long long bits = __double_as_longlong(__ldcg(L + r + (long long)k * ld));
+        const int ex = (int)((bits >> 52) & 0x7ff);
+        if (ex > 0) {
+          const long long mant = (bits & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
+          const int sh = ex - 1020 - e;  // F = mant 2^sh, sh <= 2 because |L| < 2^e
+          long long f = 0;
+          if (sh >= 0) f = mant << sh;
+          else if (sh > -60) f = (mant + (1LL << (-sh - 1))) >> (-sh);  // round half up
+          F = bits < 0 ? -f : f;
+        }
+      }
+#pragma unroll
+      for (int i = kSlices - 1; i >= 1; --i) {
+        const int d = (int)((F + 128) & 255) - 128;
+        F = (F - d) >> 8;  // exact: F - d is a multiple of 256
+        pk[i][j >> 1] |= digit_bf16(d) << (16 * (j & 1));
+      }
+      pk[0][j >> 1] |= digit_bf16((int)F) << (16 * (j & 1));
+    }
+#pragma unroll
+    for (int i = 0; i < kSlices; ++i)
+      *(uint4*)(S + (long long)i * kPlaneElems + (long long)r * kEdge + k0 + kc) =
+          make_uint4(pk[i][0], pk[i][1], pk[i][2], pk[i][3]);
+  }
+}
+
+// X 2^E as FP64, X = sum_g acc_g 2^(8(6-g)) from the exact FP32 group sums; rounded to nearest
+// (ties away from zero) from the 64 leading bits of the exact 128-bit X. Branch-free, so that the
+// compositions of neighbouring elements interleave; *odd is set when the result leaves the normal
+// FP64 range (the value returned is then wrong: see compose_slow).
+__device__ __forceinline__ double compose(const uint32_t (&acc)[kSlices], int E, bool* odd) {
+  long long a[kSlices];
+#pragma unroll
+  for (int g = 0; g < kSlices; ++g) a[g] = __float2int_rn(__uint_as_float(acc[g]));
+  const long long H = (a[0] << 16) + (a[1] << 8) + a[2];                    // |H| < 2^41
+  const long long L = (a[3] << 24) + (a[4] << 16) + (a[5] << 8) + a[6];     // |L| < 2^49
+  const __int128 X = ((__int128)H << 32) + (__int128)L;
+  const bool neg = X < 0;
+  const unsigned __int128 u = neg ? (unsigned __int128)(-X) : (unsigned __int128)X;
+  const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
+  const int zh = __clzll((long long)hi), zl = __clzll((long long)lo);
+  const int z = hi ? zh : 64 + zl;  // leading zeros of the 128 bits (128 for X = 0)
+  // the leading 64 bits, leading one at bit 63 (z <= 127 unless X = 0)
+  const unsigned __int128 ut = u << (z & 127);
+  const unsigned long long top = (unsigned long long)(ut >> 64);
+  int p = 127 - z;
+  unsigned long long mant = (top >> 11) + ((top >> 10) & 1);  // 53 bits, rounded
+  const bool carry = (mant >> 53) != 0;
+  mant = carry ? (mant >> 1) : mant;
+  p += carry;
+  const int be = p + E + 1023;
+  *odd = (u != 0) && (be <= 0 || be >= 2047);
+  const unsigned long long bits =
+      ((unsigned long long)neg << 63) | ((unsigned long long)(be & 0x7ff) << 52) | (mant & 0xFFFFFFFFFFFFFull);
+  return u == 0 ? 0.0 : __longlong_as_double((long long)bits);
+}
+
+// the same value outside the normal range (subnormal or overflowing results): scaled in FP64
+__device__ __noinline__ double compose_slow(const uint32_t (&acc)[kSlices], int E) {
+  double v = 0;
+#pragma unroll
+  for (int g = 0; g < kSlices; ++g) v += ldexp((double)__float2int_rn(__uint_as_float(acc[g])), 8 * (6 - g) + E);
+  return v;
+}
+
+}  // namespace emu
+}  // namespace gbx

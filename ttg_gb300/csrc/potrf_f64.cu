@@ -10,17 +10,24 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <thread>
 #include <vector>
 
 #include "block_ops.cuh"
+#include "emu_f64.cuh"
 #include "gbx_common.cuh"
 #include "gbx_potrf.h"
 #include "plgsy.cuh"
 #include "taskq.h"
+#include "tc_common.cuh"
 
 namespace gbx {
+namespace tc {
+int make_tmap_kmajor_bf16(CUtensorMap* map, const void* base, uint64_t rows, uint64_t k, uint64_t ld,
+                          uint32_t box_rows);  // gemm_bf16.cu
+}
 
 constexpr size_t kDagSmemBytes = (size_t)kBlk * kBlk * sizeof(double) + 64;  // POTRF dominates
 
@@ -94,6 +101,10 @@ struct DagParams {
   int* col_done;
   volatile int* host_flag;
   int group_blocks, groups;
+  // tensor-core emulated updates (kEmu launches): digit planes and row exponents of every lower
+  // block, indexed by tri_index (diagonal blocks unused)
+  uint16_t* planes;
+  int* rexp;
 };
 
 // finished POTRF/TRSM blocks a group needs: block columns J of the group hold NTb - J blocks each
@@ -110,6 +121,194 @@ __device__ __forceinline__ void release_columns(const DagParams& P) {
   }
 }
 
+// ---- the emulated update task: C(M,N) -= L(M,K) L(N,K)^T on the tensor cores -----------------
+// Two passes over the 64-column halves of C; each pass accumulates the 28 digit-plane products of
+// the seven groups g = i + j <= 6 into seven 128 x 64 FP32 accumulators in TMEM (448 columns), over
+// two 64-wide chunks of k. Roles (warps of the 256-thread CTA):
+// The emulated executor runs 384 threads (twelve warps); its FP64 tasks use the first 256.
+//   warp 8 lane 0  TMA producer: per chunk the seven B planes (64 rows each) into one of two
+//                  buffers, then the A planes i = 6..0 (128 rows each) through a ring of six slots
+//   warps 9-11 lane 0  MMA issuers: for i = 6..0, j = 0..6-i: D[i+j] += A_i B_j^T (M128 N64 K16 x 4),
+//                  each issuer owning whole accumulator groups (so that every group's MMAs keep
+//                  their order): {6, 1}, {5, 2}, {4, 3, 0}, 9, 9 and 10 of the 28 pairs of a chunk.
+//                  One thread issues a tcgen05.mma only every ~110 clocks, while an N=64 product
+//                  takes the tensor pipe ~35: three issuers keep the pipe fed. Each A slot is
+//                  released after all three have committed its pairs, each B buffer after its chunk
+//   warps 0-7      epilogue: TMEM lane quarter = warp % 4, column half = warp / 4; per element the
+//                  exact compose and one FP64 subtraction from C
+namespace emuk {
+constexpr int kASlots = 6, kBBufs = 2;
+constexpr uint32_t kABytes = 128 * 128, kBBytes = 64 * 128;  // one plane chunk: rows x 128 bytes
+constexpr uint32_t kBSetBytes = emu::kSlices * kBBytes;
+constexpr size_t kSmemBytes = (size_t)kBBufs * kBSetBytes + (size_t)kASlots * kABytes + 1024;
+constexpr int kTmemCols = 512;
+constexpr int kThreadsEmu = 384;
+constexpr int kEpiWarps = 8, kProducerWarp = 8, kIssuerWarp0 = 9;
+constexpr int kIssuers = 3;  // MMA issuer threads: lane 0 of warps 9, 10, 11
+// accumulator groups of issuer k: bit g set in kGroups[k]
+__host__ __device__ constexpr uint32_t issuer_groups(int k) { return k == 0 ? 0x42u : k == 1 ? 0x24u : 0x19u; }
+struct Bars {
+  uint64_t a_full[kASlots], a_empty[kASlots], b_full[kBBufs], b_empty[kBBufs], done, tmem_free, fin[kIssuers];
+};
+struct Pipe {  // pipeline positions, each kept by the one thread that uses it
+  uint32_t a_it = 0, b_it = 0;  // producer: plane chunks issued; MMA issuer: consumed (A ring, B buffers)
+  uint32_t passes = 0;          // MMA issuer and epilogue threads: accumulator passes begun
+  bool mma_issued = false;
+};
+}  // namespace emuk
+
+__device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtensorMap* tmB, const DagParams& P,
+                                           int M, int Nn, int K, bool syrk, uint8_t* smem, emuk::Bars& bars,
+                                           emuk::Pipe& pp, uint32_t tmem, int* s_cexp) {
+  using namespace emuk;
+  using namespace tc;
+  const BlockView& V = P.V;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long tA = tri_index(M, K, P.NTb), tB = tri_index(Nn, K, P.NTb);
+  int* err = &P.st->status;
+  uint8_t* smB = smem;                               // [kBBufs][7][64 x 128 B]
+  uint8_t* smA = smem + (size_t)kBBufs * kBSetBytes;  // [kASlots][128 x 128 B]
+  // column exponents of this task (rows of L(N,K)), before the roles split
+  if (threadIdx.x < emu::kEdge) s_cexp[threadIdx.x] = __ldcg(P.rexp + tB * emu::kEdge + threadIdx.x);
+  __syncthreads();
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      // the planes were written by other CTAs with ordinary stores, and this CTA's shared memory
+      // last by its FP64 tasks: order both before the async-proxy accesses
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      for (int pass = 0; pass < 2; ++pass)
+        for (int c = 0; c < 2; ++c) {
+          const uint32_t bb = pp.b_it % kBBufs, bph = (pp.b_it / kBBufs) & 1;
+          if (!mbar_wait(smem_u32(&bars.b_empty[bb]), bph ^ 1, err, P.timeout_ns)) return;
+          const uint32_t bdst = smem_u32(smB + (size_t)bb * kBSetBytes);
+          mbar_arrive_expect_tx(smem_u32(&bars.b_full[bb]), kBSetBytes);
+          for (int j = 0; j < emu::kSlices; ++j)
+            tma_load_2d(bdst + j * kBBytes, tmB, smem_u32(&bars.b_full[bb]), c * 64,
+                        (int)((tB * emu::kSlices + j) * emu::kEdge + pass * 64));
+          ++pp.b_it;
+          for (int i = emu::kSlices - 1; i >= 0; --i) {
+            const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
+            if (!mbar_wait(smem_u32(&bars.a_empty[sl]), aph ^ 1, err, P.timeout_ns)) return;
+            mbar_arrive_expect_tx(smem_u32(&bars.a_full[sl]), kABytes);
+            tma_load_2d(smem_u32(smA + (size_t)sl * kABytes), tmA, smem_u32(&bars.a_full[sl]), c * 64,
+                        (int)((tA * emu::kSlices + i) * emu::kEdge));
+            ++pp.a_it;
+          }
+        }
+    }
+    return;
+  }
+  if (warp >= kIssuerWarp0) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_f16(128, 64, true);
+      const uint32_t mine = issuer_groups(warp - kIssuerWarp0);
+      // consumer positions: this thread's own copy of a_it / b_it, advanced through the same
+      // sequence of plane chunks as the producer's
+      uint32_t& a_it = pp.a_it;
+      uint32_t& b_it = pp.b_it;
+      for (int pass = 0; pass < 2; ++pass) {
+        if (pp.passes > 0 &&  // the previous pass's epilogue has read the accumulators
+            !mbar_wait(smem_u32(&bars.tmem_free), (pp.passes - 1) & 1, err, P.timeout_ns))
+          return;
+        tc_fence_after();
+        for (int c = 0; c < 2; ++c) {
+          const uint32_t bb = b_it % kBBufs, bph = (b_it / kBBufs) & 1;
+          if (!mbar_wait(smem_u32(&bars.b_full[bb]), bph, err, P.timeout_ns)) return;
+          tc_fence_after();
+          const uint32_t bbase = smem_u32(smB + (size_t)bb * kBSetBytes);
+          for (int i = emu::kSlices - 1; i >= 0; --i) {
+            const uint32_t sl = a_it % kASlots, aph = (a_it / kASlots) & 1;
+            if (!mbar_wait(smem_u32(&bars.a_full[sl]), aph, err, P.timeout_ns)) return;
+            tc_fence_after();
+            const uint64_t ad = desc_kmajor_sw128(smem_u32(smA + (size_t)sl * kABytes));
+            for (int j = 0; j + i < emu::kSlices; ++j) {
+              if (!((mine >> (i + j)) & 1)) continue;
+              const uint64_t bd = desc_kmajor_sw128(bbase + j * kBBytes);
+              const uint32_t d = tmem + (uint32_t)((i + j) * 64);
+              umma_f16(d, ad, bd, idesc, (c | j) != 0 ? 1u : 0u);
+              umma_f16(d, ad + 2, bd + 2, idesc, 1u);
+              umma_f16(d, ad + 4, bd + 4, idesc, 1u);
+              umma_f16(d, ad + 6, bd + 6, idesc, 1u);
+              pp.mma_issued = true;
+            }
+            umma_commit(smem_u32(&bars.a_empty[sl]));
+            ++a_it;
+          }
+          umma_commit(smem_u32(&bars.b_empty[bb]));
+          ++b_it;
+        }
+        umma_commit(smem_u32(&bars.done));
+        ++pp.passes;
+      }
+    }
+    return;
+  }
+  if (warp < kEpiWarps) {
+    const int q = warp & 3, r = q * 32 + lane;  // TMEM lane quarter; row of C
+    const int h = warp >> 2;                    // column half of each pass
+    const int mrows = V.dim(M), ncols = V.dim(Nn);
+    double* C = V.ptr(M, Nn);
+    const int ea = (r < mrows) ? __ldcg(P.rexp + tA * emu::kEdge + r) : emu::kEmptyRow;
+    const bool row_ok = r < mrows && ea != emu::kEmptyRow;
+    // C is read a chunk ahead of the one being composed (its loads in flight during the TMEM reads
+    // and the composition); stores go last, so no load waits on an earlier store
+    auto loadc = [&](double (&dst)[8], int pass, int cc) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int col = pass * 64 + h * 32 + cc + j;
+        dst[j] = (row_ok && col < ncols && (!syrk || r >= col)) ? __ldcg(C + r + (long long)col * V.ld) : 0.0;
+      }
+    };
+    double cur[8], nxt[8];
+    loadc(cur, 0, 0);
+    for (int pass = 0; pass < 2; ++pass) {
+      if (!mbar_wait(smem_u32(&bars.done), pp.passes & 1, err, P.timeout_ns)) return;
+      tc_fence_after();
+      for (int cc = 0; cc < 32; cc += 8) {
+        uint32_t v[emu::kSlices][8];
+#pragma unroll
+        for (int g = 0; g < emu::kSlices; ++g)
+          tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * 64 + h * 32 + cc), v[g]);
+        if (cc + 8 < 32) loadc(nxt, pass, cc + 8);
+        else if (pass == 0) loadc(nxt, 1, 0);
+        tmem_ld_wait();
+        double res[8];
+        bool odd = false;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          uint32_t acc[emu::kSlices];
+#pragma unroll
+          for (int g = 0; g < emu::kSlices; ++g) acc[g] = v[g][j];
+          bool o;
+          res[j] = emu::compose(acc, ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62, &o);
+          odd |= o;
+        }
+        if (odd) {  // a result outside the normal FP64 range (extreme scales only)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            uint32_t acc[emu::kSlices];
+#pragma unroll
+            for (int g = 0; g < emu::kSlices; ++g) acc[g] = v[g][j];
+            res[j] = emu::compose_slow(acc, ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int col = pass * 64 + h * 32 + cc + j;
+          if (row_ok && col < ncols && (!syrk || r >= col)) __stcg(C + r + (long long)col * V.ld, cur[j] - res[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) cur[j] = nxt[j];
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&bars.tmem_free));
+      ++pp.passes;
+    }
+  }
+}
+
 // Persistent executor: one CTA per SM takes tasks from the ready queue in order.
 // Counter protocol (writers of block (M,N) in order: GEMM(M,N,0..N-1), then TRSM(M,N); of (M,M):
 // SYRK(0..M-1,M), then POTRF(M)):
@@ -117,17 +316,51 @@ __device__ __forceinline__ void release_columns(const DagParams& P) {
 //   TRSM(M,K):     cnt(K,K) >= K+1, cnt(M,K) >= K
 //   SYRK(K,M):     cnt(M,K) >= K+1, cnt(M,M) >= K
 //   GEMM(M,N,K):   cnt(M,K) >= K+1, cnt(N,K) >= K+1, cnt(M,N) >= K
-__global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P) {
-  extern __shared__ __align__(16) double smem[];
+// kEmu: SYRK and GEMM run on the tensor cores (emu_update) from the digit planes that each TRSM
+// writes of its block before it signals; POTRF and TRSM stay FP64.
+template <bool kEmu>
+__global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
+    potrf_dag_f64_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, DagParams P) {
+  extern __shared__ __align__(1024) uint8_t dsmem_raw[];
+  uint8_t* dsmem = kEmu ? (uint8_t*)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023) : dsmem_raw;
+  double* smem = (double*)dsmem;
   __shared__ long long s_task;
-  __shared__ int s_go;
+  __shared__ int s_go, s_failed;
+  __shared__ __align__(8) emuk::Bars bars;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_aux[2 * kBlk];
   const BlockView& V = P.V;
   const int NTb = P.NTb;
+  const int warp = threadIdx.x >> 5;
+  emuk::Pipe pp;
+  uint32_t tmem = 0;
+  if (kEmu) {
+    if (threadIdx.x == 0) {
+      using namespace tc;
+      for (int i = 0; i < emuk::kASlots; ++i) {
+        mbar_init(smem_u32(&bars.a_full[i]), 1);
+        mbar_init(smem_u32(&bars.a_empty[i]), emuk::kIssuers);
+      }
+      for (int i = 0; i < emuk::kBBufs; ++i) {
+        mbar_init(smem_u32(&bars.b_full[i]), 1);
+        mbar_init(smem_u32(&bars.b_empty[i]), emuk::kIssuers);
+      }
+      mbar_init(smem_u32(&bars.done), emuk::kIssuers);
+      mbar_init(smem_u32(&bars.tmem_free), emuk::kEpiWarps);
+      for (int i = 0; i < emuk::kIssuers; ++i) mbar_init(smem_u32(&bars.fin[i]), 1);
+      mbar_fence_init();
+    }
+    if (warp == emuk::kIssuerWarp0) tc::tmem_alloc(tc::smem_u32(&tmem_slot), emuk::kTmemCols);
+    __syncthreads();
+    tc::tc_fence_after();
+    tmem = tmem_slot;
+  }
   for (;;) {
     if (threadIdx.x == 0) {
       long long t = -1;
       if (!ld_volatile(&P.st->abort)) t = (long long)atomicAdd(&P.st->head, 1ULL);
       s_task = (t >= 0 && t < P.ntasks) ? t : -1;
+      s_failed = 0;
     }
     __syncthreads();
     const long long t = s_task;
@@ -160,38 +393,49 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     if (!s_go) break;
     const uint64_t t_start = P.trace.buf ? globaltimer_ns() : 0;
     switch (tk.type) {
-      case T_POTRF: {
+      case T_POTRF: {  // the first 256 threads (all of them in the FP64 form)
         const int K = tk.a;
-        const int info = op_potrf<double>(V.ptr(K, K), V.ld, V.dim(K), smem);
-        if (info != 0) {
-          if (threadIdx.x == 0) {
+        if (threadIdx.x < kThreads) {
+          const int info = op_potrf<double, kEmu>(V.ptr(K, K), V.ld, V.dim(K), smem);
+          if (info != 0 && threadIdx.x == 0) {
             atomicCAS(&P.st->status, 0, K * V.b + info);
             atomicExch(&P.st->abort, 1);
             release_columns(P);
+            s_failed = 1;
           }
-          __syncthreads();
-          return;
         }
         target = P.cnt + tri_index(K, K, NTb);
         break;
       }
       case T_TRSM: {
         const int M = tk.a, K = tk.b;
-        op_trsm<double>(V.ptr(K, K), V.ld, V.ptr(M, K), V.ld, V.dim(M), V.dim(K), smem);
+        if (threadIdx.x < kThreads) {
+          op_trsm<double, false, kEmu>(V.ptr(K, K), V.ld, V.ptr(M, K), V.ld, V.dim(M), V.dim(K), smem);
+          if (kEmu) {
+            // the block is final in global memory (each thread's own writes before the barrier)
+            asm volatile("bar.sync 1, 256;" ::: "memory");
+            const long long tb = tri_index(M, K, NTb);
+            emu::slice_block(V.ptr(M, K), V.ld, V.dim(M), V.dim(K), P.planes + tb * emu::kBlockElems,
+                             P.rexp + tb * emu::kEdge, s_aux);
+          }
+        }
         target = P.cnt + tri_index(M, K, NTb);
         break;
       }
       case T_SYRK: {
         const int K = tk.a, M = tk.b;
         const double* a = V.ptr(M, K);
-        if (V.b <= 64) op_gemm_nt<double, true>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
+        if (kEmu) emu_update(&tmA, &tmB, P, M, M, K, true, dsmem, bars, pp, tmem, s_aux);
+        else if (V.b <= 64) op_gemm_nt<double, true>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
         else op_gemm_nt<double>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
         target = P.cnt + tri_index(M, M, NTb);
         break;
       }
       default: {
         const int M = tk.a, Nn = tk.b, K = tk.c;
-        if (V.b <= 64)
+        if (kEmu)
+          emu_update(&tmA, &tmB, P, M, Nn, K, false, dsmem, bars, pp, tmem, s_aux);
+        else if (V.b <= 64)
           op_gemm_nt<double, true>(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn),
                                    V.dim(K), false, smem);
         else
@@ -202,7 +446,12 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
       }
     }
     __syncthreads();
+    if (s_failed) break;
     if (threadIdx.x == 0) {
+      if (kEmu && ld_volatile(&P.st->status) != 0) {  // a pipeline wait gave up: stop the launch
+        atomicExch(&P.st->abort, 1);  // (every thread leaves at the next fetch)
+        continue;
+      }
       trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);  // end stamp before any waiter can start
       signal_done(target);
       if (P.col_done && (tk.type == T_POTRF || tk.type == T_TRSM)) {  // block (a, b) of L is final
@@ -215,6 +464,33 @@ __global__ void __launch_bounds__(kThreads, 1) potrf_dag_f64_kernel(DagParams P)
     }
   }
   if (threadIdx.x == 0) release_columns(P);
+  if (kEmu) {
+    using namespace tc;
+    // after an early stop: let this CTA's copies and products in flight land (bounded waits) before
+    // the shared memory and the accumulators are released
+    if (warp == emuk::kProducerWarp && (threadIdx.x & 31) == 0) {
+      for (uint32_t sl = 0; sl < emuk::kASlots; ++sl)
+        if (pp.a_it > sl) {
+          const uint32_t last = sl + emuk::kASlots * ((pp.a_it - 1 - sl) / emuk::kASlots);
+          mbar_wait(smem_u32(&bars.a_full[sl]), (last / emuk::kASlots) & 1, nullptr, P.timeout_ns);
+        }
+      for (uint32_t bb = 0; bb < emuk::kBBufs; ++bb)
+        if (pp.b_it > bb) {
+          const uint32_t last = bb + emuk::kBBufs * ((pp.b_it - 1 - bb) / emuk::kBBufs);
+          mbar_wait(smem_u32(&bars.b_full[bb]), (last / emuk::kBBufs) & 1, nullptr, P.timeout_ns);
+        }
+    }
+    if (warp >= emuk::kIssuerWarp0 && (threadIdx.x & 31) == 0 && pp.mma_issued) {
+      umma_commit(smem_u32(&bars.fin[warp - emuk::kIssuerWarp0]));
+      mbar_wait(smem_u32(&bars.fin[warp - emuk::kIssuerWarp0]), 0, nullptr, P.timeout_ns);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == emuk::kIssuerWarp0) {
+      tc_fence_after();
+      tmem_dealloc(tmem, emuk::kTmemCols);
+    }
+  }
 }
 
 // ---- single-purpose grids for the tile-level entry points ------------------------------------
@@ -496,8 +772,11 @@ int device_info(DevInfo& out) {
   if (dev >= 32) return GBX_ERR_CUDA;
   if (!d.attrs_set) {
     if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBX_ERR_CUDA;
-    if (cudaFuncSetAttribute(potrf_dag_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(potrf_dag_f64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kDagSmemBytes) != cudaSuccess)
+      return GBX_ERR_CUDA;
+    if (cudaFuncSetAttribute(potrf_dag_f64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)emuk::kSmemBytes) != cudaSuccess)
       return GBX_ERR_CUDA;
     if (cudaFuncSetAttribute(gemm_nt_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(4 * kKC * kBlk * sizeof(double))) != cudaSuccess)
@@ -506,7 +785,7 @@ int device_info(DevInfo& out) {
                              (int)(op_trsm_smem_elems<double>() * sizeof(double))) != cudaSuccess)
       return GBX_ERR_CUDA;
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, potrf_dag_f64_kernel, kThreads, kDagSmemBytes) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, potrf_dag_f64_kernel<false>, kThreads, kDagSmemBytes) !=
         cudaSuccess)
       return GBX_ERR_CUDA;
     d.dag_blocks_per_sm = std::max(1, occ);
@@ -542,14 +821,35 @@ size_t dag_workspace_bytes(int NTb) {
   return sizeof(DagState) + ((counters + 255) / 256) * 256;
 }
 
+// FP64 update mode of the tiled executor (gbx_set_fp64_update): 0 FP64 FMA block GEMMs, 1 the
+// tensor-core emulation (128-blocks only; other block edges run the FP64 FMA form)
+int g_fp64_update = 0;
+bool emu_active(const BlockView& V) { return g_fp64_update == 1 && V.b == kBlk; }
+
+// workspace of an emulated run, after the counters: row exponents (128 per lower block), then the
+// digit planes (7 x 128 x 128 bf16 per lower block), both indexed by tri_index
+size_t emu_rexp_offset(int NTb) { return (dag_workspace_bytes(NTb) + 1023) / 1024 * 1024; }
+size_t emu_planes_offset(int NTb) {
+  const size_t ntri = (size_t)NTb * (NTb + 1) / 2;
+  return (emu_rexp_offset(NTb) + ntri * emu::kEdge * sizeof(int) + 1023) / 1024 * 1024;
+}
+size_t emu_workspace_bytes(int NTb) {
+  const size_t ntri = (size_t)NTb * (NTb + 1) / 2;
+  return emu_planes_offset(NTb) + ntri * (size_t)emu::kBlockElems * sizeof(uint16_t);
+}
+size_t executor_workspace_bytes(const BlockView& V, int NTb) {
+  return emu_active(V) ? emu_workspace_bytes(NTb) : dag_workspace_bytes(NTb);
+}
+
 int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaStream_t s, long long first_task,
                uint64_t timeout_ns, int* col_done = nullptr, volatile int* host_flag = nullptr,
-               int group_blocks = 1) {
-  const size_t need = dag_workspace_bytes(NTb);
+               int group_blocks = 1, bool allow_emu = true) {
+  const bool emu = allow_emu && emu_active(V);
+  const size_t need = emu ? emu_workspace_bytes(NTb) : dag_workspace_bytes(NTb);
   if (work == nullptr || work_bytes < need) return GBX_ERR_WORKSPACE;
   DevInfo di;
   if (int e = device_info(di)) return e;
-  if (cudaMemsetAsync(work, 0, need, s) != cudaSuccess) return GBX_ERR_CUDA;
+  if (cudaMemsetAsync(work, 0, dag_workspace_bytes(NTb), s) != cudaSuccess) return GBX_ERR_CUDA;
   DagState* st = (DagState*)work;
   if (first_task) set_head_kernel<<<1, 32, 0, s>>>(st, (unsigned long long)first_task);
   DagParams P;
@@ -564,9 +864,22 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   P.host_flag = host_flag;
   P.group_blocks = group_blocks;
   P.groups = (NTb + group_blocks - 1) / group_blocks;
-  long long grid = (long long)di.sms * di.dag_blocks_per_sm;
+  P.planes = nullptr;
+  P.rexp = nullptr;
+  CUtensorMap ta, tb;
+  memset(&ta, 0, sizeof(ta));
+  memset(&tb, 0, sizeof(tb));
+  if (emu) {
+    P.rexp = (int*)((char*)work + emu_rexp_offset(NTb));
+    P.planes = (uint16_t*)((char*)work + emu_planes_offset(NTb));
+    const uint64_t rows = (uint64_t)NTb * (NTb + 1) / 2 * emu::kSlices * emu::kEdge;
+    if (int e = tc::make_tmap_kmajor_bf16(&ta, P.planes, rows, emu::kEdge, emu::kEdge, 128)) return e;
+    if (int e = tc::make_tmap_kmajor_bf16(&tb, P.planes, rows, emu::kEdge, emu::kEdge, 64)) return e;
+  }
+  long long grid = (long long)di.sms * (emu ? 1 : di.dag_blocks_per_sm);
   grid = std::max(1LL, std::min(grid, P.ntasks));
-  potrf_dag_f64_kernel<<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(P);
+  if (emu) potrf_dag_f64_kernel<true><<<(unsigned)grid, emuk::kThreadsEmu, emuk::kSmemBytes, s>>>(ta, tb, P);
+  else potrf_dag_f64_kernel<false><<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(ta, tb, P);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
@@ -653,7 +966,8 @@ int gbx_dpotrf_tile(int n, double* A, int lda, void* work, size_t work_bytes, in
   if (n == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
   const BlockView V = plain_view(n, A, lda);
   const int NTb = (n + V.b - 1) / V.b;
-  if (int e = launch_dag(V, NTb, work, work_bytes, s, 0, gbx_get_wait_timeout_ns())) return e;
+  if (int e = launch_dag(V, NTb, work, work_bytes, s, 0, gbx_get_wait_timeout_ns(), nullptr, nullptr, 1, false))
+    return e;
   copy_info_kernel<<<1, 32, 0, s>>>((const DagState*)work, devInfo);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
@@ -713,9 +1027,16 @@ int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes) {
   const int b = dag_block_edge(N, NB);
   if (b == 0) return GBX_ERR_ARG;
   const int NTb = std::max(1, (N + b - 1) / b);
-  *bytes = dag_workspace_bytes(NTb);
+  *bytes = executor_workspace_bytes(tiled_view(std::max(N, 1), NB, nullptr), NTb);
   return GBX_OK;
 }
+
+int gbx_set_fp64_update(int mode) {
+  if (mode != 0 && mode != 1) return GBX_ERR_ARG;
+  g_fp64_update = mode;
+  return GBX_OK;
+}
+int gbx_get_fp64_update(void) { return g_fp64_update; }
 
 int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream) {
   if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
@@ -1002,7 +1323,8 @@ int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* s
   void* scratch = nullptr;
   if (int e = noalloc_scratch(&scratch)) return e;
   // launch_dag clears the header and the counters this run uses (cudaMemsetAsync, no allocation)
-  if (int e = launch_dag(V, NTb, scratch, kNoAllocBytes, s, 0, gbx_get_wait_timeout_ns())) return e;
+  if (int e = launch_dag(V, NTb, scratch, kNoAllocBytes, s, 0, gbx_get_wait_timeout_ns(), nullptr, nullptr, 1, false))
+    return e;
   copy_info_kernel<<<1, 32, 0, s>>>((const DagState*)scratch, devInfo);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
@@ -1014,7 +1336,7 @@ int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_byte
   cudaStream_t s = (cudaStream_t)stream;
   const BlockView V = tiled_view(2 * NB, NB, tiles);
   // skip task 0 (POTRF(0)): TRSM(1,0) then waits for a counter nothing will ever move
-  if (int e = launch_dag(V, 2, work, work_bytes, s, 1, timeout_ns)) return e;
+  if (int e = launch_dag(V, 2, work, work_bytes, s, 1, timeout_ns, nullptr, nullptr, 1, false)) return e;
   return gbx_dpotrf_tiled_status(work, stream);
 }
 
