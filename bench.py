@@ -43,6 +43,9 @@ def parse():
     p.add_argument("--NB", type=int, default=512)
     p.add_argument("--nrhs", type=int, default=1)
     p.add_argument("--cpu-N", type=int, default=16384, help="bounded CPU sample size")
+    p.add_argument("--fp64-update", choices=["tensor", "fma"], default="tensor",
+                   help="trailing updates of the FP64 factor: tensor-core emulation (exact digit-plane "
+                        "products, FP64 accumulation) or FP64 FMA block GEMMs")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision configuration")
@@ -50,7 +53,7 @@ def parse():
     p.add_argument("--only-main", action="store_true",
                    help="the headline step alone (no e2e, secondary configurations or CPU baseline), e.g. for a "
                         "launch-list capture")
-    p.add_argument("--profile-case", choices=["dag", "mixed", "batched", "refine", "batched_mixed"], default=None,
+    p.add_argument("--profile-case", choices=["dag", "emu", "mixed", "batched", "refine", "batched_mixed"], default=None,
                    help="run one small case of one kernel (N=8192) for an ncu capture; prints no JSON")
     p.add_argument("--profile-N", type=int, default=8192, help="matrix order of --profile-case dag/mixed")
     return p.parse_args()
@@ -241,6 +244,8 @@ def run_ours(args, ws, rank, local):
     b_host = torch.from_numpy(np.random.default_rng(42).standard_normal((nrhs, N)))
     b0 = b_host.to(dev)
     X = torch.empty_like(b0)
+    tensor_update = args.fp64_update == "tensor"
+    assert gbx.lib().gbx_set_fp64_update(1 if tensor_update else 0) == 0
     work = torch.empty(gbx.potrf_workspace_bytes(N, NB), dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
@@ -291,24 +296,34 @@ def run_ours(args, ws, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": main_config(args, ws),
+        "fp64_update": FP64_UPDATE_NOTE[args.fp64_update],
         "backward_error": berr,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
     }
 
     peak = measure_fp64_gemm_peak(dev)
+    bf16_peak, bf16_src = measured_bf16_peak()
     dag_s = statistics.mean(dag_ms) * 1e-3
     achieved = flops_factor(N) / dag_s / 1e12
-    # DRAM traffic of one launch: ncu capture at N=16384 NB=512 (45.007 GB read + 44.713 GB written),
-    # scaled to this N by the number of block tasks (~N^3); N=32768 is too large to capture
-    traffic = (45.007e9 + 44.713e9) * (N / 16384.0) ** 3 if NB == 512 else None
-    line["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                        "frac": achieved / peak, "traffic": traffic,
-                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
-                                          "N=16384 NB=512, scaled by block tasks (N^3)",
-                        "kernel": "potrf_dag_f64_kernel",
-                        "peak_source": "cuBLAS FP64 GEMM 4096^3 measured in this run (no FP64 entry in the "
-                                       "measured-peaks file)"}
+    if tensor_update:
+        line["roofline"] = tensor_roofline(N, NB, dag_s, bf16_peak, bf16_src)
+        line["roofline"]["fp64_equivalent"] = {"tflops": achieved, "fp64_gemm_peak": peak,
+                                               "ratio": achieved / peak}
+        if not args.only_main:  # the same step with FP64 FMA block GEMMs (the former form), once
+            line["fma_update"] = run_fma_step(gbx, A0, T, X, b0, N, NB, nrhs, sp, peak)
+            assert gbx.lib().gbx_set_fp64_update(1) == 0
+    else:
+        # DRAM traffic of one launch: ncu capture at N=16384 NB=512 (45.007 GB read + 44.713 GB
+        # written), scaled to this N by the number of block tasks (~N^3); N=32768 is too large to capture
+        traffic = (45.007e9 + 44.713e9) * (N / 16384.0) ** 3 if NB == 512 else None
+        line["roofline"] = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                            "frac": achieved / peak, "traffic": traffic,
+                            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at "
+                                              "N=16384 NB=512, scaled by block tasks (N^3)",
+                            "kernel": "potrf_dag_f64_kernel<false>",
+                            "peak_source": "cuBLAS FP64 GEMM 4096^3 measured in this run (no FP64 entry in the "
+                                           "measured-peaks file)"}
 
     if not args.no_e2e:
         line["e2e"] = run_e2e(gbx, A0, b0, N, NB, nrhs, work, dev, reps=max(1, min(args.steps, 2)))
@@ -335,11 +350,70 @@ def run_ours(args, ws, rank, local):
                                 "cores": cpu_cores(), "kind": "port",
                                 "sample": "N=%d NB=%d factor+solve, best of 2, %s tile kernels" %
                                           (args.cpu_N, NB, "OpenBLAS" if blas else "plain-loop")}
-    bf16_peak, bf16_src = measured_bf16_peak()
     add_roofline_fractions(line, peak, bf16_peak)
     line["peaks"]["bf16_source"] = bf16_src
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+FP64_UPDATE_NOTE = {
+    "tensor": "tensor-core emulation: each 128-block of L as 7 bf16 digit planes (8-bit digits, power-of-two "
+              "row scales), the 28 plane products of the leading digit groups exact in FP32 on tcgen05, "
+              "composed exactly and subtracted from C with one FP64 add; POTRF/TRSM in FP64",
+    "fma": "FP64 FMA block GEMMs",
+}
+
+# tensor-core work of one emulated GEMM or SYRK task (128 x 128 output, k = 128): two passes of 64
+# columns, each 28 plane pairs x 2 chunks x 4 MMAs of 128 x 64 x 16
+EMU_TASK_FLOPS = 2 * 28 * 2 * 4 * (2 * 128 * 64 * 16)
+
+
+def tensor_roofline(N, NB, seconds, bf16_peak, bf16_src):
+    """Roofline of the emulated executor: the tensor-core flops its GEMM/SYRK tasks issue per launch
+    (EMU_TASK_FLOPS each) over the launch time, against the measured dense bf16 rate. DRAM traffic:
+    ncu capture of one launch at N=16384 (EMU_TRAFFIC_16384), scaled by the number of update tasks."""
+    ntb = -(-N // 128)
+    updates = ntb * (ntb - 1) // 2 + ntb * (ntb - 1) * (ntb - 2) // 6
+    flops = updates * EMU_TASK_FLOPS
+    achieved = flops / seconds / 1e12
+    ntb16 = 128
+    upd16 = ntb16 * (ntb16 - 1) // 2 + ntb16 * (ntb16 - 1) * (ntb16 - 2) // 6
+    traffic = EMU_TRAFFIC_16384 * updates / upd16 if EMU_TRAFFIC_16384 else None
+    return {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": achieved / bf16_peak, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at N=16384 NB=512, "
+                              "scaled by the number of update tasks",
+            "kernel": "potrf_dag_f64_kernel<true>", "peak_source": bf16_src + " (of measured)",
+            "flops_per_launch": flops, "update_tasks": updates}
+
+
+# bytes per launch (read + write) at N=16384 NB=512: ncu dram__bytes_read.sum 48.002 GB +
+# dram__bytes_write.sum 47.868 GB (bench.py --profile-case emu --profile-N 16384, second launch)
+EMU_TRAFFIC_16384 = 48.001771008e9 + 47.867822080e9
+
+
+def run_fma_step(gbx, A0, T, X, b0, N, NB, nrhs, sp, fp64_peak):
+    """One factor + solve step of the same system with the FP64 FMA update form (after the timed region)."""
+    import ctypes
+
+    import torch
+    assert gbx.lib().gbx_set_fp64_update(0) == 0
+    work = torch.empty(gbx.potrf_workspace_bytes(N, NB), dtype=torch.uint8, device=T.device)
+    T.copy_(A0)
+    X.copy_(b0)
+    e0, e1, e2 = _events() + (torch.cuda.Event(enable_timing=True),)
+    e0.record()
+    gbx.call("gbx_dpotrf_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(work.data_ptr()),
+             work.numel(), sp)
+    e1.record()
+    gbx.call("gbx_dpotrs_tiled", N, NB, ctypes.c_void_p(T.data_ptr()), nrhs, ctypes.c_void_p(X.data_ptr()), N, sp)
+    e2.record()
+    e2.synchronize()
+    assert gbx.potrf_status(work) == 0
+    ms, dag = e0.elapsed_time(e2), e0.elapsed_time(e1)
+    return {"ms_per_step": ms, "tflops": flops_factor(N) / (ms * 1e-3) / 1e12,
+            "factor_ms": dag, "factor_frac_of_fp64_peak": flops_factor(N) / (dag * 1e-3) / 1e12 / fp64_peak,
+            "kernel": "potrf_dag_f64_kernel<false>"}
 
 
 def measured_bf16_peak():
@@ -818,22 +892,28 @@ def run_ttg_flowgraph(gbx, dev, N=16384, NB=512, iters=2, chain_tasks=20000):
     out["flowgraph_N4096"] = flowgraph(4096, [])
     out["flowgraph_N4096_device_queue"] = flowgraph(4096, ["-q"])
     gfs = out["flowgraph"]["gflops_per_iter"]
-    # the same factorisation by the persistent executor, device time
+    # the same factorisation by the persistent executor, device time: with FP64 FMA updates (the
+    # flowgraph's tile bodies are FP64 FMA kernels too), and with the tensor-core updates
     t = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
     gbx.plgsy(t, N, NB, N, 3872)
-    work = gbx.potrf_tiled(t.clone(), N, NB)
-    T = t.clone()
-    torch.cuda.synchronize()
-    e0, e1 = _events()
-    e0.record()
-    gbx.potrf_tiled(T, N, NB, workspace=work, check=False)
-    e1.record()
-    e1.synchronize()
-    exe_ms = e0.elapsed_time(e1)
-    out["executor"] = {"ms": exe_ms, "tflops": flops_factor(N) / (exe_ms * 1e-3) / 1e12}
+    mode0 = gbx.lib().gbx_get_fp64_update()
+    for key, mode in (("executor", 0), ("executor_tensor_updates", 1)):
+        assert gbx.lib().gbx_set_fp64_update(mode) == 0
+        work = gbx.potrf_tiled(t.clone(), N, NB)
+        T = t.clone()
+        torch.cuda.synchronize()
+        e0, e1 = _events()
+        e0.record()
+        gbx.potrf_tiled(T, N, NB, workspace=work, check=False)
+        e1.record()
+        e1.synchronize()
+        exe_ms = e0.elapsed_time(e1)
+        out[key] = {"ms": exe_ms, "tflops": flops_factor(N) / (exe_ms * 1e-3) / 1e12}
+        del T, work
+    gbx.lib().gbx_set_fp64_update(mode0)
     if gfs:
         out["flowgraph_vs_executor"] = out["flowgraph"]["tflops"] / out["executor"]["tflops"]
-    del t, T, work
+    del t
     chain = gb.build_chain()
     out["chain"] = {}
     for flows in (0, 1):
@@ -906,11 +986,12 @@ def profile_case(case, N=8192):
         B = torch.from_numpy(workloads.rhs(N, 8, 42)).to(dev)
         X, info, st = gbx.dposv_mixed(A, N, NB, B, prec="fp16", tol=1e-14)
         assert st == 0, info
-    elif case in ("dag", "mixed"):
+    elif case in ("dag", "emu", "mixed"):
+        assert gbx.lib().gbx_set_fp64_update(1 if case == "emu" else 0) == 0
         A = torch.empty(gbx.tiled_numel(N, NB), dtype=torch.float64, device=dev)
         gbx.gen_uniform_sym(A, N, NB, seed=42)
         for _ in range(2):  # the second launch is the captured one (-s 1 -c 1), or both (-c 2)
-            if case == "dag":
+            if case in ("dag", "emu"):
                 gbx.potrf_tiled(A.clone(), N, NB)
             else:
                 W, work, st, cond = gbx.potrf_mixed(A, N, NB, prec="bf16")

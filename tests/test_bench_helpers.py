@@ -36,3 +36,13 @@ def test_roofline_fractions_of_secondary_configurations():
 def test_measured_bf16_peak_has_a_source():
     peak, src = bench.measured_bf16_peak()
     assert peak > 100.0 and isinstance(src, str) and src
+
+
+def test_tensor_roofline_counts_the_update_tasks():
+    """One emulated update task issues 2 passes x 28 plane pairs x 2 chunks x 4 MMAs of 128 x 64 x 16."""
+    assert bench.EMU_TASK_FLOPS == 2 * 28 * 2 * 4 * 2 * 128 * 64 * 16
+    r = bench.tensor_roofline(256, 256, 1e-3, 1906.1, "test")  # 2 blocks: one SYRK, no GEMM
+    assert r["update_tasks"] == 1 and r["flops_per_launch"] == bench.EMU_TASK_FLOPS
+    r = bench.tensor_roofline(32768, 512, 1.0, 1906.1, "test")  # 256 blocks
+    assert r["update_tasks"] == 256 * 255 // 2 + 256 * 255 * 254 // 6
+    assert abs(r["frac"] - r["achieved"] / 1906.1) < 1e-12 and r["bound"] == "tensor"
