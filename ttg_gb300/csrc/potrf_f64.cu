@@ -121,6 +121,54 @@ __device__ __forceinline__ void release_columns(const DagParams& P) {
   }
 }
 
+// the counters a task waits on: up to three (counter, target) pairs
+__device__ __forceinline__ int dag_deps(const DagParams& P, const TaskKey& k, const int** c, int* v) {
+  const int NTb = P.NTb;
+  switch (k.type) {
+    case T_POTRF:
+      c[0] = P.cnt + tri_index(k.a, k.a, NTb), v[0] = k.a;
+      return 1;
+    case T_TRSM:
+      c[0] = P.cnt + tri_index(k.b, k.b, NTb), v[0] = k.b + 1;
+      c[1] = P.cnt + tri_index(k.a, k.b, NTb), v[1] = k.b;
+      return 2;
+    case T_SYRK:
+      c[0] = P.cnt + tri_index(k.b, k.a, NTb), v[0] = k.a + 1;
+      c[1] = P.cnt + tri_index(k.b, k.b, NTb), v[1] = k.a;
+      return 2;
+    default:
+      c[0] = P.cnt + tri_index(k.a, k.c, NTb), v[0] = k.c + 1;
+      c[1] = P.cnt + tri_index(k.b, k.c, NTb), v[1] = k.c + 1;
+      c[2] = P.cnt + tri_index(k.a, k.b, NTb), v[2] = k.c;
+      return 3;
+  }
+}
+// blocking (bounded) wait for every dependency; false when the run stopped
+__device__ __forceinline__ bool dag_deps_wait(const DagParams& P, const TaskKey& k) {
+  const int* c[3];
+  int v[3];
+  const int n = dag_deps(P, k, c, v);
+  for (int i = 0; i < n; ++i)
+    if (!wait_geq(c[i], v[i], P.st, P.timeout_ns)) return false;
+  return true;
+}
+// one non-blocking look at every dependency: relaxed loads issued together (an acquire each would
+// serialise them); the caller fences once they are all met
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey& k) {
+  const int* c[3];
+  int v[3];
+  const int n = dag_deps(P, k, c, v);
+  const int x0 = ld_relaxed_gpu(c[0]);
+  const int x1 = n > 1 ? ld_relaxed_gpu(c[1]) : v[1 % n];
+  const int x2 = n > 2 ? ld_relaxed_gpu(c[2]) : v[2 % n];
+  return x0 >= v[0] && (n < 2 || x1 >= v[1]) && (n < 3 || x2 >= v[2]);
+}
+
 // ---- the emulated update task: C(M,N) -= L(M,K) L(N,K)^T on the tensor cores -----------------
 // Two passes over the 64-column halves of C; each pass accumulates the 28 digit-plane products of
 // the seven groups g = i + j <= 6 into seven 128 x 64 FP32 accumulators in TMEM (448 columns), over
@@ -157,9 +205,38 @@ struct Pipe {  // pipeline positions, each kept by the one thread that uses it
 };
 }  // namespace emuk
 
+// The next task of the queue, taken while the current one runs (kEmu: by an epilogue warp while
+// the first pass's products run, or by the producer warp, idle in an FP64 task): decoded, and its dependencies looked at once without blocking (thread 0
+// waits for them, if they were not met, after the current task has signalled: a CTA never waits
+// on the task it runs itself). Called from a branch that no lane of a pipeline role has to
+// reconverge with before it finishes.
+struct Prefetch {
+  long long* next;  // -2 none taken, -1 queue empty, else the task index
+  int* ok;          // its dependencies were all met
+  TaskKey* key;
+};
+__device__ __noinline__ void prefetch_next(const DagParams& P, long long cur, const Prefetch& pf) {
+  if (cur + 1 >= P.ntasks) return;
+  long long tn = -1;
+  if (!ld_volatile(&P.st->abort)) tn = (long long)atomicAdd(&P.st->head, 1ULL);
+  int ok = 0;
+  if (tn >= 0 && tn < P.ntasks) {
+    const TaskKey kn = dag_decode(tn, P.NTb);
+    *pf.key = kn;
+    // one look (a polling loop here slowed the producer lane of the same warp more than it saved)
+    if (dag_deps_ready(P, kn)) {
+      __threadfence();  // acquire side of the producers' fence + counter increment
+      ok = 1;
+    }
+  }
+  *pf.ok = ok;
+  *pf.next = (tn >= 0 && tn < P.ntasks) ? tn : -1;
+}
+
 __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtensorMap* tmB, const DagParams& P,
                                            int M, int Nn, int K, bool syrk, uint8_t* smem, emuk::Bars& bars,
-                                           emuk::Pipe& pp, uint32_t tmem, int* s_cexp) {
+                                           emuk::Pipe& pp, uint32_t tmem, int* s_cexp, long long cur_task,
+                                           const Prefetch& pf) {
   using namespace emuk;
   using namespace tc;
   const BlockView& V = P.V;
@@ -260,6 +337,9 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
         dst[j] = (row_ok && col < ncols && (!syrk || r >= col)) ? __ldcg(C + r + (long long)col * V.ld) : 0.0;
       }
     };
+    // the next task, while the first pass's products run (this warp waits for them otherwise)
+    if (warp == kEpiWarps - 1 && lane == 0) prefetch_next(P, cur_task, pf);
+    __syncwarp();
     double cur[8], nxt[8];
     loadc(cur, 0, 0);
     for (int pass = 0; pass < 2; ++pass) {
@@ -324,8 +404,9 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
   extern __shared__ __align__(1024) uint8_t dsmem_raw[];
   uint8_t* dsmem = kEmu ? (uint8_t*)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023) : dsmem_raw;
   double* smem = (double*)dsmem;
-  __shared__ long long s_task;
-  __shared__ int s_go, s_failed;
+  __shared__ long long s_task, s_next;
+  __shared__ int s_go, s_failed, s_next_ok;
+  __shared__ TaskKey s_key, s_next_key;
   __shared__ __align__(8) emuk::Bars bars;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_aux[2 * kBlk];
@@ -355,41 +436,33 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
     tc::tc_fence_after();
     tmem = tmem_slot;
   }
+  // kEmu: the next task is taken while the current one runs (prefetch_next)
+  if (threadIdx.x == 0) s_next = -2;  // none prefetched
+  const Prefetch pf{&s_next, &s_next_ok, &s_next_key};
   for (;;) {
     if (threadIdx.x == 0) {
       long long t = -1;
-      if (!ld_volatile(&P.st->abort)) t = (long long)atomicAdd(&P.st->head, 1ULL);
+      bool ready = false;
+      if (s_next != -2) {
+        t = s_next;
+        ready = s_next_ok != 0;
+      } else if (!ld_volatile(&P.st->abort)) {
+        t = (long long)atomicAdd(&P.st->head, 1ULL);
+      }
       s_task = (t >= 0 && t < P.ntasks) ? t : -1;
       s_failed = 0;
+      s_next = -2;
+      if (s_task >= 0) {
+        const TaskKey k = ready ? s_next_key : dag_decode(s_task, NTb);
+        s_key = k;
+        s_go = ready ? 1 : (dag_deps_wait(P, k) ? 1 : 0);
+      }
     }
     __syncthreads();
     const long long t = s_task;
     if (t < 0) break;
-    const TaskKey tk = dag_decode(t, NTb);
+    const TaskKey tk = s_key;
     int* target;
-    if (threadIdx.x == 0) {
-      bool ok = true;
-      switch (tk.type) {
-        case T_POTRF:
-          ok = wait_geq(P.cnt + tri_index(tk.a, tk.a, NTb), tk.a, P.st, P.timeout_ns);
-          break;
-        case T_TRSM:
-          ok = wait_geq(P.cnt + tri_index(tk.b, tk.b, NTb), tk.b + 1, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.a, tk.b, NTb), tk.b, P.st, P.timeout_ns);
-          break;
-        case T_SYRK:
-          ok = wait_geq(P.cnt + tri_index(tk.b, tk.a, NTb), tk.a + 1, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.b, tk.b, NTb), tk.a, P.st, P.timeout_ns);
-          break;
-        default:
-          ok = wait_geq(P.cnt + tri_index(tk.a, tk.c, NTb), tk.c + 1, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.b, tk.c, NTb), tk.c + 1, P.st, P.timeout_ns) &&
-               wait_geq(P.cnt + tri_index(tk.a, tk.b, NTb), tk.c, P.st, P.timeout_ns);
-          break;
-      }
-      s_go = ok;
-    }
-    __syncthreads();
     if (!s_go) break;
     const uint64_t t_start = P.trace.buf ? globaltimer_ns() : 0;
     switch (tk.type) {
@@ -403,6 +476,8 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
             release_columns(P);
             s_failed = 1;
           }
+        } else if (kEmu && threadIdx.x == 32 * emuk::kProducerWarp + 1) {
+          prefetch_next(P, t, pf);  // the producer warp has no role in an FP64 task
         }
         target = P.cnt + tri_index(K, K, NTb);
         break;
@@ -418,6 +493,8 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
             emu::slice_block(V.ptr(M, K), V.ld, V.dim(M), V.dim(K), P.planes + tb * emu::kBlockElems,
                              P.rexp + tb * emu::kEdge, s_aux);
           }
+        } else if (kEmu && threadIdx.x == 32 * emuk::kProducerWarp + 1) {
+          prefetch_next(P, t, pf);
         }
         target = P.cnt + tri_index(M, K, NTb);
         break;
@@ -425,7 +502,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       case T_SYRK: {
         const int K = tk.a, M = tk.b;
         const double* a = V.ptr(M, K);
-        if (kEmu) emu_update(&tmA, &tmB, P, M, M, K, true, dsmem, bars, pp, tmem, s_aux);
+        if (kEmu) emu_update(&tmA, &tmB, P, M, M, K, true, dsmem, bars, pp, tmem, s_aux, t, pf);
         else if (V.b <= 64) op_gemm_nt<double, true>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
         else op_gemm_nt<double>(a, V.ld, a, V.ld, V.ptr(M, M), V.ld, V.dim(M), V.dim(M), V.dim(K), true, smem);
         target = P.cnt + tri_index(M, M, NTb);
@@ -434,7 +511,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       default: {
         const int M = tk.a, Nn = tk.b, K = tk.c;
         if (kEmu)
-          emu_update(&tmA, &tmB, P, M, Nn, K, false, dsmem, bars, pp, tmem, s_aux);
+          emu_update(&tmA, &tmB, P, M, Nn, K, false, dsmem, bars, pp, tmem, s_aux, t, pf);
         else if (V.b <= 64)
           op_gemm_nt<double, true>(V.ptr(M, K), V.ld, V.ptr(Nn, K), V.ld, V.ptr(M, Nn), V.ld, V.dim(M), V.dim(Nn),
                                    V.dim(K), false, smem);
