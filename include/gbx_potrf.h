@@ -422,6 +422,13 @@ int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_byte
  * t < 0), or GBX_ERR_ARG. The orders are the executors' task lists, in which every task's
  * predecessors come earlier, so CTAs that take tasks in order cannot deadlock. */
 long long gbx_dag_task(int NTb, long long t, int* key);
+/* The same order with `lead` tasks of each step's trailing updates queued ahead of that step's
+ * TRSMs (the emulated executor's order; lead 0 is gbx_dag_task's). */
+long long gbx_dag_task_lead(int NTb, long long lead, long long t, int* key);
+/* Tasks of each step's trailing updates the executor queues ahead of the step's TRSMs: -1 (default)
+ * automatic (24 per CTA with tensor-core updates, none with FP64 FMA updates), else that count.
+ * Returns 0 or GBX_ERR_ARG. */
+int gbx_set_dag_lead(long long tasks);
 long long gbx_mixed_task(int NT, long long t, int* key);
 
 #ifdef __cplusplus

@@ -69,3 +69,30 @@ def test_order_argument_checks(gbx, fn):
     assert n == len(_expected(4))
     assert getattr(L, fn)(4, n, key) == gbx.GBX_ERR_ARG
     assert getattr(L, fn)(4, 0, None) == gbx.GBX_ERR_ARG
+
+
+@pytest.mark.parametrize("lead", [1, 3, 40, 10**9])
+@pytest.mark.parametrize("nt", [2, 5, 17, 33])
+def test_order_with_trailing_lead_is_complete_and_topological(gbx, nt, lead):
+    """The emulated executor's order: `lead` trailing tasks of each step ahead of its TRSMs."""
+    key = np.zeros(4, dtype=np.int32)
+    n = gbx.call("gbx_dag_task_lead", nt, lead, -1, None)
+    order = []
+    for t in range(n):
+        gbx.call("gbx_dag_task_lead", nt, lead, t, key.ctypes.data_as(ctypes.c_void_p))
+        order.append(tuple(int(v) for v in key))
+    assert len(order) == len(set(order)) and set(order) == _expected(nt)
+    pos = {t: i for i, t in enumerate(order)}
+    for t, i in pos.items():
+        for d in _deps(t):
+            assert pos[d] < i, (t, d)
+    if nt >= 5 and lead < 10**9:  # the leading trailing tasks really precede the step's TRSMs
+        k0 = [i for i, t in enumerate(order) if t == (TRSM, 2, 1, 0)][0]
+        assert order[k0 - 1][0] in (SYRK, GEMM)
+
+
+def test_dag_lead_setting(gbx):
+    L = gbx.lib()
+    assert L.gbx_set_dag_lead(-2) == gbx.GBX_ERR_ARG
+    assert L.gbx_dag_task_lead(4, -1, -1, None) == gbx.GBX_ERR_ARG
+    assert L.gbx_set_dag_lead(100) == 0 and L.gbx_set_dag_lead(-1) == 0

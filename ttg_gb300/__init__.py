@@ -87,6 +87,8 @@ SIGNATURES = {
     "gbx_dpotri_tiled": (_i, [_i, _i, _vp, _vp, _sz, _vp]),
     "gbx_split_f64": (_i, [_vp, _vp, _vp, ctypes.c_longlong, _vp]),
     "gbx_dag_task": (ctypes.c_longlong, [_i, ctypes.c_longlong, _vp]),
+    "gbx_dag_task_lead": (ctypes.c_longlong, [_i, ctypes.c_longlong, ctypes.c_longlong, _vp]),
+    "gbx_set_dag_lead": (_i, [ctypes.c_longlong]),
     "gbx_mixed_task": (ctypes.c_longlong, [_i, ctypes.c_longlong, _vp]),
     "gbx_dposv_tiled_host_bufferSize": (_i, [_i, _i, _szp]),
     "gbx_dposv_tiled_host": (_i, [_i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

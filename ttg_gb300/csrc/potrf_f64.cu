@@ -57,7 +57,10 @@ __host__ __device__ __forceinline__ long long dag_num_tasks(int NTb) {
   return NTb + seg_prefix(NTb - 1, NTb - 1);
 }
 
-__host__ __device__ inline TaskKey dag_decode(long long t, int NTb) {
+// lead > 0 (the emulated executor): the first `lead` tasks of each step's trailing part go ahead of
+// that step's TRSMs, so that the CTAs which take the TRSMs find their POTRF done instead of waiting
+// for it (the order stays topological: trailing tasks of step k need only TRSMs of step k - 1).
+__host__ __device__ inline TaskKey dag_decode(long long t, int NTb, long long lead = 0) {
   if (t < NTb) return t == 0 ? TaskKey{T_POTRF, 0, 0, 0} : TaskKey{T_TRSM, (int)t, 0, 0};
   const long long u = t - NTb, R = NTb - 1;
   int lo = 0, hi = NTb - 2;  // largest k with seg_prefix(k) <= u
@@ -72,8 +75,12 @@ __host__ __device__ inline TaskKey dag_decode(long long t, int NTb) {
   if (p == 0) return TaskKey{T_SYRK, k, k + 1, 0};
   if (p < r) return TaskKey{T_GEMM, k + 1 + (int)p, k + 1, k};
   if (p == r) return TaskKey{T_POTRF, k + 1, 0, 0};
-  if (p < 2 * (long long)r) return TaskKey{T_TRSM, k + 1 + (int)(p - r), k + 1, 0};
-  const long long pp = p - 2 * (long long)r, q = r - 1;  // trailing columns n = k+2 .. NTb-1
+  const long long q = r - 1;  // trailing columns n = k+2 .. NTb-1: q (q + 1) / 2 tasks
+  const long long X = lead < q * (q + 1) / 2 ? lead : q * (q + 1) / 2;
+  long long pp;
+  if (p <= r + X) pp = p - r - 1;  // the leading trailing tasks
+  else if (p < 2 * (long long)r + X) return TaskKey{T_TRSM, k + 1 + (int)(p - r - X), k + 1, 0};
+  else pp = p - 2 * (long long)r;
   int clo = 0, chi = (int)q - 1;                           // largest c with S(c) <= pp
   while (clo < chi) {
     const int mid = (clo + chi + 1) >> 1;
@@ -105,6 +112,7 @@ struct DagParams {
   // block, indexed by tri_index (diagonal blocks unused)
   uint16_t* planes;
   int* rexp;
+  long long lead;  // trailing tasks of a step queued ahead of its TRSMs (dag_decode)
 };
 
 // finished POTRF/TRSM blocks a group needs: block columns J of the group hold NTb - J blocks each
@@ -221,7 +229,7 @@ __device__ __noinline__ void prefetch_next(const DagParams& P, long long cur, co
   if (!ld_volatile(&P.st->abort)) tn = (long long)atomicAdd(&P.st->head, 1ULL);
   int ok = 0;
   if (tn >= 0 && tn < P.ntasks) {
-    const TaskKey kn = dag_decode(tn, P.NTb);
+    const TaskKey kn = dag_decode(tn, P.NTb, P.lead);
     *pf.key = kn;
     // one look (a polling loop here slowed the producer lane of the same warp more than it saved)
     if (dag_deps_ready(P, kn)) {
@@ -453,7 +461,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       s_failed = 0;
       s_next = -2;
       if (s_task >= 0) {
-        const TaskKey k = ready ? s_next_key : dag_decode(s_task, NTb);
+        const TaskKey k = ready ? s_next_key : dag_decode(s_task, NTb, P.lead);
         s_key = k;
         s_go = ready ? 1 : (dag_deps_wait(P, k) ? 1 : 0);
       }
@@ -901,6 +909,7 @@ size_t dag_workspace_bytes(int NTb) {
 // FP64 update mode of the tiled executor (gbx_set_fp64_update): 0 FP64 FMA block GEMMs, 1 the
 // tensor-core emulation (128-blocks only; other block edges run the FP64 FMA form)
 int g_fp64_update = 0;
+long long g_dag_lead = -1;  // gbx_set_dag_lead: -1 automatic
 bool emu_active(const BlockView& V) { return g_fp64_update == 1 && V.b == kBlk; }
 
 // workspace of an emulated run, after the counters: row exponents (128 per lower block), then the
@@ -955,6 +964,10 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   }
   long long grid = (long long)di.sms * (emu ? 1 : di.dag_blocks_per_sm);
   grid = std::max(1LL, std::min(grid, P.ntasks));
+  // emulated updates: a POTRF takes about twelve update tasks' time; 24 tasks per CTA ahead of each
+  // step's TRSMs measured best (N=32768: 0 -> 859 ms, 12/CTA 815, 24/CTA 796, 48/CTA 800). The FP64
+  // FMA form keeps its order (its update tasks take longer than a POTRF).
+  P.lead = g_dag_lead >= 0 ? g_dag_lead : (emu ? 24 * grid : 0);
   if (emu) potrf_dag_f64_kernel<true><<<(unsigned)grid, emuk::kThreadsEmu, emuk::kSmemBytes, s>>>(ta, tb, P);
   else potrf_dag_f64_kernel<false><<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(ta, tb, P);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
@@ -990,12 +1003,14 @@ using namespace gbx;
 
 extern "C" {
 
-long long gbx_dag_task(int NTb, long long t, int* key) {
-  if (NTb <= 0) return GBX_ERR_ARG;
+long long gbx_dag_task(int NTb, long long t, int* key) { return gbx_dag_task_lead(NTb, 0, t, key); }
+
+long long gbx_dag_task_lead(int NTb, long long lead, long long t, int* key) {
+  if (NTb <= 0 || lead < 0) return GBX_ERR_ARG;
   const long long n = dag_num_tasks(NTb);
   if (t >= n || (t >= 0 && !key)) return GBX_ERR_ARG;
   if (t >= 0) {
-    const TaskKey k = dag_decode(t, NTb);
+    const TaskKey k = dag_decode(t, NTb, lead);
     key[0] = k.type;
     key[1] = k.a;
     key[2] = k.b;
@@ -1114,6 +1129,12 @@ int gbx_set_fp64_update(int mode) {
   return GBX_OK;
 }
 int gbx_get_fp64_update(void) { return g_fp64_update; }
+
+int gbx_set_dag_lead(long long tasks) {
+  if (tasks < -1) return GBX_ERR_ARG;
+  g_dag_lead = tasks;
+  return GBX_OK;
+}
 
 int gbx_dpotrf_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream) {
   if (gbx::recording_stream(stream)) return GBX_ERR_ARG;  // not a CUDA stream
