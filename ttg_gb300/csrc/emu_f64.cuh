@@ -14,9 +14,9 @@
 // The groups g = 0..6 are kept (the dropped ones are below 2^-56 of the leading term). Each acc_g is
 // a sum of at most 7 * 128 products of magnitude <= 2^14: below 2^24 in magnitude, so the tensor
 // cores' FP32 accumulation of these integers is exact. Then
-//     sum_k A B = X 2^(eA_r + eB_c - 62),   X = sum_{g=0..6} acc_g 2^(8(6-g))   (an integer < 2^73),
-// rounded once to FP64 from the exact 128-bit X with integer instructions, and subtracted from C
-// with one FP64 add: two roundings in all, against k of them for the FP64 dot product.
+//     sum_k A B = X 2^(eA_r + eB_c - 62),   X = sum_{g=0..6} acc_g 2^(8(6-g))   (an integer < 2^70),
+// rounded once to FP64 from X with integer instructions, and subtracted from C with one FP64 add:
+// two roundings in all, against k of them for the FP64 dot product.
 //
 // Costs on GB300 (measured per SM per clock): FP64 add/FMA and every conversion to or from FP64
 // ~1.6-1.9, float->int ~15, integer ~60, FP32 ~113. Hence integer-only splitting and composing, and
@@ -97,26 +97,25 @@ __device__ __forceinline__ void slice_block(const double* __restrict__ L, int ld
   }
 }
 
-// X 2^E as FP64, X = sum_g acc_g 2^(8(6-g)) from the exact FP32 group sums; rounded to nearest
-// (ties away from zero) from the 64 leading bits of the exact 128-bit X. Branch-free, so that the
-// compositions of neighbouring elements interleave; *odd is set when the result leaves the normal
-// FP64 range (the value returned is then wrong: see compose_slow).
+// X 2^E as FP64, X = sum_g acc_g 2^(8(6-g)) from the exact FP32 group sums, rounded to nearest
+// (ties away from zero). X = H 2^32 + L with H = acc_0..2 (|H| < 2^38) and L = acc_3..6 (|L| < 2^49)
+// is formed in 64 bits: exactly while |H| < 2^30 (|X| < 2^62 + 2^49), else as X 2^-8, which drops
+// only bits below 2^-54 of |X| >= 2^62. Branch-free, so that the compositions of neighbouring
+// elements interleave; *odd is set when the result leaves the normal FP64 range (the value returned
+// is then wrong: see compose_slow).
 __device__ __forceinline__ double compose(const uint32_t (&acc)[kSlices], int E, bool* odd) {
-  long long a[kSlices];
+  int a[kSlices];
 #pragma unroll
   for (int g = 0; g < kSlices; ++g) a[g] = __float2int_rn(__uint_as_float(acc[g]));
-  const long long H = (a[0] << 16) + (a[1] << 8) + a[2];                    // |H| < 2^41
-  const long long L = (a[3] << 24) + (a[4] << 16) + (a[5] << 8) + a[6];     // |L| < 2^49
-  const __int128 X = ((__int128)H << 32) + (__int128)L;
+  const long long H = (long long)a[0] * 65536 + (long long)a[1] * 256 + (long long)a[2];
+  const long long L = (long long)a[3] * 16777216 + (long long)a[4] * 65536 + (long long)a[5] * 256 + (long long)a[6];
+  const int s = (H >= (1LL << 30) || H <= -(1LL << 30)) ? 8 : 0;
+  const long long X = (long long)((unsigned long long)H << (32 - s)) + (L >> s);
   const bool neg = X < 0;
-  const unsigned __int128 u = neg ? (unsigned __int128)(-X) : (unsigned __int128)X;
-  const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
-  const int zh = __clzll((long long)hi), zl = __clzll((long long)lo);
-  const int z = hi ? zh : 64 + zl;  // leading zeros of the 128 bits (128 for X = 0)
-  // the leading 64 bits, leading one at bit 63 (z <= 127 unless X = 0)
-  const unsigned __int128 ut = u << (z & 127);
-  const unsigned long long top = (unsigned long long)(ut >> 64);
-  int p = 127 - z;
+  const unsigned long long u = neg ? 0ull - (unsigned long long)X : (unsigned long long)X;
+  const int z = __clzll((long long)u);  // 64 for X = 0
+  const unsigned long long top = u << (z & 63);  // leading one at bit 63
+  int p = 63 - z + s;                            // position of X's leading one
   unsigned long long mant = (top >> 11) + ((top >> 10) & 1);  // 53 bits, rounded
   const bool carry = (mant >> 53) != 0;
   mant = carry ? (mant >> 1) : mant;
