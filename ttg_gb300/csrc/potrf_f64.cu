@@ -183,13 +183,14 @@ __device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey
 // two 64-wide chunks of k. Roles (warps of the 256-thread CTA):
 // The emulated executor runs 384 threads (twelve warps); its FP64 tasks use the first 256.
 //   warp 8 lane 0  TMA producer: per chunk the seven B planes (64 rows each) into one of two
-//                  buffers, then the A planes i = 6..0 (128 rows each) through a ring of six slots
-//   warps 9-11 lane 0  MMA issuers: for i = 6..0, j = 0..6-i: D[i+j] += A_i B_j^T (M128 N64 K16 x 4),
-//                  each issuer owning whole accumulator groups (so that every group's MMAs keep
-//                  their order): {6, 1}, {5, 2}, {4, 3, 0}, 9, 9 and 10 of the 28 pairs of a chunk.
-//                  One thread issues a tcgen05.mma only every ~110 clocks, while an N=64 product
-//                  takes the tensor pipe ~35: three issuers keep the pipe fed. Each A slot is
-//                  released after all three have committed its pairs, each B buffer after its chunk
+//                  buffers, then the A planes i = 0..6 (128 rows each) through a ring of six slots
+//   warp 9 lane 0  MMA issuer: for i = 0..6, k-steps 0..3: D[i..6] += A_i [B_0 .. B_(6-i)]^T as one
+//                  M128 x N(64 (7-i)) x K16 product (N at most 256 per instruction): the B planes of
+//                  a chunk are consecutive 64-row blocks of one K-major tile and the groups i + j
+//                  consecutive 64-column blocks of TMEM, so ten instructions per k-step cover the
+//                  28 plane pairs (one thread issues a tcgen05.mma only every ~110 clocks; an N=64
+//                  product takes the tensor pipe ~35). Each A slot is released after its
+//                  instructions, each B buffer after its chunk. Warps 10-11 have no part.
 //   warps 0-7      epilogue: TMEM lane quarter = warp % 4, column half = warp / 4; per element the
 //                  exact compose and one FP64 subtraction from C
 namespace emuk {
@@ -200,11 +201,8 @@ constexpr size_t kSmemBytes = (size_t)kBBufs * kBSetBytes + (size_t)kASlots * kA
 constexpr int kTmemCols = 512;
 constexpr int kThreadsEmu = 384;
 constexpr int kEpiWarps = 8, kProducerWarp = 8, kIssuerWarp0 = 9;
-constexpr int kIssuers = 3;  // MMA issuer threads: lane 0 of warps 9, 10, 11
-// accumulator groups of issuer k: bit g set in kGroups[k]
-__host__ __device__ constexpr uint32_t issuer_groups(int k) { return k == 0 ? 0x42u : k == 1 ? 0x24u : 0x19u; }
 struct Bars {
-  uint64_t a_full[kASlots], a_empty[kASlots], b_full[kBBufs], b_empty[kBBufs], done, tmem_free, fin[kIssuers];
+  uint64_t a_full[kASlots], a_empty[kASlots], b_full[kBBufs], b_empty[kBBufs], done, tmem_free, fin;
 };
 struct Pipe {  // pipeline positions, each kept by the one thread that uses it
   uint32_t a_it = 0, b_it = 0;  // producer: plane chunks issued; MMA issuer: consumed (A ring, B buffers)
@@ -272,7 +270,7 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
             tma_load_2d(bdst + j * kBBytes, tmB, smem_u32(&bars.b_full[bb]), c * 64,
                         (int)((tB * emu::kSlices + j) * emu::kEdge + pass * 64));
           ++pp.b_it;
-          for (int i = emu::kSlices - 1; i >= 0; --i) {
+          for (int i = 0; i < emu::kSlices; ++i) {
             const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
             if (!mbar_wait(smem_u32(&bars.a_empty[sl]), aph ^ 1, err, P.timeout_ns)) return;
             mbar_arrive_expect_tx(smem_u32(&bars.a_full[sl]), kABytes);
@@ -284,10 +282,8 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     }
     return;
   }
-  if (warp >= kIssuerWarp0) {
+  if (warp == kIssuerWarp0) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_f16(128, 64, true);
-      const uint32_t mine = issuer_groups(warp - kIssuerWarp0);
       // consumer positions: this thread's own copy of a_it / b_it, advanced through the same
       // sequence of plane chunks as the producer's
       uint32_t& a_it = pp.a_it;
@@ -302,21 +298,26 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
           if (!mbar_wait(smem_u32(&bars.b_full[bb]), bph, err, P.timeout_ns)) return;
           tc_fence_after();
           const uint32_t bbase = smem_u32(smB + (size_t)bb * kBSetBytes);
-          for (int i = emu::kSlices - 1; i >= 0; --i) {
+          for (int i = 0; i < emu::kSlices; ++i) {
             const uint32_t sl = a_it % kASlots, aph = (a_it / kASlots) & 1;
             if (!mbar_wait(smem_u32(&bars.a_full[sl]), aph, err, P.timeout_ns)) return;
             tc_fence_after();
             const uint64_t ad = desc_kmajor_sw128(smem_u32(smA + (size_t)sl * kABytes));
-            for (int j = 0; j + i < emu::kSlices; ++j) {
-              if (!((mine >> (i + j)) & 1)) continue;
-              const uint64_t bd = desc_kmajor_sw128(bbase + j * kBBytes);
-              const uint32_t d = tmem + (uint32_t)((i + j) * 64);
-              umma_f16(d, ad, bd, idesc, (c | j) != 0 ? 1u : 0u);
-              umma_f16(d, ad + 2, bd + 2, idesc, 1u);
-              umma_f16(d, ad + 4, bd + 4, idesc, 1u);
-              umma_f16(d, ad + 6, bd + 6, idesc, 1u);
-              pp.mma_issued = true;
+            // A_i against the B planes j = 0..6-i at once: the planes are consecutive 64-row blocks
+            // of one K-major tile, their groups i+j consecutive 64-column blocks of TMEM; at most
+            // four planes (N = 256) per instruction
+            const int np = emu::kSlices - i, n0 = np < 4 ? np : 4;
+            const uint32_t id0 = idesc_f16(128, 64 * n0, true), id1 = idesc_f16(128, 64 * (np - n0), true);
+            const uint64_t bd0 = desc_kmajor_sw128(bbase), bd1 = desc_kmajor_sw128(bbase + 4 * kBBytes);
+            const uint32_t d0 = tmem + (uint32_t)(i * 64), d1 = tmem + (uint32_t)((i + 4) * 64);
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              // i = 0 first touches every group: it alone starts the sums (chunk 0, k-step 0)
+              const uint32_t acc = (c | i | ks) != 0 ? 1u : 0u;
+              umma_f16(d0, ad + 2 * ks, bd0 + 2 * ks, id0, acc);
+              if (np > 4) umma_f16(d1, ad + 2 * ks, bd1 + 2 * ks, id1, acc);
             }
+            pp.mma_issued = true;
             umma_commit(smem_u32(&bars.a_empty[sl]));
             ++a_it;
           }
@@ -329,6 +330,7 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     }
     return;
   }
+  if (warp > kIssuerWarp0) return;
   if (warp < kEpiWarps) {
     const int q = warp & 3, r = q * 32 + lane;  // TMEM lane quarter; row of C
     const int h = warp >> 2;                    // column half of each pass
@@ -428,15 +430,15 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       using namespace tc;
       for (int i = 0; i < emuk::kASlots; ++i) {
         mbar_init(smem_u32(&bars.a_full[i]), 1);
-        mbar_init(smem_u32(&bars.a_empty[i]), emuk::kIssuers);
+        mbar_init(smem_u32(&bars.a_empty[i]), 1);
       }
       for (int i = 0; i < emuk::kBBufs; ++i) {
         mbar_init(smem_u32(&bars.b_full[i]), 1);
-        mbar_init(smem_u32(&bars.b_empty[i]), emuk::kIssuers);
+        mbar_init(smem_u32(&bars.b_empty[i]), 1);
       }
-      mbar_init(smem_u32(&bars.done), emuk::kIssuers);
+      mbar_init(smem_u32(&bars.done), 1);
       mbar_init(smem_u32(&bars.tmem_free), emuk::kEpiWarps);
-      for (int i = 0; i < emuk::kIssuers; ++i) mbar_init(smem_u32(&bars.fin[i]), 1);
+      mbar_init(smem_u32(&bars.fin), 1);
       mbar_fence_init();
     }
     if (warp == emuk::kIssuerWarp0) tc::tmem_alloc(tc::smem_u32(&tmem_slot), emuk::kTmemCols);
@@ -565,9 +567,9 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
           mbar_wait(smem_u32(&bars.b_full[bb]), (last / emuk::kBBufs) & 1, nullptr, P.timeout_ns);
         }
     }
-    if (warp >= emuk::kIssuerWarp0 && (threadIdx.x & 31) == 0 && pp.mma_issued) {
-      umma_commit(smem_u32(&bars.fin[warp - emuk::kIssuerWarp0]));
-      mbar_wait(smem_u32(&bars.fin[warp - emuk::kIssuerWarp0]), 0, nullptr, P.timeout_ns);
+    if (warp == emuk::kIssuerWarp0 && (threadIdx.x & 31) == 0 && pp.mma_issued) {
+      umma_commit(smem_u32(&bars.fin));
+      mbar_wait(smem_u32(&bars.fin), 0, nullptr, P.timeout_ns);
     }
     tc_fence_before();
     __syncthreads();
