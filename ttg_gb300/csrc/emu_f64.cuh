@@ -97,18 +97,24 @@ __device__ __forceinline__ void slice_block(const double* __restrict__ L, int ld
   }
 }
 
-// X 2^E as FP64, X = sum_g acc_g 2^(8(6-g)) from the exact FP32 group sums, rounded to nearest
-// (ties away from zero). X = H 2^32 + L with H = acc_0..2 (|H| < 2^38) and L = acc_3..6 (|L| < 2^49)
-// is formed in 64 bits: exactly while |H| < 2^30 (|X| < 2^62 + 2^49), else as X 2^-8, which drops
+// the integer group sums of one element: H = acc_0 2^16 + acc_1 2^8 + acc_2 (|H| < 2^38) and
+// L = acc_3 2^24 + acc_4 2^16 + acc_5 2^8 + acc_6 (|L| < 2^49), from the exact FP32 values
+__device__ __forceinline__ long long group_h(uint32_t a0, uint32_t a1, uint32_t a2) {
+  return (long long)__float2int_rn(__uint_as_float(a0)) * 65536 + (long long)__float2int_rn(__uint_as_float(a1)) * 256 +
+         (long long)__float2int_rn(__uint_as_float(a2));
+}
+__device__ __forceinline__ long long group_l(uint32_t a3, uint32_t a4, uint32_t a5, uint32_t a6) {
+  return (long long)__float2int_rn(__uint_as_float(a3)) * 16777216 +
+         (long long)__float2int_rn(__uint_as_float(a4)) * 65536 + (long long)__float2int_rn(__uint_as_float(a5)) * 256 +
+         (long long)__float2int_rn(__uint_as_float(a6));
+}
+
+// X 2^E as FP64, X = H 2^32 + L = sum_g acc_g 2^(8(6-g)), rounded to nearest (ties away from zero).
+// X is formed in 64 bits: exactly while |H| < 2^30 (|X| < 2^62 + 2^49), else as X 2^-8, which drops
 // only bits below 2^-54 of |X| >= 2^62. Branch-free, so that the compositions of neighbouring
 // elements interleave; *odd is set when the result leaves the normal FP64 range (the value returned
 // is then wrong: see compose_slow).
-__device__ __forceinline__ double compose(const uint32_t (&acc)[kSlices], int E, bool* odd) {
-  int a[kSlices];
-#pragma unroll
-  for (int g = 0; g < kSlices; ++g) a[g] = __float2int_rn(__uint_as_float(acc[g]));
-  const long long H = (long long)a[0] * 65536 + (long long)a[1] * 256 + (long long)a[2];
-  const long long L = (long long)a[3] * 16777216 + (long long)a[4] * 65536 + (long long)a[5] * 256 + (long long)a[6];
+__device__ __forceinline__ double compose(long long H, long long L, int E, bool* odd) {
   const int s = (H >= (1LL << 30) || H <= -(1LL << 30)) ? 8 : 0;
   const long long X = (long long)((unsigned long long)H << (32 - s)) + (L >> s);
   const bool neg = X < 0;
@@ -128,11 +134,9 @@ __device__ __forceinline__ double compose(const uint32_t (&acc)[kSlices], int E,
 }
 
 // the same value outside the normal range (subnormal or overflowing results): scaled in FP64
-__device__ __noinline__ double compose_slow(const uint32_t (&acc)[kSlices], int E) {
-  double v = 0;
-#pragma unroll
-  for (int g = 0; g < kSlices; ++g) v += ldexp((double)__float2int_rn(__uint_as_float(acc[g])), 8 * (6 - g) + E);
-  return v;
+// (H and L are exact in FP64)
+__device__ __noinline__ double compose_slow(long long H, long long L, int E) {
+  return ldexp((double)H, 32 + E) + ldexp((double)L, E);
 }
 
 }  // namespace emu

@@ -179,20 +179,25 @@ __device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey
 
 // ---- the emulated update task: C(M,N) -= L(M,K) L(N,K)^T on the tensor cores -----------------
 // Two passes over the 64-column halves of C; each pass accumulates the 28 digit-plane products of
-// the seven groups g = i + j <= 6 into seven 128 x 64 FP32 accumulators in TMEM (448 columns), over
-// two 64-wide chunks of k. Roles (warps of the 256-thread CTA):
+// the seven groups g = i + j <= 6 into seven 128 x 64 FP32 accumulators in TMEM (group g in columns
+// 64 g .. 64 g + 63), over two 64-wide chunks of k, in two phases: A (groups 3-6, 22 of the 28
+// plane pairs) and B (groups 0-2). As soon as phase A of a pass is done the epilogue folds its four
+// groups into one 64-bit integer per element (L) and frees their columns, so the next pass's phase
+// A runs while this pass's groups 0-2 are composed with L and subtracted from C.
 // The emulated executor runs 384 threads (twelve warps); its FP64 tasks use the first 256.
-//   warp 8 lane 0  TMA producer: per chunk the seven B planes (64 rows each) into one of two
-//                  buffers, then the A planes i = 0..6 (128 rows each) through a ring of six slots
-//   warp 9 lane 0  MMA issuer: for i = 0..6, k-steps 0..3: D[i..6] += A_i [B_0 .. B_(6-i)]^T as one
-//                  M128 x N(64 (7-i)) x K16 product (N at most 256 per instruction): the B planes of
-//                  a chunk are consecutive 64-row blocks of one K-major tile and the groups i + j
-//                  consecutive 64-column blocks of TMEM, so ten instructions per k-step cover the
-//                  28 plane pairs (one thread issues a tcgen05.mma only every ~110 clocks; an N=64
-//                  product takes the tensor pipe ~35). Each A slot is released after its
-//                  instructions, each B buffer after its chunk. Warps 10-11 have no part.
+//   warp 8 lane 0  TMA producer: per phase and chunk the phase's B planes (64 rows each) into one
+//                  of two buffers, then its A planes (128 rows each) through a ring of six slots
+//   warp 9 lane 0  MMA issuer: per phase and chunk, for each A plane i and k-step, one MMA of
+//                  M128 x N(64 x planes) x K16 against all the B planes j of the phase's groups
+//                  i + j: the B planes of a chunk are consecutive 64-row blocks of one K-major tile
+//                  and the groups consecutive 64-column blocks of TMEM, so 10 instructions per
+//                  k-step cover the 28 plane pairs (one thread issues a tcgen05.mma only every
+//                  ~110 clocks; an N=64 product takes the tensor pipe ~35). Each A slot is
+//                  released after its instructions, each B buffer after its chunk. Warps 10-11
+//                  have no part.
 //   warps 0-7      epilogue: TMEM lane quarter = warp % 4, column half = warp / 4; per element the
-//                  exact compose and one FP64 subtraction from C
+//                  integer group sums L (after phase A) and H (after phase B), the exact compose
+//                  and one FP64 subtraction from C
 namespace emuk {
 constexpr int kASlots = 6, kBBufs = 2;
 constexpr uint32_t kABytes = 128 * 128, kBBytes = 64 * 128;  // one plane chunk: rows x 128 bytes
@@ -202,7 +207,10 @@ constexpr int kTmemCols = 512;
 constexpr int kThreadsEmu = 384;
 constexpr int kEpiWarps = 8, kProducerWarp = 8, kIssuerWarp0 = 9;
 struct Bars {
-  uint64_t a_full[kASlots], a_empty[kASlots], b_full[kBBufs], b_empty[kBBufs], done, tmem_free, fin;
+  uint64_t a_full[kASlots], a_empty[kASlots], b_full[kBBufs], b_empty[kBBufs];
+  uint64_t done_a, done_b;  // phase A / B products of a pass complete (issuer commit)
+  uint64_t free_l, free_h;  // the epilogue has read groups 3-6 / 0-2 of a pass (eight warps)
+  uint64_t fin;
 };
 struct Pipe {  // pipeline positions, each kept by the one thread that uses it
   uint32_t a_it = 0, b_it = 0;  // producer: plane chunks issued; MMA issuer: consumed (A ring, B buffers)
@@ -260,25 +268,29 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
       // last by its FP64 tasks: order both before the async-proxy accesses
       asm volatile("fence.proxy.async.global;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      // per pass: phase A (groups 3-6: all seven planes of A and B), then phase B (groups 0-2:
+      // planes 0-2 of A and B), each over the two 64-wide chunks of k
       for (int pass = 0; pass < 2; ++pass)
-        for (int c = 0; c < 2; ++c) {
-          const uint32_t bb = pp.b_it % kBBufs, bph = (pp.b_it / kBBufs) & 1;
-          if (!mbar_wait(smem_u32(&bars.b_empty[bb]), bph ^ 1, err, P.timeout_ns)) return;
-          const uint32_t bdst = smem_u32(smB + (size_t)bb * kBSetBytes);
-          mbar_arrive_expect_tx(smem_u32(&bars.b_full[bb]), kBSetBytes);
-          for (int j = 0; j < emu::kSlices; ++j)
-            tma_load_2d(bdst + j * kBBytes, tmB, smem_u32(&bars.b_full[bb]), c * 64,
-                        (int)((tB * emu::kSlices + j) * emu::kEdge + pass * 64));
-          ++pp.b_it;
-          for (int i = 0; i < emu::kSlices; ++i) {
-            const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
-            if (!mbar_wait(smem_u32(&bars.a_empty[sl]), aph ^ 1, err, P.timeout_ns)) return;
-            mbar_arrive_expect_tx(smem_u32(&bars.a_full[sl]), kABytes);
-            tma_load_2d(smem_u32(smA + (size_t)sl * kABytes), tmA, smem_u32(&bars.a_full[sl]), c * 64,
-                        (int)((tA * emu::kSlices + i) * emu::kEdge));
-            ++pp.a_it;
+        for (int ph = 0; ph < 2; ++ph)
+          for (int c = 0; c < 2; ++c) {
+            const int np = ph == 0 ? emu::kSlices : 3;
+            const uint32_t bb = pp.b_it % kBBufs, bph = (pp.b_it / kBBufs) & 1;
+            if (!mbar_wait(smem_u32(&bars.b_empty[bb]), bph ^ 1, err, P.timeout_ns)) return;
+            const uint32_t bdst = smem_u32(smB + (size_t)bb * kBSetBytes);
+            mbar_arrive_expect_tx(smem_u32(&bars.b_full[bb]), np * kBBytes);
+            for (int j = 0; j < np; ++j)
+              tma_load_2d(bdst + j * kBBytes, tmB, smem_u32(&bars.b_full[bb]), c * 64,
+                          (int)((tB * emu::kSlices + j) * emu::kEdge + pass * 64));
+            ++pp.b_it;
+            for (int i = 0; i < np; ++i) {
+              const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
+              if (!mbar_wait(smem_u32(&bars.a_empty[sl]), aph ^ 1, err, P.timeout_ns)) return;
+              mbar_arrive_expect_tx(smem_u32(&bars.a_full[sl]), kABytes);
+              tma_load_2d(smem_u32(smA + (size_t)sl * kABytes), tmA, smem_u32(&bars.a_full[sl]), c * 64,
+                          (int)((tA * emu::kSlices + i) * emu::kEdge));
+              ++pp.a_it;
+            }
           }
-        }
     }
     return;
   }
@@ -289,42 +301,43 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
       uint32_t& a_it = pp.a_it;
       uint32_t& b_it = pp.b_it;
       for (int pass = 0; pass < 2; ++pass) {
-        if (pp.passes > 0 &&  // the previous pass's epilogue has read the accumulators
-            !mbar_wait(smem_u32(&bars.tmem_free), (pp.passes - 1) & 1, err, P.timeout_ns))
-          return;
-        tc_fence_after();
-        for (int c = 0; c < 2; ++c) {
-          const uint32_t bb = b_it % kBBufs, bph = (b_it / kBBufs) & 1;
-          if (!mbar_wait(smem_u32(&bars.b_full[bb]), bph, err, P.timeout_ns)) return;
+        for (int ph = 0; ph < 2; ++ph) {
+          // phase A writes groups 3-6 (TMEM columns 192-447), phase B groups 0-2 (columns 0-191):
+          // each waits until the epilogue has read its columns of the previous pass
+          if (pp.passes > 0 && !mbar_wait(smem_u32(ph == 0 ? &bars.free_l : &bars.free_h), (pp.passes - 1) & 1,
+                                          err, P.timeout_ns))
+            return;
           tc_fence_after();
-          const uint32_t bbase = smem_u32(smB + (size_t)bb * kBSetBytes);
-          for (int i = 0; i < emu::kSlices; ++i) {
-            const uint32_t sl = a_it % kASlots, aph = (a_it / kASlots) & 1;
-            if (!mbar_wait(smem_u32(&bars.a_full[sl]), aph, err, P.timeout_ns)) return;
+          const int np_a = ph == 0 ? emu::kSlices : 3;  // A planes of the phase
+          for (int c = 0; c < 2; ++c) {
+            const uint32_t bb = b_it % kBBufs, bph = (b_it / kBBufs) & 1;
+            if (!mbar_wait(smem_u32(&bars.b_full[bb]), bph, err, P.timeout_ns)) return;
             tc_fence_after();
-            const uint64_t ad = desc_kmajor_sw128(smem_u32(smA + (size_t)sl * kABytes));
-            // A_i against the B planes j = 0..6-i at once: the planes are consecutive 64-row blocks
-            // of one K-major tile, their groups i+j consecutive 64-column blocks of TMEM; at most
-            // four planes (N = 256) per instruction
-            const int np = emu::kSlices - i, n0 = np < 4 ? np : 4;
-            const uint32_t id0 = idesc_f16(128, 64 * n0, true), id1 = idesc_f16(128, 64 * (np - n0), true);
-            const uint64_t bd0 = desc_kmajor_sw128(bbase), bd1 = desc_kmajor_sw128(bbase + 4 * kBBytes);
-            const uint32_t d0 = tmem + (uint32_t)(i * 64), d1 = tmem + (uint32_t)((i + 4) * 64);
+            const uint32_t bbase = smem_u32(smB + (size_t)bb * kBSetBytes);
+            for (int i = 0; i < np_a; ++i) {
+              const uint32_t sl = a_it % kASlots, aph = (a_it / kASlots) & 1;
+              if (!mbar_wait(smem_u32(&bars.a_full[sl]), aph, err, P.timeout_ns)) return;
+              tc_fence_after();
+              const uint64_t ad = desc_kmajor_sw128(smem_u32(smA + (size_t)sl * kABytes));
+              // A_i against its B planes j of the phase's groups g = i + j at once: the planes are
+              // consecutive 64-row blocks of one K-major tile and the groups consecutive 64-column
+              // blocks of TMEM. Phase A: g = max(i,3)..6 (N <= 256); phase B: g = i..2.
+              const int g0 = ph == 0 ? (i > 3 ? i : 3) : i, g1 = ph == 0 ? 6 : 2;
+              const int np = g1 - g0 + 1;
+              const uint64_t bd = desc_kmajor_sw128(bbase + (uint32_t)(g0 - i) * kBBytes);
+              const uint32_t d = tmem + (uint32_t)(g0 * 64), id = idesc_f16(128, 64 * np, true);
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              // i = 0 first touches every group: it alone starts the sums (chunk 0, k-step 0)
-              const uint32_t acc = (c | i | ks) != 0 ? 1u : 0u;
-              umma_f16(d0, ad + 2 * ks, bd0 + 2 * ks, id0, acc);
-              if (np > 4) umma_f16(d1, ad + 2 * ks, bd1 + 2 * ks, id1, acc);
+              for (int ks = 0; ks < 4; ++ks)  // i = 0 first touches every group of the phase
+                umma_f16(d, ad + 2 * ks, bd + 2 * ks, id, (c | i | ks) != 0 ? 1u : 0u);
+              pp.mma_issued = true;
+              umma_commit(smem_u32(&bars.a_empty[sl]));
+              ++a_it;
             }
-            pp.mma_issued = true;
-            umma_commit(smem_u32(&bars.a_empty[sl]));
-            ++a_it;
+            umma_commit(smem_u32(&bars.b_empty[bb]));
+            ++b_it;
           }
-          umma_commit(smem_u32(&bars.b_empty[bb]));
-          ++b_it;
+          umma_commit(smem_u32(ph == 0 ? &bars.done_a : &bars.done_b));
         }
-        umma_commit(smem_u32(&bars.done));
         ++pp.passes;
       }
     }
@@ -351,37 +364,48 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     if (warp == kEpiWarps - 1 && lane == 0) prefetch_next(P, cur_task, pf);
     __syncwarp();
     double cur[8], nxt[8];
-    loadc(cur, 0, 0);
+    long long Lv[32];  // group sums 3-6 of this thread's 32 columns of the pass
     for (int pass = 0; pass < 2; ++pass) {
-      if (!mbar_wait(smem_u32(&bars.done), pp.passes & 1, err, P.timeout_ns)) return;
+      // phase A done: groups 3-6 -> L, then their TMEM columns go back to the issuer
+      if (!mbar_wait(smem_u32(&bars.done_a), pp.passes & 1, err, P.timeout_ns)) return;
       tc_fence_after();
-      for (int cc = 0; cc < 32; cc += 8) {
-        uint32_t v[emu::kSlices][8];
 #pragma unroll
-        for (int g = 0; g < emu::kSlices; ++g)
-          tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * 64 + h * 32 + cc), v[g]);
+      for (int cc = 0; cc < 32; cc += 8) {
+        uint32_t v[4][8];
+#pragma unroll
+        for (int g = 0; g < 4; ++g) tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((g + 3) * 64 + h * 32 + cc), v[g]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 8; ++j) Lv[cc + j] = emu::group_l(v[0][j], v[1][j], v[2][j], v[3][j]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&bars.free_l));
+      loadc(cur, pass, 0);
+      // phase B done: groups 0-2 -> H, composed with L and subtracted from C
+      if (!mbar_wait(smem_u32(&bars.done_b), pp.passes & 1, err, P.timeout_ns)) return;
+      tc_fence_after();
+#pragma unroll
+      for (int cc = 0; cc < 32; cc += 8) {
+        uint32_t v[3][8];
+#pragma unroll
+        for (int g = 0; g < 3; ++g) tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * 64 + h * 32 + cc), v[g]);
         if (cc + 8 < 32) loadc(nxt, pass, cc + 8);
-        else if (pass == 0) loadc(nxt, 1, 0);
         tmem_ld_wait();
         double res[8];
         bool odd = false;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          uint32_t acc[emu::kSlices];
-#pragma unroll
-          for (int g = 0; g < emu::kSlices; ++g) acc[g] = v[g][j];
           bool o;
-          res[j] = emu::compose(acc, ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62, &o);
+          res[j] = emu::compose(emu::group_h(v[0][j], v[1][j], v[2][j]), Lv[cc + j],
+                                ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62, &o);
           odd |= o;
         }
         if (odd) {  // a result outside the normal FP64 range (extreme scales only)
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            uint32_t acc[emu::kSlices];
-#pragma unroll
-            for (int g = 0; g < emu::kSlices; ++g) acc[g] = v[g][j];
-            res[j] = emu::compose_slow(acc, ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62);
-          }
+          for (int j = 0; j < 8; ++j)
+            res[j] = emu::compose_slow(emu::group_h(v[0][j], v[1][j], v[2][j]), Lv[cc + j],
+                                       ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62);
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -393,7 +417,7 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(smem_u32(&bars.tmem_free));
+      if (lane == 0) mbar_arrive(smem_u32(&bars.free_h));
       ++pp.passes;
     }
   }
@@ -436,8 +460,10 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
         mbar_init(smem_u32(&bars.b_full[i]), 1);
         mbar_init(smem_u32(&bars.b_empty[i]), 1);
       }
-      mbar_init(smem_u32(&bars.done), 1);
-      mbar_init(smem_u32(&bars.tmem_free), emuk::kEpiWarps);
+      mbar_init(smem_u32(&bars.done_a), 1);
+      mbar_init(smem_u32(&bars.done_b), 1);
+      mbar_init(smem_u32(&bars.free_l), emuk::kEpiWarps);
+      mbar_init(smem_u32(&bars.free_h), emuk::kEpiWarps);
       mbar_init(smem_u32(&bars.fin), 1);
       mbar_fence_init();
     }
