@@ -26,9 +26,11 @@
  * Thread safety. Calls on different streams with disjoint workspaces may run concurrently.
  * Mutable global state, each part guarded by a mutex or set only by its own setter: per-device
  * caches of launch attributes and of the FP64 solve's scratch, the wait time limit
- * (gbx_set_wait_timeout_ns), the trace buffer (gbx_set_trace_buffer), the copy streams and
- * mapped flags of gbx_dposv_tiled_host (one caller at a time), and the static scratch of
- * gbx_dpotrf_tiled_noalloc with its per-device address.
+ * (gbx_set_wait_timeout_ns), the trace buffer (gbx_set_trace_buffer), the copy stream and
+ * events of gbx_dposv_tiled_host (one caller at a time), the static scratch of
+ * gbx_dpotrf_tiled_noalloc with its per-device address, and the executor settings
+ * (gbx_set_dag_block_edge, gbx_set_fp64_update, gbx_set_dag_lead: read at each launch; set them
+ * before the calls they are meant for, not concurrently with other calls).
  */
 #ifndef GBX_POTRF_H
 #define GBX_POTRF_H
@@ -330,16 +332,16 @@ int gbx_split_f64(const double* a, float* hi, float* lo, long long n, void* stre
 int gbx_dpotri_tiled_bufferSize(int N, int NB, size_t* bytes);
 int gbx_dpotri_tiled(int N, int NB, double* tiles, void* work, size_t work_bytes, void* stream);
 
-/* Factorisation and solve from host buffers (pinned for overlap): A_host and L_host hold the
- * tile-major lower storage (tiled_numel doubles), B_host / X_host are column-major N x nrhs; tiles
- * and X are device buffers of the same sizes. A and B are copied in, the executor runs, each tile
- * column of L is copied back as soon as it is final (while the factorisation goes on), then
- * X = (L L^T)^{-1} B comes back. Returns once the factorisation has finished on the device (the
- * calling thread issues the copy-out as the columns complete); the solve and the last copies are
- * still queued on `stream`. gbx_dpotrf_tiled_status(work) gives the factorisation status. If the
- * factorisation stopped early (a non-positive pivot or a timed-out wait), the solve is skipped,
- * the stream is synchronised, L_host holds the partial factor and the call returns the status
- * itself (>0 first bad pivot, or GBX_ERR_TIMEOUT). No
+/* Factorisation and solve from host buffers (pinned for full copy speed): A_host and L_host hold
+ * the tile-major lower storage (tiled_numel doubles), B_host / X_host are column-major N x nrhs;
+ * tiles and X are device buffers of the same sizes. A and B are copied in, the executor runs, then
+ * L is copied back on a second stream while X = (L L^T)^{-1} B is solved and copied back on
+ * `stream`. Returns once the factorisation has finished on the device; the solve and the copies
+ * are still queued (`stream` waits for the copy of L). gbx_dpotrf_tiled_status(work) gives the
+ * factorisation status. If the factorisation stopped early (a non-positive pivot or a timed-out
+ * wait), the solve is skipped, L_host receives the partial factor before the call returns, and
+ * the call returns the status itself (>0 first bad pivot, or GBX_ERR_TIMEOUT). The workspace is
+ * gbx_dpotrf_tiled's. No
  * counterpart in the reference, whose tiles reach the device through PaRSEC's stage-in
  * (parsec/ttg.h:1434-1672) and come back on wait() (parsec/devicefunc.h:232-256). */
 int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes);

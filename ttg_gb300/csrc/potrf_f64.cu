@@ -102,12 +102,6 @@ struct DagParams {
   DagState* st;
   int* cnt;            // packed lower per-block completion counters
   uint64_t timeout_ns;
-  // host-buffer runs (gbx_dposv_tiled_host), else null: col_done[g] counts finished POTRF/TRSM
-  // blocks of the g-th group of group_blocks consecutive block columns; the block that completes a
-  // group raises host_flag[g] (mapped pinned host memory) to 1
-  int* col_done;
-  volatile int* host_flag;
-  int group_blocks, groups;
   // tensor-core emulated updates (kEmu launches): digit planes and row exponents of every lower
   // block, indexed by tri_index (diagonal blocks unused)
   uint16_t* planes;
@@ -115,19 +109,6 @@ struct DagParams {
   long long lead;  // trailing tasks of a step queued ahead of its TRSMs (dag_decode)
 };
 
-// finished POTRF/TRSM blocks a group needs: block columns J of the group hold NTb - J blocks each
-__device__ __forceinline__ int group_target(const DagParams& P, int g) {
-  const int a = g * P.group_blocks, b = min(P.NTb, a + P.group_blocks);
-  return (b - a) * P.NTb - (a + b - 1) * (b - a) / 2;
-}
-
-// the host waits on host_flag: a launch that stops early raises every flag to 2
-__device__ __forceinline__ void release_columns(const DagParams& P) {
-  if (P.host_flag && ld_volatile(&P.st->abort)) {
-    __threadfence_system();
-    for (int k = 0; k < P.groups; ++k) P.host_flag[k] = 2;
-  }
-}
 
 // the counters a task waits on: up to three (counter, target) pairs
 __device__ __forceinline__ int dag_deps(const DagParams& P, const TaskKey& k, const int** c, int* v) {
@@ -509,7 +490,6 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
           if (info != 0 && threadIdx.x == 0) {
             atomicCAS(&P.st->status, 0, K * V.b + info);
             atomicExch(&P.st->abort, 1);
-            release_columns(P);
             s_failed = 1;
           }
         } else if (kEmu && threadIdx.x == 32 * emuk::kProducerWarp + 1) {
@@ -567,16 +547,8 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       }
       trace_record(P.trace, t_start, tk.type, tk.a, tk.b, tk.c, 0);  // end stamp before any waiter can start
       signal_done(target);
-      if (P.col_done && (tk.type == T_POTRF || tk.type == T_TRSM)) {  // block (a, b) of L is final
-        const int g = (tk.type == T_POTRF ? tk.a : tk.b) / P.group_blocks;
-        if (atomicAdd(P.col_done + g, 1) + 1 == group_target(P, g)) {
-          __threadfence_system();  // every block of the group (each CTA fenced before counting) first
-          P.host_flag[g] = 1;
-        }
-      }
     }
   }
-  if (threadIdx.x == 0) release_columns(P);
   if (kEmu) {
     using namespace tc;
     // after an early stop: let this CTA's copies and products in flight land (bounded waits) before
@@ -956,8 +928,7 @@ size_t executor_workspace_bytes(const BlockView& V, int NTb) {
 }
 
 int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaStream_t s, long long first_task,
-               uint64_t timeout_ns, int* col_done = nullptr, volatile int* host_flag = nullptr,
-               int group_blocks = 1, bool allow_emu = true) {
+               uint64_t timeout_ns, bool allow_emu = true) {
   const bool emu = allow_emu && emu_active(V);
   const size_t need = emu ? emu_workspace_bytes(NTb) : dag_workspace_bytes(NTb);
   if (work == nullptr || work_bytes < need) return GBX_ERR_WORKSPACE;
@@ -974,10 +945,6 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   P.cnt = (int*)((char*)work + sizeof(DagState));
   P.timeout_ns = timeout_ns;
   P.trace = current_trace();
-  P.col_done = col_done;
-  P.host_flag = host_flag;
-  P.group_blocks = group_blocks;
-  P.groups = (NTb + group_blocks - 1) / group_blocks;
   P.planes = nullptr;
   P.rexp = nullptr;
   CUtensorMap ta, tb;
@@ -1086,7 +1053,7 @@ int gbx_dpotrf_tile(int n, double* A, int lda, void* work, size_t work_bytes, in
   if (n == 0) return cudaMemsetAsync(devInfo, 0, sizeof(int), s) == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
   const BlockView V = plain_view(n, A, lda);
   const int NTb = (n + V.b - 1) / V.b;
-  if (int e = launch_dag(V, NTb, work, work_bytes, s, 0, gbx_get_wait_timeout_ns(), nullptr, nullptr, 1, false))
+  if (int e = launch_dag(V, NTb, work, work_bytes, s, 0, gbx_get_wait_timeout_ns(), false))
     return e;
   copy_info_kernel<<<1, 32, 0, s>>>((const DagState*)work, devInfo);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
@@ -1224,58 +1191,45 @@ int gbx_dpotrs_tiled(int N, int NB, const double* tiles, int nrhs, double* B, in
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
 }
 
-// ---- factorisation and solve from host buffers, the copies overlapped ---------------------------
+// ---- factorisation and solve from host buffers -------------------------------------------------
 //   copy-in:  one cudaMemcpyAsync of the whole tile array, then one of the right-hand sides, both
 //             on the caller's stream ahead of the executor launch (copies interleaved with other
 //             stream operations ran many times slower on this platform than one large copy);
-//   copy-out: each finished POTRF/TRSM block adds to the count of its group of tile columns
-//             (about eight groups); the block that completes a group raises the group's flag in
-//             mapped pinned host memory, and the calling thread, which polls those flags, issues
-//             that group's copy back (its tiles are contiguous) on a second copy stream, so L
-//             streams out while the factorisation runs.
-// Stream memory operations were measured to signal a quarter of a second late on this platform,
-// hence plain copies and a polling thread. The executor raises every group flag (to 2) on any early
-// exit, and the thread also stops when the launch has finished, so no side waits on a flag that
-// cannot come; after an early exit the solve is skipped.
+//   copy-out: one copy of the whole factor on a second stream once the executor has finished,
+//             running beside the solve on the caller's stream (both only read L).
+// Host copies of pinned memory run at ~200 GB/s here (4.4 GB of tiles in ~22 ms each way), so the
+// copies are a few percent of the step. Streaming L out per column group while the factorisation
+// runs, signalled through flags in mapped host memory, was measured slower: the flags became
+// visible to the host a quarter of a second late, as stream memory operations did.
 namespace {
-struct HostOverlap {
+struct HostCopies {
   cudaStream_t out = nullptr;
-  cudaEvent_t ev0 = nullptr, ev_kernel = nullptr, ev_out = nullptr;
-  int* flags = nullptr;        // pinned mapped host memory: kMaxGroups copy-out flags
-  int* flags_dev = nullptr;    // its device address
+  cudaEvent_t ev_kernel = nullptr, ev_out = nullptr;
+  int* status = nullptr;  // pinned host copy of the executor's status
   bool ready = false;
 };
-constexpr int kMaxGroups = 64;
 std::mutex g_host_mtx;
-HostOverlap g_host[32];
+HostCopies g_host[32];
 
-int host_overlap(HostOverlap*& ho) {
+int host_copies(HostCopies*& ho) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 32) return GBX_ERR_CUDA;
-  HostOverlap& h = g_host[dev];
+  HostCopies& h = g_host[dev];
   ho = &h;
   if (h.ready) return GBX_OK;
   if (cudaStreamCreateWithFlags(&h.out, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&h.ev0, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h.ev_kernel, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h.ev_out, cudaEventDisableTiming) != cudaSuccess ||
-      cudaHostAlloc((void**)&h.flags, kMaxGroups * sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
-      cudaHostGetDevicePointer((void**)&h.flags_dev, h.flags, 0) != cudaSuccess)
+      cudaHostAlloc((void**)&h.status, sizeof(int), cudaHostAllocDefault) != cudaSuccess)
     return GBX_ERR_CUDA;
   h.ready = true;
   return GBX_OK;
-}
-size_t host_dag_bytes(int N, int NB) {
-  size_t b = 0;
-  gbx_dpotrf_tiled_bufferSize(N, NB, &b);
-  return (b + 255) / 256 * 256;
 }
 }  // namespace
 
 int gbx_dposv_tiled_host_bufferSize(int N, int NB, size_t* bytes) {
   if (N <= 0 || NB <= 0 || block_edge(NB) == 0 || !bytes) return GBX_ERR_ARG;
-  *bytes = host_dag_bytes(N, NB) + (size_t)kMaxGroups * sizeof(int);
-  return GBX_OK;
+  return gbx_dpotrf_tiled_bufferSize(N, NB, bytes);
 }
 
 int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, int nrhs, const double* B_host,
@@ -1285,59 +1239,33 @@ int gbx_dposv_tiled_host(int N, int NB, const double* A_host, double* L_host, in
   if (int e = gbx_dposv_tiled_host_bufferSize(N, NB, &need)) return e;
   if (nrhs < 0 || !A_host || !L_host || !tiles || (nrhs > 0 && (!B_host || !X_host || !X))) return GBX_ERR_ARG;
   if (!work || work_bytes < need) return GBX_ERR_WORKSPACE;
-  std::lock_guard<std::mutex> lk(g_host_mtx);  // one caller at a time on the shared flags and copy streams
-  HostOverlap* h = nullptr;
-  if (int e = host_overlap(h)) return e;
+  std::lock_guard<std::mutex> lk(g_host_mtx);  // one caller at a time on the shared copy stream and events
+  HostCopies* h = nullptr;
+  if (int e = host_copies(h)) return e;
   cudaStream_t s = (cudaStream_t)stream;
   const BlockView V = tiled_view(N, NB, tiles);
-  const int NTb = (N + V.b - 1) / V.b, NT = V.NT, r = V.r;
-  const size_t dag = host_dag_bytes(N, NB);
-  int* col_done = (int*)((char*)work + dag);  // kMaxGroups counts
-  const long long tile = (long long)NB * NB;
-  auto col_off = [&](int n) { return ((long long)n * NT - (long long)n * (n - 1) / 2) * tile; };
-  const int G = (NT + 7) / 8, ngroups = (NT + G - 1) / G;  // tile columns per copy-out group (<= 8 groups)
-  // the previous call's launch may still be leaving (an aborted launch raises flags from every CTA)
-  if (cudaEventSynchronize(h->ev_kernel) != cudaSuccess) return GBX_ERR_CUDA;
-  volatile int* out_flag = h->flags;
-  for (int g = 0; g < ngroups; ++g) out_flag[g] = 0;
-  // copy-in: one copy of the whole tile array (copies interleaved with other stream operations ran
-  // many times slower here), then the right-hand sides
-  if (cudaMemcpyAsync(tiles, A_host, (size_t)col_off(NT) * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
-    return GBX_ERR_CUDA;
+  const int NTb = (N + V.b - 1) / V.b, NT = V.NT;
+  const size_t tile_bytes = ((size_t)NT * (NT + 1) / 2) * (size_t)NB * NB * sizeof(double);
+  if (cudaMemcpyAsync(tiles, A_host, tile_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return GBX_ERR_CUDA;
   if (nrhs > 0 &&
       cudaMemcpyAsync(X, B_host, (size_t)N * nrhs * sizeof(double), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return GBX_ERR_CUDA;
-  if (cudaMemsetAsync(col_done, 0, (size_t)kMaxGroups * sizeof(int), s) != cudaSuccess) return GBX_ERR_CUDA;
-  if (cudaEventRecord(h->ev0, s) != cudaSuccess || cudaStreamWaitEvent(h->out, h->ev0, 0) != cudaSuccess)
+  if (int e = launch_dag(V, NTb, work, need, s, 0, gbx_get_wait_timeout_ns())) return e;
+  // the status first (behind the 4.4 GB copy of L it would wait ~20 ms for the copy engine)
+  if (cudaMemcpyAsync(h->status, work, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaEventRecord(h->ev_kernel, s) != cudaSuccess)
     return GBX_ERR_CUDA;
-  if (int e = launch_dag(V, NTb, work, dag, s, 0, gbx_get_wait_timeout_ns(), col_done, h->flags_dev, G * r)) return e;
-  if (cudaEventRecord(h->ev_kernel, s) != cudaSuccess) return GBX_ERR_CUDA;
-  // copy-out: each group as soon as the executor raises its flag (2: the executor stopped early)
-  bool stopped = false;
-  for (int g = 0; g < ngroups;) {
-    if (out_flag[g] != 0) {
-      if (out_flag[g] == 2) stopped = true;
-      const int k0 = g * G, k1 = std::min(NT, k0 + G);
-      const long long off = col_off(k0), cnt = col_off(k1) - off;
-      if (cudaMemcpyAsync(L_host + off, tiles + off, (size_t)cnt * sizeof(double), cudaMemcpyDeviceToHost, h->out) !=
-          cudaSuccess)
-        return GBX_ERR_CUDA;
-      ++g;
-      continue;
-    }
-    const cudaError_t q = cudaEventQuery(h->ev_kernel);
-    if (q == cudaSuccess) {  // the launch is over: its flags are all visible by now
-      if (out_flag[g] != 0) continue;
-      return GBX_ERR_CUDA;  // finished without completing the group and without an abort: a failure
-    }
-    if (q != cudaErrorNotReady) return GBX_ERR_CUDA;
-    std::this_thread::sleep_for(std::chrono::microseconds(50));
-  }
-  if (cudaEventRecord(h->ev_out, h->out) != cudaSuccess) return GBX_ERR_CUDA;
-  if (stopped) {  // bad pivot or timed-out wait: no solve on a partial factor; report the status
-    if (cudaStreamWaitEvent(s, h->ev_out, 0) != cudaSuccess) return GBX_ERR_CUDA;
-    const int st = gbx_dpotrf_tiled_status(work, stream);
-    return st != 0 ? st : GBX_ERR_CUDA;  // an early exit always leaves a nonzero status
+  // L goes back on the copy stream as soon as the executor is done
+  if (cudaStreamWaitEvent(h->out, h->ev_kernel, 0) != cudaSuccess ||
+      cudaMemcpyAsync(L_host, tiles, tile_bytes, cudaMemcpyDeviceToHost, h->out) != cudaSuccess ||
+      cudaEventRecord(h->ev_out, h->out) != cudaSuccess)
+    return GBX_ERR_CUDA;
+  // the factorisation's status decides on the solve: wait for the executor
+  if (cudaEventSynchronize(h->ev_kernel) != cudaSuccess) return GBX_ERR_CUDA;
+  const int st = *(volatile int*)h->status;
+  if (st != 0) {  // bad pivot or timed-out wait: no solve on a partial factor; L_host gets it anyway
+    if (cudaEventSynchronize(h->ev_out) != cudaSuccess) return GBX_ERR_CUDA;
+    return st;
   }
   if (nrhs > 0) {
     if (int e = gbx_dpotrs_tiled(N, NB, tiles, nrhs, X, N, stream)) return e;
@@ -1449,7 +1377,7 @@ int gbx_dpotrf_tiled_noalloc(int N, int NB, double* tiles, int* devInfo, void* s
   void* scratch = nullptr;
   if (int e = noalloc_scratch(&scratch)) return e;
   // launch_dag clears the header and the counters this run uses (cudaMemsetAsync, no allocation)
-  if (int e = launch_dag(V, NTb, scratch, kNoAllocBytes, s, 0, gbx_get_wait_timeout_ns(), nullptr, nullptr, 1, false))
+  if (int e = launch_dag(V, NTb, scratch, kNoAllocBytes, s, 0, gbx_get_wait_timeout_ns(), false))
     return e;
   copy_info_kernel<<<1, 32, 0, s>>>((const DagState*)scratch, devInfo);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
@@ -1462,7 +1390,7 @@ int gbx_dag_timeout_selftest(int NB, double* tiles, void* work, size_t work_byte
   cudaStream_t s = (cudaStream_t)stream;
   const BlockView V = tiled_view(2 * NB, NB, tiles);
   // skip task 0 (POTRF(0)): TRSM(1,0) then waits for a counter nothing will ever move
-  if (int e = launch_dag(V, 2, work, work_bytes, s, 1, timeout_ns, nullptr, nullptr, 1, false)) return e;
+  if (int e = launch_dag(V, 2, work, work_bytes, s, 1, timeout_ns, false)) return e;
   return gbx_dpotrf_tiled_status(work, stream);
 }
 
