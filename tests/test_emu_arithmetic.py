@@ -1,0 +1,109 @@
+"""The arithmetic of the executor's tensor-core FP64 updates (ttg_gb300/csrc/emu_f64.cuh), restated
+with Python integers and checked against exact rationals (CPU):
+  * splitting: row scale 2^e (|x| < 2^e), F = round(x 2^(55-e)) as seven balanced base-256 digits,
+    each of at most 8 significant bits (exact in bf16);
+  * products: group sums acc_g = sum_{i+j=g} sum_k a_i b_j for g <= 6 stay below 2^24 in magnitude
+    for k = 128 (exact in the tensor cores' FP32 accumulation);
+  * composition: X = H 2^32 + L in 64 bits (X 2^-8 when |H| >= 2^30), rounded once to FP64.
+The emulated dot product must be at least as accurate as a plain FP64 loop over the same inputs."""
+import struct
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+
+def _bits(x):
+    return struct.unpack("<q", struct.pack("<d", x))[0]
+
+
+def split_row(row):
+    mex = max(((_bits(v) >> 52) & 0x7FF) for v in row)
+    e = mex - 1022
+    digits = []
+    for v in row:
+        b = _bits(v)
+        ex = (b >> 52) & 0x7FF
+        F = 0
+        if ex > 0 and mex > 0:
+            mant = (b & ((1 << 52) - 1)) | (1 << 52)
+            sh = ex - 1020 - e
+            assert sh <= 2
+            f = mant << sh if sh >= 0 else ((mant + (1 << (-sh - 1))) >> (-sh) if sh > -60 else 0)
+            F = -f if b < 0 else f
+        d = [0] * 7
+        for i in range(6, 0, -1):
+            d[i] = ((F + 128) & 255) - 128
+            F = (F - d[i]) >> 8
+        d[0] = F
+        assert all(-128 <= x <= 128 for x in d)
+        digits.append(d)
+    return e, digits
+
+
+def compose(acc, E):
+    H = (acc[0] << 16) + (acc[1] << 8) + acc[2]
+    L = (acc[3] << 24) + (acc[4] << 16) + (acc[5] << 8) + acc[6]
+    s = 8 if abs(H) >= 2 ** 30 else 0
+    X = (H << (32 - s)) + (L >> s)  # >> floors, as the arithmetic shift does
+    assert abs(X) < 2 ** 63
+    if X == 0:
+        return 0.0
+    u = abs(X)
+    z = 64 - u.bit_length()
+    top = (u << z) & ((1 << 64) - 1)
+    p = 63 - z
+    mant = (top >> 11) + ((top >> 10) & 1)
+    if mant >> 53:
+        mant >>= 1
+        p += 1
+    v = float(mant) * 2.0 ** (p - 52 + E + s)
+    return -v if X < 0 else v
+
+
+def emulated_dot(a, b):
+    ea, da = split_row(a)
+    eb, db = split_row(b)
+    acc = []
+    for g in range(7):
+        t = sum(da[k][i] * db[k][g - i] for i in range(g + 1) for k in range(len(a)))
+        assert abs(t) < 2 ** 24, "group sum not exact in FP32"
+        acc.append(t)
+    return compose(acc, ea + eb - 62)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_emulated_dot_is_at_least_fp64_accurate(seed):
+    rng = np.random.default_rng(seed)
+    worst_emu = worst_fp64 = 0.0
+    for trial in range(40):
+        scale = 10.0 ** rng.uniform(-3, 3, size=2)
+        a = rng.uniform(-1, 1, 128) * scale[0]
+        b = rng.uniform(-1, 1, 128) * scale[1]
+        if trial % 4 == 0:  # no cancellation: the largest group sums
+            a, b = np.abs(a), np.abs(b)
+        if trial % 7 == 0:  # entries far below the row maximum
+            a[rng.integers(0, 128, 20)] *= 1e-9
+        exact = sum(Fraction(x) * Fraction(y) for x, y in zip(a, b))
+        den = Fraction(float(np.max(np.abs(a)) * np.max(np.abs(b))))
+        worst_emu = max(worst_emu, float(abs(Fraction(emulated_dot(a, b)) - exact) / den))
+        s = 0.0
+        for x, y in zip(a, b):
+            s = s + x * y
+        worst_fp64 = max(worst_fp64, float(abs(Fraction(s) - exact) / den))
+    assert worst_emu <= 4e-15
+    assert worst_emu <= worst_fp64
+
+
+def test_extreme_digits_stay_exact():
+    """All-equal rows of the largest magnitude: every digit at its bound, group sums at their maximum."""
+    a = np.full(128, np.nextafter(1.0, 0.0))
+    exact = sum(Fraction(x) * Fraction(x) for x in a)
+    got = emulated_dot(a, a)
+    assert abs(Fraction(got) - exact) <= exact * Fraction(2.0 ** -52)
+
+
+def test_zero_and_subnormal_rows():
+    assert emulated_dot(np.zeros(128), np.ones(128)) == 0.0
+    tiny = np.full(128, 5e-324)
+    assert emulated_dot(tiny, np.ones(128)) == 0.0  # subnormal rows carry no digits
