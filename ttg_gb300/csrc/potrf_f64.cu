@@ -191,11 +191,14 @@ struct Bars {
   uint64_t a_full[kASlots], a_empty[kASlots], b_full[kBBufs], b_empty[kBBufs];
   uint64_t done_a, done_b;  // phase A / B products of a pass complete (issuer commit)
   uint64_t free_l, free_h;  // the epilogue has read groups 3-6 / 0-2 of a pass (eight warps)
+  uint64_t decided;         // the producer has decided whether to start the next task early
   uint64_t fin;
 };
 struct Pipe {  // pipeline positions, each kept by the one thread that uses it
   uint32_t a_it = 0, b_it = 0;  // producer: plane chunks issued; MMA issuer: consumed (A ring, B buffers)
   uint32_t passes = 0;          // MMA issuer and epilogue threads: accumulator passes begun
+  uint32_t tasks = 0;           // MMA issuer: update tasks done (parity of the `decided` barrier)
+  bool ahead = false;           // producer / issuer: the first phase of the next task is already out
   bool mma_issued = false;
 };
 }  // namespace emuk
@@ -209,9 +212,14 @@ struct Prefetch {
   long long* next;  // -2 none taken, -1 queue empty, else the task index
   int* ok;          // its dependencies were all met
   TaskKey* key;
+  int* done;        // the three above are written (set last)
+  int* ahead;       // kEmu: the producer started the next task's first phase (emu_update)
 };
 __device__ __noinline__ void prefetch_next(const DagParams& P, long long cur, const Prefetch& pf) {
-  if (cur + 1 >= P.ntasks) return;
+  if (cur + 1 >= P.ntasks) {
+    *(volatile int*)pf.done = 1;
+    return;
+  }
   long long tn = -1;
   if (!ld_volatile(&P.st->abort)) tn = (long long)atomicAdd(&P.st->head, 1ULL);
   int ok = 0;
@@ -226,6 +234,8 @@ __device__ __noinline__ void prefetch_next(const DagParams& P, long long cur, co
   }
   *pf.ok = ok;
   *pf.next = (tn >= 0 && tn < P.ntasks) ? tn : -1;
+  __threadfence_block();
+  *(volatile int*)pf.done = 1;
 }
 
 __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtensorMap* tmB, const DagParams& P,
@@ -243,35 +253,98 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
   // column exponents of this task (rows of L(N,K)), before the roles split
   if (threadIdx.x < emu::kEdge) s_cexp[threadIdx.x] = __ldcg(P.rexp + tB * emu::kEdge + threadIdx.x);
   __syncthreads();
+  // one phase of one pass: the producer's loads (per 64-wide chunk of k the phase's B planes, 64
+  // rows each, into one of two buffers, then its A planes, 128 rows each, through the ring) and the
+  // issuer's products. Phase A (ph 0): groups 3-6, all seven planes; phase B (ph 1): groups 0-2,
+  // planes 0-2.
+  auto load_phase = [&](long long ta, long long tb, int pass, int ph) -> bool {
+    const int np = ph == 0 ? emu::kSlices : 3;
+    for (int c = 0; c < 2; ++c) {
+      const uint32_t bb = pp.b_it % kBBufs, bph = (pp.b_it / kBBufs) & 1;
+      if (!mbar_wait(smem_u32(&bars.b_empty[bb]), bph ^ 1, err, P.timeout_ns)) return false;
+      const uint32_t bdst = smem_u32(smB + (size_t)bb * kBSetBytes);
+      mbar_arrive_expect_tx(smem_u32(&bars.b_full[bb]), np * kBBytes);
+      for (int j = 0; j < np; ++j)
+        tma_load_2d(bdst + j * kBBytes, tmB, smem_u32(&bars.b_full[bb]), c * 64,
+                    (int)((tb * emu::kSlices + j) * emu::kEdge + pass * 64));
+      ++pp.b_it;
+      for (int i = 0; i < np; ++i) {
+        const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
+        if (!mbar_wait(smem_u32(&bars.a_empty[sl]), aph ^ 1, err, P.timeout_ns)) return false;
+        mbar_arrive_expect_tx(smem_u32(&bars.a_full[sl]), kABytes);
+        tma_load_2d(smem_u32(smA + (size_t)sl * kABytes), tmA, smem_u32(&bars.a_full[sl]), c * 64,
+                    (int)((ta * emu::kSlices + i) * emu::kEdge));
+        ++pp.a_it;
+      }
+    }
+    return true;
+  };
+  auto issue_phase = [&](int ph) -> bool {
+    // phase A writes groups 3-6 (TMEM columns 192-447), phase B groups 0-2 (columns 0-191): each
+    // waits until the epilogue has read its columns of the previous pass
+    if (pp.passes > 0 &&
+        !mbar_wait(smem_u32(ph == 0 ? &bars.free_l : &bars.free_h), (pp.passes - 1) & 1, err, P.timeout_ns))
+      return false;
+    tc_fence_after();
+    const int np_a = ph == 0 ? emu::kSlices : 3;  // A planes of the phase
+    for (int c = 0; c < 2; ++c) {
+      const uint32_t bb = pp.b_it % kBBufs, bph = (pp.b_it / kBBufs) & 1;
+      if (!mbar_wait(smem_u32(&bars.b_full[bb]), bph, err, P.timeout_ns)) return false;
+      tc_fence_after();
+      const uint32_t bbase = smem_u32(smB + (size_t)bb * kBSetBytes);
+      for (int i = 0; i < np_a; ++i) {
+        const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
+        if (!mbar_wait(smem_u32(&bars.a_full[sl]), aph, err, P.timeout_ns)) return false;
+        tc_fence_after();
+        const uint64_t ad = desc_kmajor_sw128(smem_u32(smA + (size_t)sl * kABytes));
+        // A_i against its B planes j of the phase's groups g = i + j at once: the planes are
+        // consecutive 64-row blocks of one K-major tile and the groups consecutive 64-column
+        // blocks of TMEM. Phase A: g = max(i,3)..6 (N <= 256); phase B: g = i..2.
+        const int g0 = ph == 0 ? (i > 3 ? i : 3) : i, g1 = ph == 0 ? 6 : 2;
+        const int np = g1 - g0 + 1;
+        const uint64_t bd = desc_kmajor_sw128(bbase + (uint32_t)(g0 - i) * kBBytes);
+        const uint32_t d = tmem + (uint32_t)(g0 * 64), id = idesc_f16(128, 64 * np, true);
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks)  // i = 0 first touches every group of the phase
+          umma_f16(d, ad + 2 * ks, bd + 2 * ks, id, (c | i | ks) != 0 ? 1u : 0u);
+        pp.mma_issued = true;
+        umma_commit(smem_u32(&bars.a_empty[sl]));
+        ++pp.a_it;
+      }
+      umma_commit(smem_u32(&bars.b_empty[bb]));
+      ++pp.b_it;
+    }
+    umma_commit(smem_u32(ph == 0 ? &bars.done_a : &bars.done_b));
+    return true;
+  };
+  // the four phases of a task: (pass 0, A), (pass 0, B), (pass 1, A), (pass 1, B); the first is
+  // already out when the previous task started it early (pp.ahead)
   if (warp == kProducerWarp) {
     if (lane == 0) {
       // the planes were written by other CTAs with ordinary stores, and this CTA's shared memory
       // last by its FP64 tasks: order both before the async-proxy accesses
       asm volatile("fence.proxy.async.global;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      // per pass: phase A (groups 3-6: all seven planes of A and B), then phase B (groups 0-2:
-      // planes 0-2 of A and B), each over the two 64-wide chunks of k
-      for (int pass = 0; pass < 2; ++pass)
-        for (int ph = 0; ph < 2; ++ph)
-          for (int c = 0; c < 2; ++c) {
-            const int np = ph == 0 ? emu::kSlices : 3;
-            const uint32_t bb = pp.b_it % kBBufs, bph = (pp.b_it / kBBufs) & 1;
-            if (!mbar_wait(smem_u32(&bars.b_empty[bb]), bph ^ 1, err, P.timeout_ns)) return;
-            const uint32_t bdst = smem_u32(smB + (size_t)bb * kBSetBytes);
-            mbar_arrive_expect_tx(smem_u32(&bars.b_full[bb]), np * kBBytes);
-            for (int j = 0; j < np; ++j)
-              tma_load_2d(bdst + j * kBBytes, tmB, smem_u32(&bars.b_full[bb]), c * 64,
-                          (int)((tB * emu::kSlices + j) * emu::kEdge + pass * 64));
-            ++pp.b_it;
-            for (int i = 0; i < np; ++i) {
-              const uint32_t sl = pp.a_it % kASlots, aph = (pp.a_it / kASlots) & 1;
-              if (!mbar_wait(smem_u32(&bars.a_empty[sl]), aph ^ 1, err, P.timeout_ns)) return;
-              mbar_arrive_expect_tx(smem_u32(&bars.a_full[sl]), kABytes);
-              tma_load_2d(smem_u32(smA + (size_t)sl * kABytes), tmA, smem_u32(&bars.a_full[sl]), c * 64,
-                          (int)((tA * emu::kSlices + i) * emu::kEdge));
-              ++pp.a_it;
-            }
-          }
+      for (int u = pp.ahead ? 1 : 0; u < 4; ++u)
+        if (!load_phase(tA, tB, u >> 1, u & 1)) return;
+      pp.ahead = false;
+      // start the next task's first phase now, while this task's last composition runs, if it is an
+      // update task whose dependencies were met when it was taken (only its digit planes are read
+      // before it starts; its C block waits for its own start)
+      bool ahead = false;
+      TaskKey kn{};
+      if (*(volatile int*)pf.done && *(volatile long long*)pf.next >= 0 && *(volatile int*)pf.ok) {
+        kn = *pf.key;
+        ahead = kn.type == T_SYRK || kn.type == T_GEMM;
+      }
+      *(volatile int*)pf.ahead = ahead ? 1 : 0;
+      mbar_arrive(smem_u32(&bars.decided));
+      if (ahead) {
+        const int m = kn.type == T_SYRK ? kn.b : kn.a, n = kn.b;  // SYRK(K, M): C(M,M); GEMM(M, N, K)
+        const int k = kn.type == T_SYRK ? kn.a : kn.c;
+        if (!load_phase(tri_index(m, k, P.NTb), tri_index(n, k, P.NTb), 0, 0)) return;
+        pp.ahead = true;
+      }
     }
     return;
   }
@@ -279,47 +352,16 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     if (lane == 0) {
       // consumer positions: this thread's own copy of a_it / b_it, advanced through the same
       // sequence of plane chunks as the producer's
-      uint32_t& a_it = pp.a_it;
-      uint32_t& b_it = pp.b_it;
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int ph = 0; ph < 2; ++ph) {
-          // phase A writes groups 3-6 (TMEM columns 192-447), phase B groups 0-2 (columns 0-191):
-          // each waits until the epilogue has read its columns of the previous pass
-          if (pp.passes > 0 && !mbar_wait(smem_u32(ph == 0 ? &bars.free_l : &bars.free_h), (pp.passes - 1) & 1,
-                                          err, P.timeout_ns))
-            return;
-          tc_fence_after();
-          const int np_a = ph == 0 ? emu::kSlices : 3;  // A planes of the phase
-          for (int c = 0; c < 2; ++c) {
-            const uint32_t bb = b_it % kBBufs, bph = (b_it / kBBufs) & 1;
-            if (!mbar_wait(smem_u32(&bars.b_full[bb]), bph, err, P.timeout_ns)) return;
-            tc_fence_after();
-            const uint32_t bbase = smem_u32(smB + (size_t)bb * kBSetBytes);
-            for (int i = 0; i < np_a; ++i) {
-              const uint32_t sl = a_it % kASlots, aph = (a_it / kASlots) & 1;
-              if (!mbar_wait(smem_u32(&bars.a_full[sl]), aph, err, P.timeout_ns)) return;
-              tc_fence_after();
-              const uint64_t ad = desc_kmajor_sw128(smem_u32(smA + (size_t)sl * kABytes));
-              // A_i against its B planes j of the phase's groups g = i + j at once: the planes are
-              // consecutive 64-row blocks of one K-major tile and the groups consecutive 64-column
-              // blocks of TMEM. Phase A: g = max(i,3)..6 (N <= 256); phase B: g = i..2.
-              const int g0 = ph == 0 ? (i > 3 ? i : 3) : i, g1 = ph == 0 ? 6 : 2;
-              const int np = g1 - g0 + 1;
-              const uint64_t bd = desc_kmajor_sw128(bbase + (uint32_t)(g0 - i) * kBBytes);
-              const uint32_t d = tmem + (uint32_t)(g0 * 64), id = idesc_f16(128, 64 * np, true);
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks)  // i = 0 first touches every group of the phase
-                umma_f16(d, ad + 2 * ks, bd + 2 * ks, id, (c | i | ks) != 0 ? 1u : 0u);
-              pp.mma_issued = true;
-              umma_commit(smem_u32(&bars.a_empty[sl]));
-              ++a_it;
-            }
-            umma_commit(smem_u32(&bars.b_empty[bb]));
-            ++b_it;
-          }
-          umma_commit(smem_u32(ph == 0 ? &bars.done_a : &bars.done_b));
-        }
-        ++pp.passes;
+      for (int u = pp.ahead ? 1 : 0; u < 4; ++u) {
+        if (!issue_phase(u & 1)) return;
+        if (u & 1) ++pp.passes;
+      }
+      pp.ahead = false;
+      if (!mbar_wait(smem_u32(&bars.decided), pp.tasks & 1, err, P.timeout_ns)) return;
+      ++pp.tasks;
+      if (*(volatile int*)pf.ahead) {
+        if (!issue_phase(0)) return;
+        pp.ahead = true;
       }
     }
     return;
@@ -420,7 +462,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
   uint8_t* dsmem = kEmu ? (uint8_t*)(((uintptr_t)dsmem_raw + 1023) & ~(uintptr_t)1023) : dsmem_raw;
   double* smem = (double*)dsmem;
   __shared__ long long s_task, s_next;
-  __shared__ int s_go, s_failed, s_next_ok;
+  __shared__ int s_go, s_failed, s_next_ok, s_next_done, s_ahead;
   __shared__ TaskKey s_key, s_next_key;
   __shared__ __align__(8) emuk::Bars bars;
   __shared__ uint32_t tmem_slot;
@@ -445,6 +487,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       mbar_init(smem_u32(&bars.done_b), 1);
       mbar_init(smem_u32(&bars.free_l), emuk::kEpiWarps);
       mbar_init(smem_u32(&bars.free_h), emuk::kEpiWarps);
+      mbar_init(smem_u32(&bars.decided), 1);
       mbar_init(smem_u32(&bars.fin), 1);
       mbar_fence_init();
     }
@@ -455,7 +498,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
   }
   // kEmu: the next task is taken while the current one runs (prefetch_next)
   if (threadIdx.x == 0) s_next = -2;  // none prefetched
-  const Prefetch pf{&s_next, &s_next_ok, &s_next_key};
+  const Prefetch pf{&s_next, &s_next_ok, &s_next_key, &s_next_done, &s_ahead};
   for (;;) {
     if (threadIdx.x == 0) {
       long long t = -1;
@@ -469,6 +512,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
       s_task = (t >= 0 && t < P.ntasks) ? t : -1;
       s_failed = 0;
       s_next = -2;
+      s_next_done = 0;
       if (s_task >= 0) {
         const TaskKey k = ready ? s_next_key : dag_decode(s_task, NTb, P.lead);
         s_key = k;
