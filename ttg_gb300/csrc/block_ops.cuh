@@ -36,7 +36,7 @@ __device__ __forceinline__ void lds4(const double* p, double (&v)[4]) {
 
 // pivot of the Cholesky column: l = sqrt(d) and 1/l. FP32: hardware reciprocal square root with
 // one Newton step (r <- r (3 - d r^2) / 2), a few ulp, short latency on the factor's serial chain;
-// FP64: IEEE sqrt and division.
+// FP64: rsqrt (within an ulp or two) and one multiply.
 __device__ __forceinline__ void chol_pivot(float d, float& l, float& inv) {
   float r = rsqrtf(d);
   r = r * fmaf(-0.5f * d * r, r, 1.5f);
@@ -44,8 +44,8 @@ __device__ __forceinline__ void chol_pivot(float d, float& l, float& inv) {
   l = d * r;
 }
 __device__ __forceinline__ void chol_pivot(double d, double& l, double& inv) {
-  l = sqrt(d);
-  inv = 1.0 / l;
+  inv = rsqrt(d);  // about half the FP64 work of sqrt and a division (each FP64 op is slow on GB300)
+  l = d * inv;
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -151,8 +151,11 @@ __device__ __forceinline__ float rcp_nr(float d) {
 // ------------------------------------------------------------------------------------------------
 // One row of a 32-column panel held in registers: x := x * L_blk^{-T} (row-wise forward
 // substitution against the panel's lower triangle Lp, column-major with leading dimension ldp).
+// rinv (optional): the 32 reciprocals of the panel's diagonal at rinv[rinv_at(c)], computed once
+// for all rows (an FP64 division per row and column is ~500 clocks of a warp on GB300).
+__device__ __forceinline__ int rinv_at(int c, int ldp) { return (c & 15) + ldp * (16 + (c >> 4)); }
 template <typename T>
-__device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, int pw) {
+__device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, int pw, const T* rinv = nullptr) {
 #pragma unroll
   for (int c = 0; c < 32; ++c) {
     if (c < pw) {
@@ -163,9 +166,18 @@ __device__ __forceinline__ void row_solve32(T (&x)[32], const T* Lp, int ldp, in
         s1 = fma(-x[c2 + 1], Lp[c + ldp * (c2 + 1)], s1);
       }
       if (c & 1) s0 = fma(-x[c - 1], Lp[c + ldp * (c - 1)], s0);
-      x[c] = (s0 + s1) * (T(1) / Lp[c + ldp * c]);  // the reciprocal does not depend on x: off the chain
+      // the reciprocal does not depend on x: off the chain
+      x[c] = (s0 + s1) * (rinv ? rinv[rinv_at(c, ldp)] : (T(1) / Lp[c + ldp * c]));
     }
   }
+}
+// the reciprocals of a 32 x 32 lower panel Lp (column-major, ldp) into its strict upper triangle at
+// rinv_at(c): rows 0-15 of columns 16 and 17, never read as part of the lower triangle. One warp.
+template <typename T>
+__device__ __forceinline__ void panel_reciprocals(T* Lp, int ldp, int pw, int lane) {
+  const T v = lane < pw ? T(1) / Lp[lane + ldp * lane] : T(0);
+  __syncwarp();
+  Lp[rinv_at(lane, ldp)] = v;
 }
 
 // The same solve column by column for a full FP32 panel: once x(c) is final it is subtracted from
@@ -216,6 +228,7 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
           }
           T ljj, inv;
           chol_pivot(d, ljj, inv);
+          if (lane == 0) S[p0 + rinv_at(j, kBlk) + kBlk * p0] = inv;  // for the rows below the block
           // column j of L in every lane (0 above the diagonal); selects, not branches, so the
           // warp never diverges inside the column loop
           const T lij = lane == j ? ljj : (lane > j ? x[j] * inv : T(0));
@@ -242,7 +255,7 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
       T x[32];
 #pragma unroll
       for (int c = 0; c < 32; ++c) x[c] = c < pw ? S[r + kBlk * (p0 + c)] : T(0);
-      row_solve32<T>(x, S + p0 + kBlk * p0, kBlk, pw);
+      row_solve32<T>(x, S + p0 + kBlk * p0, kBlk, pw, S + p0 + kBlk * p0);
 #pragma unroll
       for (int c = 0; c < 32; ++c)
         if (c < pw) S[r + kBlk * (p0 + c)] = x[c];
@@ -387,6 +400,10 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
         for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + 4 * tx + i] -= acc[i][j];
       ops_sync<kNamed>();
     }
+    if (!kColSolve) {  // the panel's reciprocals once, into Ld's unused upper triangle
+      if (tid < 32) panel_reciprocals<T>(Ld, kPW, pw, tid);
+      ops_sync<kNamed>();
+    }
     // each thread solves its row of the panel in registers; the column-wise solve synchronises its
     // warp, so it runs on whole warps (rows past m are zero in P and are never stored back)
     const int solvers = kColSolve ? ((m + 31) & ~31) : m;
@@ -399,7 +416,7 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
         if (pw == kPW) col_solve32(x, Ld, kPW);
         else row_solve32<T>(x, Ld, kPW, pw);
       } else {
-        row_solve32<T>(x, Ld, kPW, pw);  // Ld holds L(p0+c, p0+c2) at c + 32*c2
+        row_solve32<T>(x, Ld, kPW, pw, Ld);  // Ld holds L(p0+c, p0+c2) at c + 32*c2
       }
 #pragma unroll
       for (int c = 0; c < kPW; ++c) P[c * kBlk + r] = x[c];
