@@ -432,9 +432,10 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
 
 
 // Triangular solves of one right-hand side held in shared memory xs[0..n) against the lower
-// factor L (column-major, ld), by 32-column panels: warp 0 solves the panel's triangle with
-// __syncwarp only, then the whole CTA applies the panel to the other rows (two CTA barriers per
-// panel instead of two per column).
+// factor L (column-major, ld), by 32-column panels: warp 0 solves the panel's triangle with its
+// rows in registers, the solved value broadcast by a shuffle and the diagonal's reciprocals taken
+// once per panel (an FP64 division is ~500 clocks of a warp on GB300), then the whole CTA applies
+// the panel to the other rows (two CTA barriers per panel instead of two per column).
 template <typename T>
 __device__ void fwd_solve(const T* L, int n, int ld, T* xs) {  // L y = x
   __shared__ T tri[32 * 33];  // the panel's 32 x 32 triangle, staged once per panel
@@ -446,13 +447,15 @@ __device__ void fwd_solve(const T* L, int n, int ld, T* xs) {  // L y = x
       tri[r + 33 * c] = (r < pw && c < pw && r >= c) ? L[(p0 + r) + (long long)(p0 + c) * ld] : T(0);
     }
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 0) {  // lane = row of the panel, x in a register; the reciprocals once per panel
+      T x = lane < pw ? xs[p0 + lane] : T(0);
+      const T ri = lane < pw ? T(1) / tri[lane * 34] : T(0);
       for (int c = 0; c < pw; ++c) {
-        if (lane == c) xs[p0 + c] /= tri[c + 33 * c];
-        __syncwarp();
-        if (lane > c && lane < pw) xs[p0 + lane] -= tri[lane + 33 * c] * xs[p0 + c];
-        __syncwarp();
+        const T xc = __shfl_sync(0xffffffffu, x * ri, c);
+        if (lane == c) x = xc;
+        else if (lane > c) x = fma(-tri[lane + 33 * c], xc, x);
       }
+      if (lane < pw) xs[p0 + lane] = x;
     }
     __syncthreads();
     for (int i = p0 + pw + tid; i < n; i += blockDim.x) {
@@ -485,13 +488,15 @@ __device__ void bwd_solve(const T* L, int n, int ld, T* xs) {  // L^T x = y
       tri[r + 33 * c] = (r < pw && c < pw && r >= c) ? L[(p0 + r) + (long long)(p0 + c) * ld] : T(0);
     }
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 0) {  // as in fwd_solve, from the last row up
+      T x = lane < pw ? xs[p0 + lane] : T(0);
+      const T ri = lane < pw ? T(1) / tri[lane * 34] : T(0);
       for (int c = pw - 1; c >= 0; --c) {
-        if (lane == c) xs[p0 + c] /= tri[c + 33 * c];
-        __syncwarp();
-        if (lane < c) xs[p0 + lane] -= tri[c + 33 * lane] * xs[p0 + c];
-        __syncwarp();
+        const T xc = __shfl_sync(0xffffffffu, x * ri, c);
+        if (lane == c) x = xc;
+        else if (lane < c) x = fma(-tri[c + 33 * lane], xc, x);
       }
+      if (lane < pw) xs[p0 + lane] = x;
     }
     __syncthreads();
   }
