@@ -53,6 +53,23 @@ def test_emulated_updates_match_oracle(gbx, cuda, emu, gen, N, NB):
     assert oracle.frob_residual(L, A0) <= 1e-15
 
 
+@pytest.mark.parametrize("spread", [0.0, 2.5])
+def test_emulated_updates_graded_scaling(gbx, cuda, emu, spread):
+    """D A D with D = 10^U(-spread, spread): rows of L over five orders of magnitude (the per-row
+    scales of the digit planes) and ill-conditioned diagonal blocks (condition ~1e5)."""
+    N, NB = 1536, 384
+    A = oracle.uniform_sym_full(N, 11)
+    d = 10.0 ** np.random.default_rng(3).uniform(-spread, spread, N)
+    A = A * d[:, None] * d[None, :]
+    t0 = oracle.tiles_from_full(A, NB)
+    t = to_dev(t0, cuda)
+    work = gbx.potrf_tiled(t, N, NB)
+    assert gbx.potrf_status(work) == 0
+    L = oracle.tiles_to_lower(t.cpu().numpy(), N, NB)
+    assert_factor_close(L, _oracle_factor(t0, N, NB))
+    assert oracle.frob_residual(L, A) <= 1e-15
+
+
 def test_emulated_updates_8192(gbx, cuda, emu):
     """The checked size of the N=32768 configuration (128-blocks by default at this size)."""
     if not oracle.load_openblas():
