@@ -213,7 +213,57 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
   int info = 0;
   for (int p0 = 0; p0 < n; p0 += 32) {
     const int pw = min(32, n - p0);
-    if (warp == 0) {
+    if (sizeof(T) == 8 && warp < 4) {
+      // FP64: the 32 x 32 diagonal block on four warps, warp w holding columns 8w..8w+7 of every
+      // row (lane = row). Per column j the owner warp takes the pivot and publishes column j of L;
+      // after one barrier every warp applies it to its columns, the next pivot's column first, so
+      // only the pivot and one FMA per column stay on the serial chain (each warp-wide FP64
+      // instruction occupies a GB300 SM sub-partition for 64 clocks)
+      T* colbuf = S + p0 + kBlk * (p0 + 20);  // [2][32] at rows 0-15 of columns 20-23: upper, unused
+      auto cb = [&](int b, int r) -> T& { return colbuf[(r & 15) + kBlk * (2 * b + (r >> 4))]; };
+      T xw[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int c = 8 * warp + q;
+        xw[q] = (lane < pw && c <= lane) ? S[(p0 + lane) + kBlk * (p0 + c)] : T(0);
+      }
+      for (int j = 0; j < pw; ++j) {
+        if (warp == (j >> 3)) {
+          T xj = T(0);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) xj = q == (j & 7) ? xw[q] : xj;
+          const T d = __shfl_sync(0xffffffffu, xj, j);
+          if (!(d > T(0))) {
+            if (lane == 0) *flag = p0 + j + 1;
+          } else {
+            T ljj, inv;
+            chol_pivot(d, ljj, inv);
+            if (lane == 0) S[p0 + rinv_at(j, kBlk) + kBlk * p0] = inv;  // for the rows below the block
+            const T lij = lane == j ? ljj : (lane > j ? xj * inv : T(0));
+#pragma unroll
+            for (int q = 0; q < 8; ++q) xw[q] = q == (j & 7) ? lij : xw[q];
+            cb(j & 1, lane) = lij;
+          }
+        }
+        asm volatile("bar.sync 2, 128;" ::: "memory");
+        if (*(volatile int*)flag) break;
+        const T lj = cb(j & 1, lane);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int cc = 8 * warp + q;
+          if (cc > j && cc < pw) {
+            const T upd = fma(-lj, cb(j & 1, cc), xw[q]);
+            xw[q] = lane >= cc ? upd : xw[q];
+          }
+        }
+      }
+      if (*(volatile int*)flag == 0 && lane < pw)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int c = 8 * warp + q;
+          if (c <= lane && c < pw) S[(p0 + lane) + kBlk * (p0 + c)] = xw[q];
+        }
+    } else if (sizeof(T) == 4 && warp == 0) {
       // 32 x 32 diagonal block: lane = row, the row in registers, columns exchanged by shuffles
       T x[32];
 #pragma unroll
