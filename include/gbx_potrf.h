@@ -428,7 +428,7 @@ long long gbx_dag_task(int NTb, long long t, int* key);
  * TRSMs (the emulated executor's order; lead 0 is gbx_dag_task's). */
 long long gbx_dag_task_lead(int NTb, long long lead, long long t, int* key);
 /* Tasks of each step's trailing updates the executor queues ahead of the step's TRSMs: -1 (default)
- * automatic (24 per CTA with tensor-core updates, none with FP64 FMA updates), else that count.
+ * automatic (16 per CTA with tensor-core updates, none with FP64 FMA updates), else that count.
  * Returns 0 or GBX_ERR_ARG. */
 int gbx_set_dag_lead(long long tasks);
 long long gbx_mixed_task(int NT, long long t, int* key);

@@ -1003,10 +1003,11 @@ int launch_dag(const BlockView& V, int NTb, void* work, size_t work_bytes, cudaS
   }
   long long grid = (long long)di.sms * (emu ? 1 : di.dag_blocks_per_sm);
   grid = std::max(1LL, std::min(grid, P.ntasks));
-  // emulated updates: a POTRF takes about twelve update tasks' time; 24 tasks per CTA ahead of each
-  // step's TRSMs measured best (N=32768: 0 -> 859 ms, 12/CTA 815, 24/CTA 796, 48/CTA 800). The FP64
-  // FMA form keeps its order (its update tasks take longer than a POTRF).
-  P.lead = g_dag_lead >= 0 ? g_dag_lead : (emu ? 24 * grid : 0);
+  // emulated updates: a POTRF (~350 us) takes about fourteen update tasks' time (~25 us); 16 tasks
+  // per CTA ahead of each step's TRSMs measured best (N=32768: 8/CTA 629 ms, 12 617, 16 606, 24 608;
+  // N=16384: 120, 117, 116, 118 ms). The FP64 FMA form keeps its order (its update tasks take
+  // longer than a POTRF).
+  P.lead = g_dag_lead >= 0 ? g_dag_lead : (emu ? 16 * grid : 0);
   if (emu) potrf_dag_f64_kernel<true><<<(unsigned)grid, emuk::kThreadsEmu, emuk::kSmemBytes, s>>>(ta, tb, P);
   else potrf_dag_f64_kernel<false><<<(unsigned)grid, kThreads, kDagSmemBytes, s>>>(ta, tb, P);
   return cudaGetLastError() == cudaSuccess ? GBX_OK : GBX_ERR_CUDA;
