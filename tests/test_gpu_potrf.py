@@ -362,7 +362,8 @@ def test_task_timeline_trace(gbx, cuda, tmp_path, edge, ntb):
         gbx.lib().gbx_set_trace_buffer(None, 0)
         gbx.lib().gbx_set_dag_block_edge(0)
     recs = gbx.trace_records(buf)
-    assert len(recs) == ntb + ntb * (ntb - 1) + ntb * (ntb - 1) * (ntb - 2) // 6
+    # every task once; TRSM(K+1,K) (on the critical path) as 4 row sub-tasks
+    assert len(recs) == ntb + ntb * (ntb - 1) + ntb * (ntb - 1) * (ntb - 2) // 6 + 3 * (ntb - 1)
     assert all(r["end_ns"] >= r["start_ns"] for r in recs)
     pot = {r["a"]: r for r in recs if r["type"] == "POTRF"}
     trsm = [r for r in recs if r["type"] == "TRSM"]

@@ -427,27 +427,46 @@ __device__ void op_trsm(const T* __restrict__ L, int ldl, T* B, int ldb, int m, 
         for (int u = 0; u < (KC * kPW + kThreads - 1) / kThreads; ++u)
           if (tid + u * kThreads < KC * kPW) Lc[tid + u * kThreads] = rl[u];
       };
+      // m <= 32 (a row sub-task): lane = row, warp = four columns, so that no FP64 instruction
+      // works on absent rows (a warp-wide FP64 instruction costs the same with any active lanes)
+      const bool narrow = m <= 32;
       gload(0);
       for (int k0 = 0; k0 < p0; k0 += KC) {
         sstore();
         ops_sync<kNamed>();
         if (k0 + KC < p0) gload(k0 + KC);
+        if (narrow) {
 #pragma unroll
-        for (int kk = 0; kk < KC; ++kk) {  // rows 4tx..4tx+3 x columns 4ty..4ty+3, vector loads
-          T a[4], b[4];
-          lds4(Xc + kk * kBlk + 4 * tx, a);
-          lds4(Lc + kk * kPW + 4 * ty, b);
+          for (int kk = 0; kk < KC; ++kk) {  // row tx x columns 4ty..4ty+3
+            const T a = Xc[kk * kBlk + tx];
+            T b[4];
+            lds4(Lc + kk * kPW + 4 * ty, b);
 #pragma unroll
-          for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) acc[0][j] = fma(a, b[j], acc[0][j]);
+          }
+        } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int kk = 0; kk < KC; ++kk) {  // rows 4tx..4tx+3 x columns 4ty..4ty+3, vector loads
+            T a[4], b[4];
+            lds4(Xc + kk * kBlk + 4 * tx, a);
+            lds4(Lc + kk * kPW + 4 * ty, b);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          }
         }
         ops_sync<kNamed>();
       }
+      if (narrow) {
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + tx] -= acc[0][j];
+      } else {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + 4 * tx + i] -= acc[i][j];
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) P[(4 * ty + j) * kBlk + 4 * tx + i] -= acc[i][j];
+      }
       ops_sync<kNamed>();
     }
     if (!kColSolve) {  // the panel's reciprocals once, into Ld's unused upper triangle

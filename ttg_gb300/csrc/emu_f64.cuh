@@ -40,27 +40,33 @@ __device__ __forceinline__ uint32_t digit_bf16(int d) {
   return __float_as_uint(f) >> 16;
 }
 
-// Splits the FP64 block L (m x n valid of a 128 x 128 block, column-major, leading dimension ld)
-// into kSlices bf16 digit planes S[i][r][k] (row-major, k contiguous, zero outside m x n) and the
-// row exponents rexp[r]. Threads 0..255 of the CTA (synchronised with named barrier 1);
-// s_exp: 256 ints of shared memory.
+// Splits kRows rows of an FP64 block (m x n valid, m <= kRows, column-major, leading dimension ld)
+// into kSlices bf16 digit planes S[i][r][k] (row-major, k contiguous, plane stride kPlaneElems,
+// zero outside m x n) and the row exponents rexp[r]: the whole 128-row block, or (kRows = 32) the
+// rows of one TRSM sub-task, leaving the other rows alone. Threads 0..255 of the CTA: thread t
+// handles row t % kRows and part t / kRows of the 256 / kRows parts of k (synchronised with named
+// barrier 1); s_exp: 256 ints of shared memory.
+template <int kRows = kEdge>
 __device__ __forceinline__ void slice_block(const double* __restrict__ L, int ld, int m, int n,
                                             uint16_t* __restrict__ S, int* __restrict__ rexp, int* s_exp) {
-  const int r = threadIdx.x & (kEdge - 1), h = threadIdx.x >> 7;  // row, column half
-  const int k0 = h * (kEdge / 2);
+  constexpr int kParts = 256 / kRows, kSpan = kEdge / kParts;  // k-range parts, elements per part
+  static_assert(kSpan % 8 == 0, "whole 16-byte stores");
+  const int r = threadIdx.x % kRows, h = threadIdx.x / kRows;
+  const int k0 = h * kSpan;
   // 1. largest biased exponent in the row (integer compare of the exponent fields)
   int mex = 0;
   if (r < m)
-    for (int k = k0; k < min(k0 + kEdge / 2, n); ++k) mex = max(mex, (__double2hiint(__ldcg(L + r + (long long)k * ld)) >> 20) & 0x7ff);
-  s_exp[h * kEdge + r] = mex;
+    for (int k = k0; k < min(k0 + kSpan, n); ++k) mex = max(mex, (__double2hiint(__ldcg(L + r + (long long)k * ld)) >> 20) & 0x7ff);
+  s_exp[h * kRows + r] = mex;
   asm volatile("bar.sync 1, 256;" ::: "memory");
-  mex = max(s_exp[r], s_exp[kEdge + r]);
+#pragma unroll
+  for (int q = 0; q < kParts; ++q) mex = max(mex, s_exp[q * kRows + r]);
   asm volatile("bar.sync 1, 256;" ::: "memory");
   // every |L(r,k)| < 2^e (frexp exponent of the largest); rows of zeros and subnormals give no digits
   const int e = mex - 1022;
   if (h == 0) rexp[r] = (mex > 0) ? e : kEmptyRow;
   // 2. fixed point and digits, eight consecutive k per 16-byte store of each plane
-  for (int kc = 0; kc < kEdge / 2; kc += 8) {
+  for (int kc = 0; kc < kSpan; kc += 8) {
     uint32_t pk[kSlices][4];
 #pragma unroll
     for (int i = 0; i < kSlices; ++i)

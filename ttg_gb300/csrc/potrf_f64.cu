@@ -37,32 +37,50 @@ constexpr size_t kDagSmemBytes = (size_t)kBlk * kBlk * sizeof(double) + 64;  // 
 //   for k = 0 .. NTb-2:
 //     panel part (column k+1): SYRK(k,k+1), GEMM(m,k+1,k) m>k+1, POTRF(k+1), TRSM(m,k+1) m>k+1
 //     trailing part: for n = k+2..: SYRK(k,n), GEMM(m,n,k) m>n
+// The TRSM of the block just below a diagonal block, TRSM(K+1,K), is on the critical path
+// POTRF(K) -> TRSM(K+1,K) -> SYRK(K,K+1) -> POTRF(K+1): it runs as kTrsmParts row sub-tasks
+// (key c = sub-task) on as many CTAs, and its block counts as final after all of them.
 // Every task's predecessors come earlier in this order, so CTAs that take tasks in order and
 // wait for their predecessors always make progress.
 // ------------------------------------------------------------------------------------------------
 enum : int { T_POTRF = 0, T_TRSM = 1, T_SYRK = 2, T_GEMM = 3 };
+constexpr int kTrsmParts = 4;
 
 struct TaskKey {
   int type, a, b, c;
 };
 
+// TRSM completions block (M,K) counts before it is final
+__host__ __device__ __forceinline__ int trsm_parts(int M, int K) { return M == K + 1 ? kTrsmParts : 1; }
+
 __host__ __device__ __forceinline__ long long seg_prefix(long long k, long long R) {
-  // sum over j < k of seg(j) = 2 r + r (r-1) / 2 with r = R - j
+  // sum over j < k of seg(j) = 2 r + r (r-1) / 2 (+ kTrsmParts - 1 when r >= 2, the split TRSM)
+  // with r = R - j
   const long long s1 = k * R - k * (k - 1) / 2;
   const long long s2 = k * R * R - R * k * (k - 1) + (k - 1) * k * (2 * k - 1) / 6;
-  return (3 * s1 + s2) / 2;
+  const long long split = k < R - 1 ? k : (R - 1 > 0 ? R - 1 : 0);  // steps j < k with R - j >= 2
+  return (3 * s1 + s2) / 2 + (kTrsmParts - 1) * split;
+}
+
+__host__ __device__ __forceinline__ long long dag_prologue(int NTb) {
+  return NTb + (NTb >= 2 ? kTrsmParts - 1 : 0);
 }
 
 __host__ __device__ __forceinline__ long long dag_num_tasks(int NTb) {
-  return NTb + seg_prefix(NTb - 1, NTb - 1);
+  return dag_prologue(NTb) + seg_prefix(NTb - 1, NTb - 1);
 }
 
 // lead > 0 (the emulated executor): the first `lead` tasks of each step's trailing part go ahead of
 // that step's TRSMs, so that the CTAs which take the TRSMs find their POTRF done instead of waiting
 // for it (the order stays topological: trailing tasks of step k need only TRSMs of step k - 1).
 __host__ __device__ inline TaskKey dag_decode(long long t, int NTb, long long lead = 0) {
-  if (t < NTb) return t == 0 ? TaskKey{T_POTRF, 0, 0, 0} : TaskKey{T_TRSM, (int)t, 0, 0};
-  const long long u = t - NTb, R = NTb - 1;
+  const long long P0 = dag_prologue(NTb);
+  if (t < P0) {
+    if (t == 0) return TaskKey{T_POTRF, 0, 0, 0};
+    if (t <= kTrsmParts) return TaskKey{T_TRSM, 1, 0, (int)(t - 1)};
+    return TaskKey{T_TRSM, (int)(t - (kTrsmParts - 1)), 0, 0};
+  }
+  const long long u = t - P0, R = NTb - 1;
   int lo = 0, hi = NTb - 2;  // largest k with seg_prefix(k) <= u
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -77,10 +95,14 @@ __host__ __device__ inline TaskKey dag_decode(long long t, int NTb, long long le
   if (p == r) return TaskKey{T_POTRF, k + 1, 0, 0};
   const long long q = r - 1;  // trailing columns n = k+2 .. NTb-1: q (q + 1) / 2 tasks
   const long long X = lead < q * (q + 1) / 2 ? lead : q * (q + 1) / 2;
+  const long long nts = q + (q > 0 ? kTrsmParts - 1 : 0);  // TRSM slots: TRSM(k+2,k+1) split
   long long pp;
   if (p <= r + X) pp = p - r - 1;  // the leading trailing tasks
-  else if (p < 2 * (long long)r + X) return TaskKey{T_TRSM, k + 1 + (int)(p - r - X), k + 1, 0};
-  else pp = p - 2 * (long long)r;
+  else if (p < r + 1 + X + nts) {
+    const long long s = p - (r + 1 + X);
+    if (s < kTrsmParts) return TaskKey{T_TRSM, k + 2, k + 1, (int)s};
+    return TaskKey{T_TRSM, k + 2 + (int)(s - (kTrsmParts - 1)), k + 1, 0};
+  } else pp = p - (r + 1 + nts);
   int clo = 0, chi = (int)q - 1;                           // largest c with S(c) <= pp
   while (clo < chi) {
     const int mid = (clo + chi + 1) >> 1;
@@ -122,12 +144,12 @@ __device__ __forceinline__ int dag_deps(const DagParams& P, const TaskKey& k, co
       c[1] = P.cnt + tri_index(k.a, k.b, NTb), v[1] = k.b;
       return 2;
     case T_SYRK:
-      c[0] = P.cnt + tri_index(k.b, k.a, NTb), v[0] = k.a + 1;
+      c[0] = P.cnt + tri_index(k.b, k.a, NTb), v[0] = k.a + trsm_parts(k.b, k.a);
       c[1] = P.cnt + tri_index(k.b, k.b, NTb), v[1] = k.a;
       return 2;
     default:
-      c[0] = P.cnt + tri_index(k.a, k.c, NTb), v[0] = k.c + 1;
-      c[1] = P.cnt + tri_index(k.b, k.c, NTb), v[1] = k.c + 1;
+      c[0] = P.cnt + tri_index(k.a, k.c, NTb), v[0] = k.c + trsm_parts(k.a, k.c);
+      c[1] = P.cnt + tri_index(k.b, k.c, NTb), v[1] = k.c + trsm_parts(k.b, k.c);
       c[2] = P.cnt + tri_index(k.a, k.b, NTb), v[2] = k.c;
       return 3;
   }
@@ -447,12 +469,12 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
 }
 
 // Persistent executor: one CTA per SM takes tasks from the ready queue in order.
-// Counter protocol (writers of block (M,N) in order: GEMM(M,N,0..N-1), then TRSM(M,N); of (M,M):
-// SYRK(0..M-1,M), then POTRF(M)):
+// Counter protocol (writers of block (M,N) in order: GEMM(M,N,0..N-1), then TRSM(M,N), as
+// p(M,N) = trsm_parts(M,N) sub-tasks; of (M,M): SYRK(0..M-1,M), then POTRF(M)):
 //   POTRF(K):      cnt(K,K) >= K
 //   TRSM(M,K):     cnt(K,K) >= K+1, cnt(M,K) >= K
-//   SYRK(K,M):     cnt(M,K) >= K+1, cnt(M,M) >= K
-//   GEMM(M,N,K):   cnt(M,K) >= K+1, cnt(N,K) >= K+1, cnt(M,N) >= K
+//   SYRK(K,M):     cnt(M,K) >= K+p(M,K), cnt(M,M) >= K
+//   GEMM(M,N,K):   cnt(M,K) >= K+p(M,K), cnt(N,K) >= K+p(N,K), cnt(M,N) >= K
 // kEmu: SYRK and GEMM run on the tensor cores (emu_update) from the digit planes that each TRSM
 // writes of its block before it signals; POTRF and TRSM stay FP64.
 template <bool kEmu>
@@ -542,16 +564,23 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
         target = P.cnt + tri_index(K, K, NTb);
         break;
       }
-      case T_TRSM: {
+      case T_TRSM: {  // the whole block, or (TRSM(K+1,K)) rows r0 .. r0 + V.b / kTrsmParts of it
         const int M = tk.a, K = tk.b;
-        if (threadIdx.x < kThreads) {
-          op_trsm<double, false, kEmu>(V.ptr(K, K), V.ld, V.ptr(M, K), V.ld, V.dim(M), V.dim(K), smem);
+        const int parts = trsm_parts(M, K), rows = V.b / parts;
+        const int r0 = tk.c * rows, mr = min(rows, V.dim(M) - r0);
+        if (threadIdx.x < kThreads && mr > 0) {
+          op_trsm<double, false, kEmu>(V.ptr(K, K), V.ld, V.ptr(M, K) + r0, V.ld, mr, V.dim(K), smem);
           if (kEmu) {
-            // the block is final in global memory (each thread's own writes before the barrier)
+            // the rows are final in global memory (each thread's own writes before the barrier)
             asm volatile("bar.sync 1, 256;" ::: "memory");
             const long long tb = tri_index(M, K, NTb);
-            emu::slice_block(V.ptr(M, K), V.ld, V.dim(M), V.dim(K), P.planes + tb * emu::kBlockElems,
-                             P.rexp + tb * emu::kEdge, s_aux);
+            if (parts == 1)
+              emu::slice_block(V.ptr(M, K), V.ld, V.dim(M), V.dim(K), P.planes + tb * emu::kBlockElems,
+                               P.rexp + tb * emu::kEdge, s_aux);
+            else
+              emu::slice_block<emu::kEdge / kTrsmParts>(V.ptr(M, K) + r0, V.ld, mr, V.dim(K),
+                                                        P.planes + tb * emu::kBlockElems + (long long)r0 * emu::kEdge,
+                                                        P.rexp + tb * emu::kEdge + r0, s_aux);
           }
         } else if (kEmu && threadIdx.x == 32 * emuk::kProducerWarp + 1) {
           prefetch_next(P, t, pf);
