@@ -4,8 +4,10 @@ with Python integers and checked against exact rationals (CPU):
     each of at most 8 significant bits (exact in bf16);
   * products: group sums acc_g = sum_{i+j=g} sum_k a_i b_j for g <= 6 stay below 2^24 in magnitude
     for k = 128 (exact in the tensor cores' FP32 accumulation);
-  * composition: X = H 2^32 + L in 64 bits (X 2^-8 when |H| >= 2^30), rounded once to FP64.
+  * composition: X = H 2^32 + L in 64 bits (X 2^-8 when |H| >= 2^30), rounded once to FP64 and
+    scaled by a power of two.
 The emulated dot product must be at least as accurate as a plain FP64 loop over the same inputs."""
+import math
 import struct
 from fractions import Fraction
 
@@ -42,23 +44,14 @@ def split_row(row):
 
 
 def compose(acc, E):
+    """X 2^E as the executor forms it: X = sum_g acc_g 2^(8(6-g)) in 64 bits (as X 2^-s when the
+    high groups are large), rounded to FP64 (to nearest even), then scaled by 2^(s + E)."""
     H = (acc[0] << 16) + (acc[1] << 8) + acc[2]
     L = (acc[3] << 24) + (acc[4] << 16) + (acc[5] << 8) + acc[6]
     s = 8 if abs(H) >= 2 ** 30 else 0
     X = (H << (32 - s)) + (L >> s)  # >> floors, as the arithmetic shift does
     assert abs(X) < 2 ** 63
-    if X == 0:
-        return 0.0
-    u = abs(X)
-    z = 64 - u.bit_length()
-    top = (u << z) & ((1 << 64) - 1)
-    p = 63 - z
-    mant = (top >> 11) + ((top >> 10) & 1)
-    if mant >> 53:
-        mant >>= 1
-        p += 1
-    v = float(mant) * 2.0 ** (p - 52 + E + s)
-    return -v if X < 0 else v
+    return math.ldexp(float(X), E + s)  # float(int) rounds to nearest even
 
 
 def emulated_dot(a, b):

@@ -70,6 +70,25 @@ def test_emulated_updates_graded_scaling(gbx, cuda, emu, spread):
     assert oracle.frob_residual(L, A) <= 1e-15
 
 
+@pytest.mark.parametrize("lo,hi", [(-490, -490), (-490, -100)])
+def test_emulated_updates_extreme_scales(gbx, cuda, emu, lo, hi):
+    """D A D with D = 2^round(U(lo, hi)): update products near 1e-295, where the power of two 2^E
+    that scales the digit-plane products lies below the normal FP64 range (the wide-range form of
+    the subtraction), alone or beside ordinary scales. D is a power of two per row, so D^-1 L of the
+    executor and of the oracle are the factors of A itself."""
+    N, NB = 1024, 256
+    A = oracle.uniform_sym_full(N, 5)
+    d = 2.0 ** np.round(np.random.default_rng(4).uniform(lo, hi, N))
+    t0 = oracle.tiles_from_full(A * d[:, None] * d[None, :], NB)
+    t = to_dev(t0, cuda)
+    work = gbx.potrf_tiled(t, N, NB)
+    assert gbx.potrf_status(work) == 0
+    L = oracle.tiles_to_lower(t.cpu().numpy(), N, NB) / d[:, None]
+    assert np.isfinite(L).all()
+    assert_factor_close(L, _oracle_factor(t0, N, NB) / d[:, None])
+    assert oracle.frob_residual(L, A) <= 1e-15
+
+
 def test_emulated_updates_8192(gbx, cuda, emu):
     """The checked size of the N=32768 configuration (128-blocks by default at this size)."""
     if not oracle.load_openblas():

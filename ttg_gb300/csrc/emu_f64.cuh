@@ -115,34 +115,31 @@ __device__ __forceinline__ long long group_l(uint32_t a3, uint32_t a4, uint32_t 
          (long long)__float2int_rn(__uint_as_float(a6));
 }
 
-// X 2^E as FP64, X = H 2^32 + L = sum_g acc_g 2^(8(6-g)), rounded to nearest (ties away from zero).
-// X is formed in 64 bits: exactly while |H| < 2^30 (|X| < 2^62 + 2^49), else as X 2^-8, which drops
-// only bits below 2^-54 of |X| >= 2^62. Branch-free, so that the compositions of neighbouring
-// elements interleave; *odd is set when the result leaves the normal FP64 range (the value returned
-// is then wrong: see compose_slow).
-__device__ __forceinline__ double compose(long long H, long long L, int E, bool* odd) {
-  const int s = (H >= (1LL << 30) || H <= -(1LL << 30)) ? 8 : 0;
-  const long long X = (long long)((unsigned long long)H << (32 - s)) + (L >> s);
-  const bool neg = X < 0;
-  const unsigned long long u = neg ? 0ull - (unsigned long long)X : (unsigned long long)X;
-  const int z = __clzll((long long)u);  // 64 for X = 0
-  const unsigned long long top = u << (z & 63);  // leading one at bit 63
-  int p = 63 - z + s;                            // position of X's leading one
-  unsigned long long mant = (top >> 11) + ((top >> 10) & 1);  // 53 bits, rounded
-  const bool carry = (mant >> 53) != 0;
-  mant = carry ? (mant >> 1) : mant;
-  p += carry;
-  const int be = p + E + 1023;
-  *odd = (u != 0) && (be <= 0 || be >= 2047);
-  const unsigned long long bits =
-      ((unsigned long long)neg << 63) | ((unsigned long long)(be & 0x7ff) << 52) | (mant & 0xFFFFFFFFFFFFFull);
-  return u == 0 ? 0.0 : __longlong_as_double((long long)bits);
+// X = H 2^32 + L = sum_g acc_g 2^(8(6-g)) in 64 bits, as X 2^-s: exactly (s = 0) while |H| < 2^30
+// (|X| < 2^62 + 2^49), else with s = 8, which drops only bits below 2^-54 of |X| >= 2^62
+__device__ __forceinline__ long long fold(long long H, long long L, int& s) {
+  s = (H >= (1LL << 30) || H <= -(1LL << 30)) ? 8 : 0;
+  return (long long)((unsigned long long)H << (32 - s)) + (L >> s);
 }
 
-// the same value outside the normal range (subnormal or overflowing results): scaled in FP64
-// (H and L are exact in FP64)
-__device__ __noinline__ double compose_slow(long long H, long long L, int E) {
-  return ldexp((double)H, 32 + E) + ldexp((double)L, E);
+// 2^k as FP64, -1022 <= k <= 1023
+__device__ __forceinline__ double pow2(int k) { return __hiloint2double((k + 1023) << 20, 0); }
+
+// c - X 2^sE: X rounded to FP64 (to nearest even), and the product with the power of two
+// subtracted in one FMA (exact product: subnormal and overflowing results come out of the FMA
+// rounded once). *odd is set when 2^sE is not a normal FP64 number itself (extreme scales only;
+// see sub_wide).
+__device__ __forceinline__ double sub_scaled(double c, long long X, int sE, bool* odd) {
+  *odd = (unsigned)(sE + 1022) > 2045u;
+  return fma(-__ll2double_rn(X), pow2(sE), c);
+}
+
+// the same for any sE: 2^sE as 2^a 2^b with both factors normal (X 2^a is exact for X != 0, as
+// a >= -1022), exact again up to the FMA's rounding for |sE| <= 2044; beyond, the clamped factors
+// still give the limit (a product far below the smallest subnormal, or an overflow)
+__device__ __forceinline__ double sub_wide(double c, long long X, int sE) {
+  const int a = min(max(sE / 2, -1022), 1023), b = min(max(sE - a, -1022), 1023);
+  return fma(-__ll2double_rn(X) * pow2(a), pow2(b), c);
 }
 
 }  // namespace emu

@@ -186,7 +186,10 @@ __device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey
 // 64 g .. 64 g + 63), over two 64-wide chunks of k, in two phases: A (groups 3-6, 22 of the 28
 // plane pairs) and B (groups 0-2). As soon as phase A of a pass is done the epilogue folds its four
 // groups into one 64-bit integer per element (L) and frees their columns, so the next pass's phase
-// A runs while this pass's groups 0-2 are composed with L and subtracted from C.
+// A runs while this pass's groups 0-2 are read; those are folded with L into one 64-bit X per
+// element and freed in turn, and the subtraction of X 2^E from C runs beside the next pass's
+// products (and beside the first phase of the next task, which the producer and the issuer start
+// once this task's last products are out).
 // The emulated executor runs 384 threads (twelve warps); its FP64 tasks use the first 256.
 //   warp 8 lane 0  TMA producer: per phase and chunk the phase's B planes (64 rows each) into one
 //                  of two buffers, then its A planes (128 rows each) through a ring of six slots
@@ -196,10 +199,10 @@ __device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey
 //                  and the groups consecutive 64-column blocks of TMEM, so 10 instructions per
 //                  k-step cover the 28 plane pairs (one thread issues a tcgen05.mma only every
 //                  ~110 clocks; an N=64 product takes the tensor pipe ~35). Each A slot is
-//                  released after its instructions, each B buffer after its chunk. Warps 10-11
-//                  have no part.
+//                  released after its instructions, each B buffer after its chunk.
+//   warp 10        the C block's lines into L2 ahead of the epilogue's reads; warp 11 has no part
 //   warps 0-7      epilogue: TMEM lane quarter = warp % 4, column half = warp / 4; per element the
-//                  integer group sums L (after phase A) and H (after phase B), the exact compose
+//                  integer group sums L (after phase A) and X (after phase B), the rounding of X
 //                  and one FP64 subtraction from C
 namespace emuk {
 constexpr int kASlots = 6, kBBufs = 2;
@@ -220,7 +223,7 @@ struct Pipe {  // pipeline positions, each kept by the one thread that uses it
   uint32_t a_it = 0, b_it = 0;  // producer: plane chunks issued; MMA issuer: consumed (A ring, B buffers)
   uint32_t passes = 0;          // MMA issuer and epilogue threads: accumulator passes begun
   uint32_t tasks = 0;           // MMA issuer: update tasks done (parity of the `decided` barrier)
-  bool ahead = false;           // producer / issuer: the first phase of the next task is already out
+  int ahead = 0;                // producer / issuer: phases of the next task already out (0 or 1)
   bool mma_issued = false;
 };
 }  // namespace emuk
@@ -340,16 +343,17 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     return true;
   };
   // the four phases of a task: (pass 0, A), (pass 0, B), (pass 1, A), (pass 1, B); the first is
-  // already out when the previous task started it early (pp.ahead)
+  // already out when the previous task started it early (pp.ahead). (Starting the first two early
+  // measured slower: the producer then stays in the task until ring slots free up.)
   if (warp == kProducerWarp) {
     if (lane == 0) {
       // the planes were written by other CTAs with ordinary stores, and this CTA's shared memory
       // last by its FP64 tasks: order both before the async-proxy accesses
       asm volatile("fence.proxy.async.global;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      for (int u = pp.ahead ? 1 : 0; u < 4; ++u)
+      for (int u = pp.ahead; u < 4; ++u)
         if (!load_phase(tA, tB, u >> 1, u & 1)) return;
-      pp.ahead = false;
+      pp.ahead = 0;
       // start the next task's first phase now, while this task's last composition runs, if it is an
       // update task whose dependencies were met when it was taken (only its digit planes are read
       // before it starts; its C block waits for its own start)
@@ -365,7 +369,7 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
         const int m = kn.type == T_SYRK ? kn.b : kn.a, n = kn.b;  // SYRK(K, M): C(M,M); GEMM(M, N, K)
         const int k = kn.type == T_SYRK ? kn.a : kn.c;
         if (!load_phase(tri_index(m, k, P.NTb), tri_index(n, k, P.NTb), 0, 0)) return;
-        pp.ahead = true;
+        pp.ahead = 1;
       }
     }
     return;
@@ -374,17 +378,28 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     if (lane == 0) {
       // consumer positions: this thread's own copy of a_it / b_it, advanced through the same
       // sequence of plane chunks as the producer's
-      for (int u = pp.ahead ? 1 : 0; u < 4; ++u) {
+      for (int u = pp.ahead; u < 4; ++u) {
         if (!issue_phase(u & 1)) return;
         if (u & 1) ++pp.passes;
       }
-      pp.ahead = false;
+      pp.ahead = 0;
       if (!mbar_wait(smem_u32(&bars.decided), pp.tasks & 1, err, P.timeout_ns)) return;
       ++pp.tasks;
       if (*(volatile int*)pf.ahead) {
         if (!issue_phase(0)) return;
-        pp.ahead = true;
+        pp.ahead = 1;
       }
+    }
+    return;
+  }
+  if (warp == kIssuerWarp0 + 1) {
+    // C(M,N) into L2 ahead of the epilogue's reads: every 128-byte line of its columns
+    const int mrows = V.dim(M), ncols = V.dim(Nn);
+    const double* C = V.ptr(M, Nn);
+    for (int col = lane; col < ncols; col += 32) {
+      const uintptr_t c0 = (uintptr_t)(C + (long long)col * V.ld + (syrk ? col : 0));
+      const uintptr_t c1 = (uintptr_t)(C + (long long)col * V.ld + mrows);
+      for (uintptr_t a = c0 & ~(uintptr_t)127; a < c1; a += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
     }
     return;
   }
@@ -396,20 +411,10 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     double* C = V.ptr(M, Nn);
     const int ea = (r < mrows) ? __ldcg(P.rexp + tA * emu::kEdge + r) : emu::kEmptyRow;
     const bool row_ok = r < mrows && ea != emu::kEmptyRow;
-    // C is read a chunk ahead of the one being composed (its loads in flight during the TMEM reads
-    // and the composition); stores go last, so no load waits on an earlier store
-    auto loadc = [&](double (&dst)[8], int pass, int cc) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int col = pass * 64 + h * 32 + cc + j;
-        dst[j] = (row_ok && col < ncols && (!syrk || r >= col)) ? __ldcg(C + r + (long long)col * V.ld) : 0.0;
-      }
-    };
     // the next task, while the first pass's products run (this warp waits for them otherwise)
     if (warp == kEpiWarps - 1 && lane == 0) prefetch_next(P, cur_task, pf);
     __syncwarp();
-    double cur[8], nxt[8];
-    long long Lv[32];  // group sums 3-6 of this thread's 32 columns of the pass
+    long long Xv[32];  // per column of the pass: L (groups 3-6), then X (all seven groups)
     for (int pass = 0; pass < 2; ++pass) {
       // phase A done: groups 3-6 -> L, then their TMEM columns go back to the issuer
       if (!mbar_wait(smem_u32(&bars.done_a), pp.passes & 1, err, P.timeout_ns)) return;
@@ -421,48 +426,62 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
         for (int g = 0; g < 4; ++g) tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((g + 3) * 64 + h * 32 + cc), v[g]);
         tmem_ld_wait();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) Lv[cc + j] = emu::group_l(v[0][j], v[1][j], v[2][j], v[3][j]);
+        for (int j = 0; j < 8; ++j) Xv[cc + j] = emu::group_l(v[0][j], v[1][j], v[2][j], v[3][j]);
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&bars.free_l));
-      loadc(cur, pass, 0);
-      // phase B done: groups 0-2 -> H, composed with L and subtracted from C
+      // phase B done: groups 0-2 -> H, folded with L into X; the columns go back at once, and the
+      // rounding and the subtraction from C run beside the next pass's products
       if (!mbar_wait(smem_u32(&bars.done_b), pp.passes & 1, err, P.timeout_ns)) return;
       tc_fence_after();
+      uint32_t smask = 0;  // bit c: X of column c held as X 2^-8 (emu::fold)
 #pragma unroll
       for (int cc = 0; cc < 32; cc += 8) {
         uint32_t v[3][8];
 #pragma unroll
         for (int g = 0; g < 3; ++g) tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * 64 + h * 32 + cc), v[g]);
-        if (cc + 8 < 32) loadc(nxt, pass, cc + 8);
         tmem_ld_wait();
-        double res[8];
-        bool odd = false;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-          bool o;
-          res[j] = emu::compose(emu::group_h(v[0][j], v[1][j], v[2][j]), Lv[cc + j],
-                                ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62, &o);
-          odd |= o;
+          int sh;
+          Xv[cc + j] = emu::fold(emu::group_h(v[0][j], v[1][j], v[2][j]), Xv[cc + j], sh);
+          smask |= (uint32_t)(sh >> 3) << (cc + j);
         }
-        if (odd) {  // a result outside the normal FP64 range (extreme scales only)
-#pragma unroll
-          for (int j = 0; j < 8; ++j)
-            res[j] = emu::compose_slow(emu::group_h(v[0][j], v[1][j], v[2][j]), Lv[cc + j],
-                                       ea + s_cexp[pass * 64 + h * 32 + cc + j] - 62);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int col = pass * 64 + h * 32 + cc + j;
-          if (row_ok && col < ncols && (!syrk || r >= col)) __stcg(C + r + (long long)col * V.ld, cur[j] - res[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) cur[j] = nxt[j];
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&bars.free_h));
+      // per chunk of four columns: C (in L2 by then: warp 10) read, X 2^(s + ea + eb - 62) subtracted,
+      // C stored
+#pragma unroll
+      for (int cc = 0; cc < 32; cc += 4) {
+        const int c0 = pass * 64 + h * 32 + cc;
+        const int4 eb = *(const int4*)(s_cexp + c0);
+        const int ebv[4] = {eb.x, eb.y, eb.z, eb.w};
+        double cv[4], res[4];
+        bool in[4], odd = false;
+        int sE[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          in[j] = row_ok && c0 + j < ncols && (!syrk || r >= c0 + j);
+          cv[j] = in[j] ? __ldcg(C + r + (long long)(c0 + j) * V.ld) : 0.0;
+          sE[j] = ea - 62 + ebv[j] + (int)((smask >> (cc + j)) & 1) * 8;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          bool o;
+          res[j] = emu::sub_scaled(cv[j], Xv[cc + j], sE[j], &o);
+          odd |= o && in[j];
+        }
+        if (odd) {  // extreme scales only
+#pragma unroll
+          for (int j = 0; j < 4; ++j) res[j] = emu::sub_wide(cv[j], Xv[cc + j], sE[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (in[j]) __stcg(C + r + (long long)(c0 + j) * V.ld, res[j]);
+      }
       ++pp.passes;
     }
   }
@@ -488,7 +507,7 @@ __global__ void __launch_bounds__(kEmu ? emuk::kThreadsEmu : kThreads, 1)
   __shared__ TaskKey s_key, s_next_key;
   __shared__ __align__(8) emuk::Bars bars;
   __shared__ uint32_t tmem_slot;
-  __shared__ int s_aux[2 * kBlk];
+  __shared__ __align__(16) int s_aux[2 * kBlk];
   const BlockView& V = P.V;
   const int NTb = P.NTb;
   const int warp = threadIdx.x >> 5;
