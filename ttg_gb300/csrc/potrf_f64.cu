@@ -192,7 +192,8 @@ __device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey
 // once this task's last products are out).
 // The emulated executor runs 384 threads (twelve warps); its FP64 tasks use the first 256.
 //   warp 8 lane 0  TMA producer: per phase and chunk the phase's B planes (64 rows each) into one
-//                  of two buffers, then its A planes (128 rows each) through a ring of six slots
+//                  of two buffers, then its A planes (128 rows each) through a ring of seven slots
+//                  (which fills the 227 KB of shared memory a CTA can have)
 //   warp 9 lane 0  MMA issuer: per phase and chunk, for each A plane i and k-step, one MMA of
 //                  M128 x N(64 x planes) x K16 against all the B planes j of the phase's groups
 //                  i + j: the B planes of a chunk are consecutive 64-row blocks of one K-major tile
@@ -205,7 +206,7 @@ __device__ __forceinline__ bool dag_deps_ready(const DagParams& P, const TaskKey
 //                  integer group sums L (after phase A) and X (after phase B), the rounding of X
 //                  and one FP64 subtraction from C
 namespace emuk {
-constexpr int kASlots = 6, kBBufs = 2;
+constexpr int kASlots = 7, kBBufs = 2;
 constexpr uint32_t kABytes = 128 * 128, kBBytes = 64 * 128;  // one plane chunk: rows x 128 bytes
 constexpr uint32_t kBSetBytes = emu::kSlices * kBBytes;
 constexpr size_t kSmemBytes = (size_t)kBBufs * kBSetBytes + (size_t)kASlots * kABytes + 1024;
@@ -275,7 +276,10 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
   int* err = &P.st->status;
   uint8_t* smB = smem;                               // [kBBufs][7][64 x 128 B]
   uint8_t* smA = smem + (size_t)kBBufs * kBSetBytes;  // [kASlots][128 x 128 B]
-  // column exponents of this task (rows of L(N,K)), before the roles split
+  // column exponents of this task (rows of L(N,K)), before the roles split; each epilogue thread's
+  // row exponent (row of L(M,K)) is read beside them
+  const int r_ep = threadIdx.x & (emu::kEdge - 1);
+  const int ea_ld = (warp < kEpiWarps && r_ep < V.dim(M)) ? __ldcg(P.rexp + tA * emu::kEdge + r_ep) : emu::kEmptyRow;
   if (threadIdx.x < emu::kEdge) s_cexp[threadIdx.x] = __ldcg(P.rexp + tB * emu::kEdge + threadIdx.x);
   __syncthreads();
   // one phase of one pass: the producer's loads (per 64-wide chunk of k the phase's B planes, 64
@@ -409,7 +413,7 @@ __device__ __forceinline__ void emu_update(const CUtensorMap* tmA, const CUtenso
     const int h = warp >> 2;                    // column half of each pass
     const int mrows = V.dim(M), ncols = V.dim(Nn);
     double* C = V.ptr(M, Nn);
-    const int ea = (r < mrows) ? __ldcg(P.rexp + tA * emu::kEdge + r) : emu::kEmptyRow;
+    const int ea = ea_ld;  // (r = r_ep)
     const bool row_ok = r < mrows && ea != emu::kEmptyRow;
     // the next task, while the first pass's products run (this warp waits for them otherwise)
     if (warp == kEpiWarps - 1 && lane == 0) prefetch_next(P, cur_task, pf);
