@@ -120,8 +120,9 @@ int gbx_dgemm_nn_tile(int m, int n, int k, const double* A, int lda, const doubl
 int gbx_dpotrf_tiled_bufferSize(int N, int NB, size_t* bytes);
 
 /* Block edge of the executor (the reference's tile tasks run as tasks on blocks inside the tiles):
- * 0 (default) = automatic, 64-blocks for N <= 4096 (a small matrix is bound by its chain of block
- * steps) and 128 above; 32, 64 or 128 forces that edge where it divides the tile (else the
+ * 0 (default) = automatic, 64-blocks for N <= 4096 with FP64 FMA updates and for N <= 2048 with the
+ * tensor-core updates (gbx_set_fp64_update; a small matrix is bound by its chain of block steps),
+ * 128 above; 32, 64 or 128 forces that edge where it divides the tile (else the
  * automatic edge). Applies to later gbx_dpotrf_tiled / gbx_dpotrs_tiled / bufferSize calls, which
  * must agree: size the workspace after setting it. Returns 0 or GBX_ERR_ARG. */
 int gbx_set_dag_block_edge(int b);

@@ -71,7 +71,7 @@ def test_argument_validation_without_gpu(gbx):
 
 def test_dag_block_edge_setting(gbx):
     """The executor's block edge: 0 (automatic), 32, 64 or 128; anything else is refused. The
-    workspace follows the edge (64-blocks for N <= 4096 by default: four times the counters)."""
+    workspace follows the edge (64-blocks for small N by default: four times the counters)."""
     L = gbx.lib()
     for bad in (-1, 16, 96, 256):
         assert L.gbx_set_dag_block_edge(bad) == gbx.GBX_ERR_ARG
@@ -84,6 +84,25 @@ def test_dag_block_edge_setting(gbx):
         assert b.value > a.value
     finally:
         assert L.gbx_set_dag_block_edge(0) == 0
+
+
+@pytest.mark.parametrize("mode,N,edge", [(0, 4096, 64), (0, 4608, 128), (1, 2048, 64), (1, 2560, 128),
+                                         (1, 4096, 128)])
+def test_automatic_block_edge_follows_update_mode(gbx, mode, N, edge):
+    """64-blocks up to N = 4096 with FP64 FMA updates, up to N = 2048 with the tensor-core updates:
+    the automatic workspace equals the one of the forced edge."""
+    L = gbx.lib()
+    a, b = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    try:
+        assert L.gbx_set_fp64_update(mode) == 0
+        assert L.gbx_set_dag_block_edge(0) == 0
+        assert L.gbx_dpotrf_tiled_bufferSize(N, 512, ctypes.byref(a)) == 0
+        assert L.gbx_set_dag_block_edge(edge) == 0
+        assert L.gbx_dpotrf_tiled_bufferSize(N, 512, ctypes.byref(b)) == 0
+        assert a.value == b.value
+    finally:
+        L.gbx_set_dag_block_edge(0)
+        L.gbx_set_fp64_update(0)
 
 
 def test_wait_timeout_setting(gbx):

@@ -985,16 +985,19 @@ int block_edge(int NB) {
 }
 
 // Block edge of the executor for an N x N matrix of NB tiles. A small matrix is bound by its chain
-// of block steps (each a single-CTA FP64 POTRF, TRSM and update of one block), so up to
-// g_small_n it takes 64-blocks: twice the steps, each about a quarter as long; larger matrices are
-// bound by the total work and keep 128-blocks, whose block GEMM runs the FP64 pipe best.
-int g_small_n = 4096;
+// of block steps (each a single-CTA FP64 POTRF, TRSM and update of one block), so up to a size it
+// takes 64-blocks: twice the steps, each about a quarter as long; larger matrices are bound by the
+// total work and keep 128-blocks, whose block GEMM runs the FP64 pipe best and which the
+// tensor-core updates need. That size: N = 4096 with FP64 FMA updates, N = 2048 with the
+// tensor-core updates (GB300, NB = 512: N=3072 11.7 ms with 128-blocks against 14.8 with 64,
+// N=4096 15.7 against 28.3; N=2048 7.70 against 7.60).
+extern int g_fp64_update;
 int g_forced_edge = 0;  // gbx_set_dag_block_edge
 int dag_block_edge(int N, int NB) {
   const int b = block_edge(NB);
   if (b == 0) return 0;
   if (g_forced_edge > 0) return (NB % g_forced_edge == 0 && g_forced_edge <= b) ? g_forced_edge : b;
-  return (b == kBlk && N <= g_small_n) ? 64 : b;
+  return (b == kBlk && N <= (g_fp64_update == 1 ? 2048 : 4096)) ? 64 : b;
 }
 
 size_t dag_workspace_bytes(int NTb) {
