@@ -15,12 +15,13 @@
 // a sum of at most 7 * 128 products of magnitude <= 2^14: below 2^24 in magnitude, so the tensor
 // cores' FP32 accumulation of these integers is exact. Then
 //     sum_k A B = X 2^(eA_r + eB_c - 62),   X = sum_{g=0..6} acc_g 2^(8(6-g))   (an integer < 2^70),
-// rounded once to FP64 from X with integer instructions, and subtracted from C with one FP64 add:
-// two roundings in all, against k of them for the FP64 dot product.
+// X formed in 64 bits (fold), rounded once to FP64 and subtracted from C by one FMA with the power
+// of two (sub_scaled): two roundings in all, against k of them for the FP64 dot product.
 //
 // Costs on GB300 (measured per SM per clock): FP64 add/FMA and every conversion to or from FP64
-// ~1.6-1.9, float->int ~15, integer ~60, FP32 ~113. Hence integer-only splitting and composing, and
-// a single FP64 operation per element of C per task.
+// ~1.6-1.9, float->int ~15, integer ~60, FP32 ~113. Hence integer-only splitting and folding, and
+// two FP64-pipe operations per element of C per task (the conversion of X and the FMA: a rounding
+// of X in integer instructions measured slower, ~30 of them per element).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
