@@ -1,6 +1,7 @@
 // Block operations of the tiled Cholesky, templated on the element type (double for the FP64
 // path, float for the working precision of the mixed path). One CTA of 256 threads per call.
 #pragma once
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace gbx {
@@ -300,15 +301,76 @@ __device__ int op_potrf(T* A, int lda, int n, T* sm) {
     ops_sync<kNamed>();
     info = *flag;
     if (info) break;
-    // rows below the block: each thread solves one row in registers
-    for (int r = p0 + pw + tid; r < n; r += kThreads) {
-      T x[32];
+    // rows below the block: X := X L_d^{-T}
+    const int rb = p0 + pw, ng = (n - rb + 31) >> 5;  // rows rb..n-1 in groups of 32 (<= 3)
+    if (sizeof(T) == 8 && ng > 0 && n <= 64) {
+      // FP64 blocks of at most 64: the columns dealt to the eight warps (column c to warp c % 8),
+      // all rows in each (lane = row of a group), right-looking: per column j its owner scales x_j
+      // by the reciprocal and stores it, one barrier, then every warp subtracts it from its later
+      // columns (a warp's smallest column above j first: the next owner's). One row per thread
+      // leaves the 32 rows on one sub-partition's FP64 pipe (GB300, N=2048 with 64-blocks: 7.23
+      // -> 7.10 ms). On 128-blocks the 32 barriers per panel cost more than the balance gains
+      // (N=8192 32.6 -> 34.4 ms), so they keep the per-row solve.
+      const T* Ld = S + p0 + kBlk * p0;
+      T xv[3][4];  // [row group][column j = warp + 8 q]
 #pragma unroll
-      for (int c = 0; c < 32; ++c) x[c] = c < pw ? S[r + kBlk * (p0 + c)] : T(0);
-      row_solve32<T>(x, S + p0 + kBlk * p0, kBlk, pw, S + p0 + kBlk * p0);
+      for (int g = 0; g < 3; ++g)
 #pragma unroll
-      for (int c = 0; c < 32; ++c)
-        if (c < pw) S[r + kBlk * (p0 + c)] = x[c];
+        for (int q = 0; q < 4; ++q) {
+          const int r = rb + 32 * g + lane, c = warp + 8 * q;
+          xv[g][q] = (g < ng && r < n && c < pw) ? S[r + kBlk * (p0 + c)] : T(0);
+        }
+      for (int j = 0; j < pw; ++j) {
+        if (warp == (j & 7)) {
+          const T rj = Ld[rinv_at(j, kBlk)];
+          auto own = [&](auto qc) {
+            constexpr int q = decltype(qc)::value;
+#pragma unroll
+            for (int g = 0; g < 3; ++g)
+              if (g < ng) {
+                const int r = rb + 32 * g + lane;
+                xv[g][q] *= rj;
+                if (r < n) S[r + kBlk * (p0 + j)] = xv[g][q];
+              }
+          };
+          switch (j >> 3) {
+            case 0: own(std::integral_constant<int, 0>{}); break;
+            case 1: own(std::integral_constant<int, 1>{}); break;
+            case 2: own(std::integral_constant<int, 2>{}); break;
+            default: own(std::integral_constant<int, 3>{}); break;
+          }
+        }
+        ops_sync<kNamed>();
+        if (j + 1 < pw) {
+          T xj[3];
+#pragma unroll
+          for (int g = 0; g < 3; ++g) {
+            const int r = rb + 32 * g + lane;
+            xj[g] = (g < ng && r < n) ? S[r + kBlk * (p0 + j)] : T(0);
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int c = warp + 8 * q;
+            if (c > j && c < pw) {
+              const T l = Ld[c + kBlk * j];
+#pragma unroll
+              for (int g = 0; g < 3; ++g)
+                if (g < ng) xv[g][q] = fma(-l, xj[g], xv[g][q]);
+            }
+          }
+        }
+      }
+    } else {
+      // each thread solves one row in registers
+      for (int r = rb + tid; r < n; r += kThreads) {
+        T x[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) x[c] = c < pw ? S[r + kBlk * (p0 + c)] : T(0);
+        row_solve32<T>(x, S + p0 + kBlk * p0, kBlk, pw, S + p0 + kBlk * p0);
+#pragma unroll
+        for (int c = 0; c < 32; ++c)
+          if (c < pw) S[r + kBlk * (p0 + c)] = x[c];
+      }
     }
     ops_sync<kNamed>();
     // trailing update S(i, c) -= sum_k S(i, k) S(c, k), p0+pw <= c <= i < n
