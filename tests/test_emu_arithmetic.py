@@ -5,7 +5,9 @@ with Python integers and checked against exact rationals (CPU):
   * products: group sums acc_g = sum_{i+j=g} sum_k a_i b_j for g <= 6 stay below 2^24 in magnitude
     for k = 128 (exact in the tensor cores' FP32 accumulation);
   * composition: X = H 2^32 + L in 64 bits (X 2^-8 when |H| >= 2^30), rounded once to FP64 and
-    scaled by a power of two.
+    scaled by a power of two;
+  * subtraction from C: one FMA with 2^sE, or with two clamped normal powers of two where 2^sE is
+    not normal, rounded once for |sE| <= 2044 and the right limit beyond.
 The emulated dot product must be at least as accurate as a plain FP64 loop over the same inputs."""
 import math
 import struct
@@ -100,3 +102,46 @@ def test_zero_and_subnormal_rows():
     assert emulated_dot(np.zeros(128), np.ones(128)) == 0.0
     tiny = np.full(128, 5e-324)
     assert emulated_dot(tiny, np.ones(128)) == 0.0  # subnormal rows carry no digits
+
+
+def _round(q):
+    """A rational rounded to FP64 (to nearest even; float(Fraction) rounds correctly)."""
+    try:
+        return float(q)
+    except OverflowError:
+        return math.inf if q > 0 else -math.inf
+
+
+def _sub_scaled(c, X, sE):
+    """c - X 2^sE as the executor forms it (emu_f64.cuh): X rounded to FP64, then one FMA with
+    2^sE, or, when 2^sE is not a normal FP64 number, with 2^a 2^b (a = sE / 2 truncated, both
+    clamped to the normal exponents) after the exact product X 2^a."""
+    x = float(X)
+    if -1022 <= sE <= 1023:
+        return _round(Fraction(c) - Fraction(x) * Fraction(2) ** sE)
+    a = min(max(int(sE / 2), -1022), 1023)
+    b = min(max(sE - a, -1022), 1023)
+    p = x * 2.0 ** a if a >= 0 else x / 2.0 ** -a  # exact: |x| >= 1 and a >= -1022
+    assert math.isinf(p) or Fraction(p) == Fraction(x) * Fraction(2) ** a
+    if math.isinf(p):
+        return -p if c == c else c
+    return _round(Fraction(c) - Fraction(p) * Fraction(2) ** b)
+
+
+@pytest.mark.parametrize("sE", [-2150, -2044, -1600, -1100, -1075, -1074, -1060, -1023, -1022, -500, 0,
+                                900, 1023, 1024, 1500, 2046, 2200])
+def test_scaled_subtraction_rounds_once(sE):
+    """c - X 2^sE: the value rounded once from the exact c - fl(X) 2^sE wherever |sE| <= 2044
+    (subnormal and overflowing results included), and the right limit beyond."""
+    rng = np.random.default_rng(sE & 0xffff)
+    for _ in range(200):
+        X = int(rng.integers(1, 2 ** 62)) * int(rng.choice([-1, 1]))
+        x = float(X)
+        for c in (0.0, 1.5, -3.25e-300, 7e-310, 2.0 ** -1074, 1e300):
+            got = _sub_scaled(c, X, sE)
+            if abs(sE) <= 2044:
+                assert got == _round(Fraction(c) - Fraction(x) * Fraction(2) ** sE)
+            elif sE < 0:  # X 2^sE below half the smallest subnormal: c itself
+                assert got == c
+            else:
+                assert math.isinf(got) and (got < 0) == (X > 0)
